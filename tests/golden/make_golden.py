@@ -1,0 +1,220 @@
+"""Generate the golden fixtures by running the reference plugin itself.
+
+The reference (team-ocean/veris) is pure Python over the Veros operator API.
+Veros is not installed here, so ``veros_shim/`` supplies the few Veros entry
+points the plugin imports (single-process NumPy semantics); the plugin's own
+``veris/*.py`` files then run unchanged, in float64 NumPy.
+
+Usage (in a container that holds the reference checkout):
+
+    python tests/golden/make_golden.py [--reference PATH]
+
+It writes one ``<case>.npz`` per case next to this script:
+
+* ``in.<var>``: the initial state;
+* ``settings``: the settings as a JSON string;
+* ``seq.<kk>.<routine>.<output>``: the outputs of every call of one or more
+  sea-ice steps, in the order of the reference setup's step
+  (veris/setup/seaice_global_4deg/seaice_global_4deg.py:878-932), with the
+  five-value ``IceVelocities`` result unpacked in full and the stresses stored
+  back into the state;
+* ``sub.<routine>.<output>``: single calls of the inner routines
+  (strain rates, viscosities, drag coefficients, stress divergence, fluxes,
+  limiter, solve4temp, one EVP subcycle) on the state after the dynamics
+  preparation of the first step.
+
+The fixtures are the parity anchor for the oracle (tests/test_oracle_golden.py)
+and for the GPU kernels (tests/test_gpu_parity.py).
+"""
+import argparse
+import copy
+import json
+import os
+import sys
+from types import SimpleNamespace
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+
+CASES = {
+    # the first workload verbatim: 90x40 at 4 deg, dt 3600 s, 120 subcycles, from rest
+    "c1": dict(grid=dict(nx=90, ny=40, seed=0), config="c1_4deg", steps=2, overrides={}),
+    # moving ice with stresses, basal drag on, turning angles on
+    "moving": dict(grid=dict(nx=36, ny=20, seed=1, init_velocity=0.2, init_stress=3000.0,
+                             ice_lat=30.0),
+                   config="c1_4deg", steps=2,
+                   overrides=dict(nEVPsteps=30, basalDragK2=15.0, airTurnAngle=20.0,
+                                  waterTurnAngle=15.0, sinWat=float(np.sin(np.deg2rad(15.0))),
+                                  cosWat=float(np.cos(np.deg2rad(15.0))))),
+    # odd sizes, free-slip side drag, adaptive EVP, absolute wind, sea-ice load,
+    # doubly periodic halo fill, ice everywhere
+    "small_a": dict(grid=dict(nx=21, ny=13, seed=2, init_velocity=0.1, init_stress=1000.0,
+                              ice_lat=0.0),
+                    config="c1_4deg", steps=1, sea_ice_load=True,
+                    overrides=dict(nEVPsteps=10, noSlip=False, useAdaptiveEVP=True,
+                                   useRelativeWind=False, useRealFreshWaterFlux=True,
+                                   veros_fill=False)),
+    # second-order no-slip terms, non-periodic x, wet y halo, an all-land row,
+    # tensile strength
+    "small_b": dict(grid=dict(nx=21, ny=13, seed=3, init_velocity=0.1, init_stress=1000.0,
+                              ice_lat=20.0, land_fraction=0.4, wet_y_halo=True,
+                              land_rows=(5,)),
+                    config="c1_4deg", steps=1,
+                    overrides=dict(nEVPsteps=10, secondOrderBC=True, enable_cyclic_x=False,
+                                   tensileStrFac=0.05)),
+    # no ice anywhere
+    "noice": dict(grid=dict(nx=16, ny=10, seed=4, ice_lat=90.0),
+                  config="c1_4deg", steps=1, overrides=dict(nEVPsteps=5)),
+}
+
+
+def _import_reference(ref):
+    sys.path[:0] = [os.path.join(HERE, "veros_shim"), ref, REPO]
+    import veris.area_mass as area_mass
+    import veris.dynsolver as dynsolver
+    import veris.dynamics_routines as dyn
+    import veris.averaging as averaging
+    import veris.evp_solver as evp
+    import veris.ocean_stress as ocean_stress
+    import veris.advection as advection
+    import veris.clean_up as clean_up
+    import veris.growth as growth
+    import veris.solve4temp as s4t
+    import veris.fill_overlap as fo
+    return SimpleNamespace(area_mass=area_mass, dynsolver=dynsolver, dyn=dyn,
+                           averaging=averaging, evp=evp, ocean_stress=ocean_stress,
+                           advection=advection, clean_up=clean_up, growth=growth,
+                           s4t=s4t, fo=fo)
+
+
+def _state(arrays, sett):
+    return SimpleNamespace(variables=SimpleNamespace(**{k: v.copy() for k, v in arrays.items()}),
+                           settings=sett)
+
+
+def _record(out, key, names, values):
+    if not isinstance(values, tuple):
+        values = (values,)
+    assert len(names) == len(values), (key, len(values))
+    for n, val in zip(names, values):
+        out[f"{key}.{n}"] = np.array(val, dtype=np.float64)
+        yield n, val
+
+
+def run_case(R, case):
+    from veris_gb300.synthetic import make_state, config_settings
+
+    arrays = make_state(**case["grid"])
+    if case.get("sea_ice_load"):
+        rng = np.random.default_rng(99)
+        arrays["SeaIceLoad"] = 900.0 * rng.random(arrays["hIceMean"].shape)
+    sett = config_settings(case["config"], **case["overrides"])
+    out = {f"in.{k}": v.copy() for k, v in arrays.items()}
+    out["settings"] = np.array(json.dumps(vars(sett), sort_keys=True))
+    state = _state(arrays, sett)
+    vs = state.variables
+    seq = 0
+
+    def call(name, names, fn):
+        nonlocal seq
+        vals = fn(state)
+        key = f"seq.{seq:02d}.{name}"
+        seq += 1
+        for n, val in _record(out, key, names, vals):
+            setattr(vs, n, np.array(val, dtype=np.float64).copy())
+
+    for step in range(case["steps"]):
+        call("SeaIceMass", ("SeaIceMassC", "SeaIceMassU", "SeaIceMassV"), R.area_mass.SeaIceMass)
+        call("AreaWS", ("AreaW", "AreaS"), R.area_mass.AreaWS)
+        call("WindForcingXY", ("WindForcingX", "WindForcingY"), R.dynsolver.WindForcingXY)
+        call("SeaIceStrength", ("SeaIceStrength",), R.dyn.SeaIceStrength)
+        if step == 0:
+            _inner_routines(R, state, out)
+        call("IceVelocities", ("uIce", "vIce", "sigma1", "sigma2", "sigma12"),
+             R.dynsolver.IceVelocities)
+        call("OceanStressUV", ("OceanStressU", "OceanStressV"), R.ocean_stress.OceanStressUV)
+        if step == 0:
+            _advection_routines(R, state, out)
+        call("Advection", ("hIceMean", "hSnowMean", "Area"), R.advection.Advection)
+        call("clean_up_advection",
+             ("hIceMean", "hSnowMean", "Area", "TSurf", "os_hIceMean", "os_hSnowMean"),
+             R.clean_up.clean_up_advection)
+        call("ridging", ("Area",), R.clean_up.ridging)
+        if step == 0:
+            _thermo_routines(R, state, out)
+        call("Growth", ("hIceMean", "hSnowMean", "Area", "TSurf", "EmPmR",
+                        "forc_salt_surface_ice", "Qsw", "Qnet", "SeaIceLoad",
+                        "IcePenetSW", "recip_hIceMean"), R.growth.Growth)
+        for n in ("hIceMean", "hSnowMean", "Area", "forc_salt_surface_ice", "Qnet"):
+            call("fill_overlap", (n,), lambda st, n=n: R.fo.fill_overlap(st, getattr(vs, n).copy()))
+    return out
+
+
+def _inner_routines(R, state, out):
+    vs = state.variables
+    rec = lambda key, names, vals: list(_record(out, "sub." + key, names, vals))
+    u, v = vs.uIce.copy(), vs.vIce.copy()
+    e11, e22, e12 = R.dyn.strainrates(state, u, v)
+    rec("strainrates", ("e11", "e22", "e12"), (e11, e22, e12))
+    zeta, eta, press = R.dyn.viscosities(state, e11, e22, e12)
+    rec("viscosities", ("zeta", "eta", "press"), (zeta, eta, press))
+    rec("c_point_to_z_point", ("zetaZ",), R.averaging.c_point_to_z_point(state, zeta))
+    rec("ocean_drag_coeffs", ("cDrag",), R.dyn.ocean_drag_coeffs(state, u, v))
+    rec("basal_drag_coeffs", ("cBot",), R.dyn.basal_drag_coeffs(state, u, v))
+    rec("side_drag", ("SideDragU", "SideDragV"), R.dyn.side_drag(state, u, v))
+    rec("stressdiv", ("stressDivX", "stressDivY"),
+        R.dyn.stressdiv(state, vs.sigma1.copy(), vs.sigma2.copy(), vs.sigma12.copy()))
+    rec("tauXY", ("tauX", "tauY"), R.dynsolver.tauXY(state))
+    one = copy.copy(state.settings)
+    one.nEVPsteps = 1
+    st1 = SimpleNamespace(variables=vs, settings=one)
+    rec("evp_1", ("uIce", "vIce", "sigma1", "sigma2", "sigma12"), R.evp.evp_solver(st1))
+
+
+def _advection_routines(R, state, out):
+    vs = state.variables
+    sett = state.settings
+    rec = lambda key, names, vals: list(_record(out, "sub." + key, names, vals))
+    uTrans = vs.uIce * vs.dyG * vs.iceMaskU
+    vTrans = vs.vIce * vs.dxG * vs.iceMaskV
+    rec("calc_ZonalFlux", ("ZonalFlux",),
+        R.advection.calc_ZonalFlux(state, vs.hIceMean.copy(), uTrans))
+    rec("calc_MeridionalFlux", ("MeridionalFlux",),
+        R.advection.calc_MeridionalFlux(state, vs.hIceMean.copy(), vTrans))
+    rec("calc_Advection", ("field",), R.advection.calc_Advection(state, vs.Area.copy()))
+    cr = np.linspace(-3.0, 4.0, 141)
+    out["sub.limiter.Cr"] = cr
+    rec("limiter", ("phi",), R.advection.limiter(cr))
+
+
+def _thermo_routines(R, state, out):
+    vs = state.variables
+    sett = state.settings
+    rec = lambda key, names, vals: list(_record(out, "sub." + key, names, vals))
+    hI = np.maximum(vs.hIceMean * 1.3, 0.05) * (vs.hIceMean > 0)
+    hS = vs.hSnowMean * 1.3
+    TempFrz = sett.tempFrz + sett.dtempFrz_dS * vs.ocSalt + sett.celsius2K
+    out["sub.solve4temp.in_hIceActual"] = hI
+    out["sub.solve4temp.in_hSnowActual"] = hS
+    rec("solve4temp", ("TSurfOut", "F_io_net", "F_ia_net", "IcePenetSW", "FWsublim"),
+        R.s4t.solve4temp(state, hI, hS, vs.TSurf.copy(), TempFrz))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--reference", default=os.environ.get("VERIS_REFERENCE", "/root/reference"))
+    ap.add_argument("--cases", nargs="*", default=list(CASES))
+    args = ap.parse_args()
+    np.seterr(all="ignore")    # the reference's where() evaluates both branches
+    R = _import_reference(args.reference)
+    for name in args.cases:
+        out = run_case(R, CASES[name])
+        path = os.path.join(HERE, f"{name}.npz")
+        np.savez_compressed(path, **out)
+        print(f"{path}: {len(out)} arrays, {os.path.getsize(path) / 1e6:.2f} MB")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,106 @@
+"""The CPU oracle against the golden fixtures made by running the reference.
+
+The oracle restates the reference's arithmetic in its order of operations, so
+the bar here is bit-exact equality (NaN == NaN never occurs: the fixtures are
+finite).
+"""
+import numpy as np
+import pytest
+
+from oracle import veris_oracle as O
+from tests import golden_io as G
+
+
+@pytest.mark.parametrize("case", G.CASES)
+def test_step_sequence_bit_exact(case):
+    g = G.load(case)
+    st = G.initial_state(g)
+    seq = G.sequence(g)
+    got = []
+    n_steps = sum(1 for _i, r, _o in seq if r == "SeaIceMass")
+    for _ in range(n_steps):
+        O.step(st, record=lambda name, outs: got.append((name, outs)))
+    assert [r for _i, r, _o in seq] == [name for name, _o in got]
+    for (i, r, ref), (_n, outs) in zip(seq, got):
+        for k, a in ref.items():
+            np.testing.assert_array_equal(outs[k], a, err_msg=f"{case} call {i} {r}.{k}")
+
+
+@pytest.mark.parametrize("case", G.CASES)
+def test_inner_routines_bit_exact(case):
+    g = G.load(case)
+    first_evp = [i for i, r, _o in G.sequence(g) if r == "IceVelocities"][0]
+    st = G.state_before(g, first_evp)
+    v = st.variables
+    u, vv = v.uIce, v.vIce
+    e11, e22, e12 = O.strainrates(st, u, vv)
+    ref = G.sub(g, "strainrates")
+    for k, a in zip(("e11", "e22", "e12"), (e11, e22, e12)):
+        np.testing.assert_array_equal(a, ref[k], err_msg=k)
+    zeta, eta, press = O.viscosities(st, ref["e11"], ref["e22"], ref["e12"])
+    ref = G.sub(g, "viscosities")
+    for k, a in zip(("zeta", "eta", "press"), (zeta, eta, press)):
+        np.testing.assert_array_equal(a, ref[k], err_msg=k)
+    np.testing.assert_array_equal(O.c_point_to_z_point(st, ref["zeta"]),
+                                  G.sub(g, "c_point_to_z_point")["zetaZ"])
+    np.testing.assert_array_equal(O.ocean_drag_coeffs(st, u, vv), G.sub(g, "ocean_drag_coeffs")["cDrag"])
+    np.testing.assert_array_equal(O.basal_drag_coeffs(st, u, vv), G.sub(g, "basal_drag_coeffs")["cBot"])
+    sU, sV = O.side_drag(st, u, vv)
+    ref = G.sub(g, "side_drag")
+    np.testing.assert_array_equal(sU, ref["SideDragU"])
+    np.testing.assert_array_equal(sV, ref["SideDragV"])
+    dX, dY = O.stressdiv(st, v.sigma1, v.sigma2, v.sigma12)
+    ref = G.sub(g, "stressdiv")
+    np.testing.assert_array_equal(dX, ref["stressDivX"])
+    np.testing.assert_array_equal(dY, ref["stressDivY"])
+    tX, tY = O.tauXY(st)
+    ref = G.sub(g, "tauXY")
+    np.testing.assert_array_equal(tX, ref["tauX"])
+    np.testing.assert_array_equal(tY, ref["tauY"])
+    out = O.evp_solver(st, n=1)
+    ref = G.sub(g, "evp_1")
+    for k, a in zip(("uIce", "vIce", "sigma1", "sigma2", "sigma12"), out):
+        np.testing.assert_array_equal(a, ref[k], err_msg=k)
+
+
+@pytest.mark.parametrize("case", G.CASES)
+def test_advection_and_thermo_routines_bit_exact(case):
+    g = G.load(case)
+    seq = G.sequence(g)
+    adv = [i for i, r, _o in seq if r == "Advection"][0]
+    st = G.state_before(g, adv)
+    v = st.variables
+    uT = v.uIce * v.dyG * v.iceMaskU
+    vT = v.vIce * v.dxG * v.iceMaskV
+    np.testing.assert_array_equal(O.calc_ZonalFlux(st, v.hIceMean.copy(), uT),
+                                  G.sub(g, "calc_ZonalFlux")["ZonalFlux"])
+    np.testing.assert_array_equal(O.calc_MeridionalFlux(st, v.hIceMean.copy(), vT),
+                                  G.sub(g, "calc_MeridionalFlux")["MeridionalFlux"])
+    np.testing.assert_array_equal(O.calc_Advection(st, v.Area.copy()),
+                                  G.sub(g, "calc_Advection")["field"])
+    lim = G.sub(g, "limiter")
+    np.testing.assert_array_equal(O.limiter(lim["Cr"]), lim["phi"])
+
+    gr = [i for i, r, _o in seq if r == "Growth"][0]
+    st = G.state_before(g, gr)
+    v, s = st.variables, st.settings
+    ref = G.sub(g, "solve4temp")
+    TempFrz = s.tempFrz + s.dtempFrz_dS * v.ocSalt + s.celsius2K
+    out = O.solve4temp(st, ref["in_hIceActual"], ref["in_hSnowActual"], v.TSurf, TempFrz)
+    for k, a in zip(("TSurfOut", "F_io_net", "F_ia_net", "IcePenetSW", "FWsublim"), out):
+        np.testing.assert_array_equal(a, ref[k], err_msg=k)
+
+
+def test_limiter_range():
+    cr = np.linspace(-50, 50, 10001)
+    phi = O.limiter(cr)
+    assert phi.min() >= 0 and phi.max() <= 2
+
+
+def test_fill_overlap_idempotent():
+    g = G.load("c1")
+    st = G.initial_state(g)
+    a = np.random.default_rng(0).random(st.variables.iceMask.shape)
+    once = O.fill_overlap(st, a.copy())
+    twice = O.fill_overlap(st, once.copy())
+    np.testing.assert_array_equal(once, twice)
