@@ -1,0 +1,270 @@
+/*
+ * veris_gb300.h - C ABI of the GB300 sea-ice step.
+ *
+ * One GPU, device pointers only.  Every entry point:
+ *   - takes the grid (VerisGrid), the settings (VerisParams) and the state
+ *     fields (VerisFieldsF64 / VerisFieldsF32: one device pointer per state
+ *     variable, named as the plugin's variables, veris/variables.py:7-105);
+ *   - writes its results into caller-allocated device arrays of the same
+ *     2-D shape (functional style: inputs are never modified, as the
+ *     reference's kernels return new arrays);
+ *   - allocates nothing: scratch space is passed in as a workspace whose
+ *     size the matching *_workspace_bytes() function returns;
+ *   - enqueues its kernels on the given CUDA stream and returns a status
+ *     code without synchronising.
+ *
+ * Arrays are 2-D, (nx + 2*olx) x (ny + 2*oly), x-major (y contiguous), with a
+ * row pitch of `ld` elements.  Halos are 2 cells wide (olx = oly = 2, the
+ * plugin's default, veris/settings.py:9-10).  Neighbour access wraps
+ * periodically over the padded array in both axes, as the reference's
+ * `roll` does; the halo fill (veris/fill_overlap.py) then refreshes the
+ * halos where the reference does.
+ *
+ * Each declaration names the reference routine it replaces (file:line in
+ * team-ocean/veris).
+ */
+#ifndef VERIS_GB300_H
+#define VERIS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* a cudaStream_t; NULL is the legacy default stream */
+typedef void *veris_stream_t;
+
+enum VerisStatus {
+    VERIS_OK = 0,
+    VERIS_ERR_SHAPE = 1,       /* bad grid sizes, halo widths or pitch */
+    VERIS_ERR_ALIGN = 2,       /* a pointer or pitch breaks an alignment rule */
+    VERIS_ERR_NAN = 3,         /* a non-finite value was detected */
+    VERIS_ERR_TIMEOUT = 4,     /* a bounded device-side wait gave up */
+    VERIS_ERR_LAUNCH = 5,      /* a CUDA launch or API call failed */
+    VERIS_ERR_ARG = 6,         /* a NULL pointer or an invalid argument */
+    VERIS_ERR_UNSUPPORTED = 7, /* settings this entry point does not cover */
+    VERIS_ERR_WORKSPACE = 8    /* workspace missing or too small */
+};
+
+typedef struct {
+    int32_t nx, ny;   /* interior size */
+    int32_t olx, oly; /* halo widths (must be 2) */
+    int64_t ld;       /* elements between x and x+1; >= ny + 2*oly */
+} VerisGrid;
+
+/*
+ * Settings (veris/settings.py:4-176) as a flat POD struct.  The fields
+ * marked "derived" are computed by the host from other settings exactly as
+ * the reference computes them in Python, so that both sides round alike.
+ */
+#define VERIS_PARAM_DOUBLES(X)                                                        \
+    X(deltatTherm) X(recip_deltatTherm) X(deltatDyn) X(recip_deltatDyn)               \
+    X(evpAlpha) X(evpBeta) X(aEVPalphaMin) X(EVPcFac)                                 \
+    X(rhoIce) X(rhoFresh) X(rhoSea) X(rhoAir) X(rhoSnow)                              \
+    X(recip_rhoFresh) X(recip_rhoSea) X(rhoIce2rhoSnow) X(rhoIce2rhoFresh)            \
+    X(rhoFresh2rhoSnow)                                                               \
+    X(dryIceAlb) X(dryIceAlb_south) X(wetIceAlb) X(wetIceAlb_south)                   \
+    X(drySnowAlb) X(drySnowAlb_south) X(wetSnowAlb) X(wetSnowAlb_south)               \
+    X(wetAlbTemp) X(lhFusion) X(lhEvap) X(lhSublim) X(cpAir) X(cpWater)               \
+    X(stefBoltz) X(iceEmiss) X(snowEmiss) X(iceConduct) X(snowConduct) X(hCut)        \
+    X(shortwave) X(tempFrz) X(dtempFrz_dS) X(saltIce_ref) X(minLWdown) X(minTIce)    \
+    X(minTAir) X(dalton) X(Area_reg) X(hIce_reg) X(celsius2K) X(stantonNr)            \
+    X(uStarBase) X(McPheeTaperFac) X(recip_h0) X(recip_h0_south) X(recip_nITC)        \
+    X(sinWin) X(cosWin) X(sinWat) X(cosWat) X(sinWatOcn) X(cosWatOcn)                 \
+    X(wSpeedMin) X(hIce_min) X(Area_min) X(airIceDrag) X(airIceDrag_south)            \
+    X(waterIceDrag) X(waterIceDrag_south) X(cDragMin) X(seaIceLoadFac) X(gravity)     \
+    X(PlasDefCoeff) X(deltaMin) X(pressReplFac) X(pStar) X(cStar)                     \
+    X(basalDragU0) X(basalDragK1) X(basalDragK2) X(cBasalStar) X(tensileStrFac)       \
+    X(CrMax) X(sideDragCoeff) X(sideDragU0)                                           \
+    X(s4t_cc0) X(s4t_cc1) X(s4t_cc2) X(s4t_d1) X(s4t_d1i)
+
+#define VERIS_PARAM_INTS(X)                                                           \
+    X(nITC) X(noSlip) X(secondOrderBC) X(useRelativeWind) X(useRealFreshWaterFlux)    \
+    X(useAdaptiveEVP) X(veros_fill) X(enable_cyclic_x) X(use_coastline)              \
+    X(extensiveFld) X(nEVPsteps) X(pad_)
+
+#define VERIS_DECL_DOUBLE(name) double name;
+#define VERIS_DECL_INT(name) int32_t name;
+typedef struct {
+    VERIS_PARAM_DOUBLES(VERIS_DECL_DOUBLE)
+    VERIS_PARAM_INTS(VERIS_DECL_INT)
+} VerisParams;
+
+/* State variables carried by VerisFields*, in ABI order. */
+#define VERIS_FIELDS(X)                                                               \
+    X(hIceMean) X(hSnowMean) X(Area) X(TSurf) X(uIce) X(vIce)                         \
+    X(sigma1) X(sigma2) X(sigma12)                                                    \
+    X(SeaIceMassC) X(SeaIceMassU) X(SeaIceMassV) X(SeaIceStrength)                    \
+    X(AreaW) X(AreaS) X(WindForcingX) X(WindForcingY)                                 \
+    X(os_hIceMean) X(os_hSnowMean) X(recip_hIceMean) X(SeaIceLoad) X(IcePenetSW)      \
+    X(OceanStressU) X(OceanStressV) X(forc_salt_surface_ice)                          \
+    X(uOcean) X(vOcean) X(theta) X(ocSalt) X(Qnet) X(Qsw) X(ssh_an) X(R_low)           \
+    X(uWind) X(vWind) X(wSpeed) X(surfPress) X(SWdown) X(LWdown) X(ATemp) X(aqh)      \
+    X(precip) X(snowfall) X(evap) X(runoff) X(EmPmR) X(saltflux)                      \
+    X(maskInC) X(maskInU) X(maskInV) X(iceMask) X(iceMaskU) X(iceMaskV)               \
+    X(k1AtC) X(k2AtC) X(k1AtZ) X(k2AtZ) X(Fu) X(Fv) X(fCori)                          \
+    X(dxC) X(dyC) X(dxG) X(dyG) X(dxU) X(dyU) X(dxV) X(dyV)                           \
+    X(recip_dxC) X(recip_dyC) X(recip_dxG) X(recip_dyG)                               \
+    X(recip_dxU) X(recip_dyU) X(recip_dxV) X(recip_dyV)                               \
+    X(rA) X(rAu) X(rAv) X(rAz) X(recip_rA) X(recip_rAu) X(recip_rAv) X(recip_rAz)
+
+#define VERIS_DECL_F64(name) const double *name;
+#define VERIS_DECL_F32(name) const float *name;
+typedef struct { VERIS_FIELDS(VERIS_DECL_F64) } VerisFieldsF64;
+typedef struct { VERIS_FIELDS(VERIS_DECL_F32) } VerisFieldsF32;
+
+/* ---- introspection (lets a binding check its struct layouts) ---------- */
+size_t veris_params_size(void);
+size_t veris_fields_count(void);
+const char *veris_field_name(size_t index);
+const char *veris_status_string(int status);
+/* 1 when the library was built for sm_103a and a device of that kind is usable */
+int veris_device_ok(void);
+
+/* ---- halo fill -------------------------------------------------------- */
+/* veris/fill_overlap.py:6-18 fill_overlap(state, A): in place on A */
+int veris_fill_overlap_f64(const VerisGrid *g, const VerisParams *p, double *A,
+                           veris_stream_t s);
+int veris_fill_overlap_f32(const VerisGrid *g, const VerisParams *p, float *A,
+                           veris_stream_t s);
+
+/* ---- dynamics preparation (once per step) ---------------------------- */
+/* veris/area_mass.py:17-28 SeaIceMass */
+int veris_sea_ice_mass_f64(const VerisGrid *g, const VerisParams *p,
+                           const VerisFieldsF64 *vs, double *SeaIceMassC,
+                           double *SeaIceMassU, double *SeaIceMassV, veris_stream_t s);
+/* veris/area_mass.py:5-14 AreaWS */
+int veris_area_ws_f64(const VerisGrid *g, const VerisParams *p, const VerisFieldsF64 *vs,
+                      double *AreaW, double *AreaS, veris_stream_t s);
+/* veris/dynsolver.py:7-47 tauXY */
+int veris_tau_xy_f64(const VerisGrid *g, const VerisParams *p, const VerisFieldsF64 *vs,
+                     double *tauX, double *tauY, veris_stream_t s);
+/* veris/dynsolver.py:50-84 WindForcingXY */
+int veris_wind_forcing_xy_f64(const VerisGrid *g, const VerisParams *p,
+                              const VerisFieldsF64 *vs, double *WindForcingX,
+                              double *WindForcingY, veris_stream_t s);
+/* veris/dynamics_routines.py:5-18 SeaIceStrength */
+int veris_sea_ice_strength_f64(const VerisGrid *g, const VerisParams *p,
+                               const VerisFieldsF64 *vs, double *SeaIceStrength,
+                               veris_stream_t s);
+
+/* ---- EVP building blocks (the inner routines, for parity and reuse) -- */
+/* veris/dynamics_routines.py:143-217 strainrates(state, uIce, vIce) */
+int veris_strainrates_f64(const VerisGrid *g, const VerisParams *p, const VerisFieldsF64 *vs,
+                          const double *uIce, const double *vIce, double *e11, double *e22,
+                          double *e12, veris_stream_t s);
+/* veris/dynamics_routines.py:220-268 viscosities(state, e11, e22, e12) */
+int veris_viscosities_f64(const VerisGrid *g, const VerisParams *p, const VerisFieldsF64 *vs,
+                          const double *e11, const double *e22, const double *e12,
+                          double *zeta, double *eta, double *press, veris_stream_t s);
+/* veris/averaging.py:4-19 c_point_to_z_point(state, Cfield, noSlip) */
+int veris_c_point_to_z_point_f64(const VerisGrid *g, const VerisParams *p,
+                                 const VerisFieldsF64 *vs, const double *Cfield,
+                                 int32_t noSlip, double *Zfield, veris_stream_t s);
+/* veris/dynamics_routines.py:21-52 ocean_drag_coeffs(state, uIce, vIce) */
+int veris_ocean_drag_coeffs_f64(const VerisGrid *g, const VerisParams *p,
+                                const VerisFieldsF64 *vs, const double *uIce,
+                                const double *vIce, double *cDrag, veris_stream_t s);
+/* veris/dynamics_routines.py:55-96 basal_drag_coeffs(state, uIce, vIce) */
+int veris_basal_drag_coeffs_f64(const VerisGrid *g, const VerisParams *p,
+                                const VerisFieldsF64 *vs, const double *uIce,
+                                const double *vIce, double *cBot, veris_stream_t s);
+/* veris/dynamics_routines.py:99-140 side_drag(state, uIce, vIce) */
+int veris_side_drag_f64(const VerisGrid *g, const VerisParams *p, const VerisFieldsF64 *vs,
+                        const double *uIce, const double *vIce, double *SideDragU,
+                        double *SideDragV, veris_stream_t s);
+/* veris/dynamics_routines.py:284-303 stressdiv(state, sig11, sig22, sig12) */
+int veris_stressdiv_f64(const VerisGrid *g, const VerisParams *p, const VerisFieldsF64 *vs,
+                        const double *sig11, const double *sig22, const double *sig12,
+                        double *stressDivX, double *stressDivY, veris_stream_t s);
+
+/* ---- the EVP solver (the hot loop) ----------------------------------- */
+/*
+ * veris/evp_solver.py:257-319 evp_solver(state) and its loop body :21-254:
+ * `n_subcycles` mEVP subcycles starting from vs->uIce, vIce, sigma1, sigma2,
+ * sigma12 (which are also u^{n-1}, v^{n-1}); results in the five outputs.
+ * Plain form: one tiled kernel per subcycle, halo fill fused into it.
+ */
+size_t veris_evp_workspace_bytes(const VerisGrid *g, int32_t elem_size);
+int veris_evp_solver_f64(const VerisGrid *g, const VerisParams *p, const VerisFieldsF64 *vs,
+                         int32_t n_subcycles, double *uIce, double *vIce, double *sigma1,
+                         double *sigma2, double *sigma12, void *workspace,
+                         size_t workspace_bytes, veris_stream_t s);
+int veris_evp_solver_f32(const VerisGrid *g, const VerisParams *p, const VerisFieldsF32 *vs,
+                         int32_t n_subcycles, float *uIce, float *vIce, float *sigma1,
+                         float *sigma2, float *sigma12, void *workspace,
+                         size_t workspace_bytes, veris_stream_t s);
+
+/* veris/ocean_stress.py:8-40 OceanStressUV */
+int veris_ocean_stress_uv_f64(const VerisGrid *g, const VerisParams *p,
+                              const VerisFieldsF64 *vs, double *OceanStressU,
+                              double *OceanStressV, veris_stream_t s);
+
+/* ---- advection -------------------------------------------------------- */
+/* veris/advection.py:170-175 limiter(Cr), elementwise over n values */
+int veris_limiter_f64(const double *Cr, double *phi, int64_t n, veris_stream_t s);
+/* veris/advection.py:94-129 calc_ZonalFlux(state, field, uTrans) */
+int veris_calc_zonal_flux_f64(const VerisGrid *g, const VerisParams *p,
+                              const VerisFieldsF64 *vs, const double *field,
+                              const double *uTrans, double *ZonalFlux, veris_stream_t s);
+/* veris/advection.py:132-167 calc_MeridionalFlux(state, field, vTrans) */
+int veris_calc_meridional_flux_f64(const VerisGrid *g, const VerisParams *p,
+                                   const VerisFieldsF64 *vs, const double *field,
+                                   const double *vTrans, double *MeridionalFlux,
+                                   veris_stream_t s);
+/* veris/advection.py:28-91 calc_Advection(state, field) */
+size_t veris_advection_workspace_bytes(const VerisGrid *g, int32_t elem_size);
+int veris_calc_advection_f64(const VerisGrid *g, const VerisParams *p,
+                             const VerisFieldsF64 *vs, const double *field, double *out,
+                             void *workspace, size_t workspace_bytes, veris_stream_t s);
+/* veris/advection.py:15-25 Advection(state): hIceMean, hSnowMean, Area */
+int veris_advection_f64(const VerisGrid *g, const VerisParams *p, const VerisFieldsF64 *vs,
+                        double *hIceMean, double *hSnowMean, double *Area, void *workspace,
+                        size_t workspace_bytes, veris_stream_t s);
+/* the same in float32 arithmetic, on a float32 field table */
+int veris_advection_f32(const VerisGrid *g, const VerisParams *p, const VerisFieldsF32 *vs,
+                        float *hIceMean, float *hSnowMean, float *Area, void *workspace,
+                        size_t workspace_bytes, veris_stream_t s);
+/* veris/clean_up.py:5-39 clean_up_advection(state) */
+int veris_clean_up_advection_f64(const VerisGrid *g, const VerisParams *p,
+                                 const VerisFieldsF64 *vs, double *hIceMean,
+                                 double *hSnowMean, double *Area, double *TSurf,
+                                 double *os_hIceMean, double *os_hSnowMean, veris_stream_t s);
+/* veris/clean_up.py:42-47 ridging(state) */
+int veris_ridging_f64(const VerisGrid *g, const VerisParams *p, const VerisFieldsF64 *vs,
+                      double *Area, veris_stream_t s);
+
+/* ---- thermodynamics (float64 throughout) ------------------------------ */
+/* veris/solve4temp.py:5-174 solve4temp(state, hIceActual, hSnowActual, TSurfIn, TempFrz) */
+int veris_solve4temp_f64(const VerisGrid *g, const VerisParams *p, const VerisFieldsF64 *vs,
+                         const double *hIceActual, const double *hSnowActual,
+                         const double *TSurfIn, const double *TempFrz, double *TSurfOut,
+                         double *F_io_net, double *F_ia_net, double *IcePenetSW,
+                         double *FWsublim, veris_stream_t s);
+/* veris/growth.py:8-397 Growth(state): the eleven outputs in the reference's order */
+int veris_growth_f64(const VerisGrid *g, const VerisParams *p, const VerisFieldsF64 *vs,
+                     double *hIceMean, double *hSnowMean, double *Area, double *TSurf,
+                     double *EmPmR, double *forc_salt_surface, double *Qsw, double *Qnet,
+                     double *SeaIceLoad, double *IcePenetSW, double *recip_hIceMean,
+                     veris_stream_t s);
+
+/* ---- reductions and conversions -------------------------------------- */
+/*
+ * veris/global_sum.py:1-4 is an identity on one process; this is the
+ * deterministic float64 sum of the interior of A (fixed-order tree), written
+ * to *result (device memory).  Workspace: veris_reduce_workspace_bytes().
+ */
+size_t veris_reduce_workspace_bytes(const VerisGrid *g);
+int veris_global_sum_f64(const VerisGrid *g, const double *A, const double *weight,
+                         double *result, void *workspace, size_t workspace_bytes,
+                         veris_stream_t s);
+/* elementwise precision conversion of n values */
+int veris_convert_f64_to_f32(const double *src, float *dst, int64_t n, veris_stream_t s);
+int veris_convert_f32_to_f64(const float *src, double *dst, int64_t n, veris_stream_t s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* VERIS_GB300_H */

@@ -1,0 +1,318 @@
+// The mEVP subcycle loop (veris/evp_solver.py:21-319), plain form: one tiled
+// kernel per subcycle.
+//
+// A CTA owns a TI x TJ tile of padded points (x rows by y columns, y
+// contiguous).  It recomputes the intermediates it needs on a thin ring
+// around the tile into shared memory, so one launch does the whole subcycle:
+//
+//   A  e12 (and rAz*e12^2) at Z points  [-1, TI+1] x [-1, TJ+1]
+//   B  e11, e22, Delta, zeta, press at C [-1, TI] x [-1, TJ]; on [-1, TI) x
+//      [-1, TJ) also the new sigma1/sigma2, sig11/sig22, the drag
+//      coefficients and the Coriolis terms at C
+//   C  zeta at Z and the new sigma12      [0, TI] x [0, TJ]
+//   D  stress divergence, forcing, implicit drag and the new u, v on the tile
+//
+// The new u, v are stored together with their periodic images in the halo
+// columns (and rows) that the reference's fill_overlap_uv refreshes
+// (veris/evp_solver.py:190).  Stresses are not halo-filled, as in the
+// reference.  Inputs and outputs alternate between the caller's output
+// arrays and the workspace (ping-pong), so no CTA reads a value another CTA
+// of the same launch writes.
+#include "stencil.cuh"
+
+namespace veris {
+
+constexpr int EVP_TI = 32, EVP_TJ = 32, EVP_THREADS = 256;
+
+template <class T>
+struct EvpIO {
+    const T *u, *v, *s1, *s2, *s12;   // state at the start of the subcycle
+    T *uo, *vo, *s1o, *s2o, *s12o;    // state at its end
+    const T *uNm1, *vNm1;             // velocities of the previous time step
+};
+
+template <class T>
+struct EvpSmem {
+    // widths of the regions
+    static constexpr int WZ = EVP_TJ + 3, HZ = EVP_TI + 3;   // stage A
+    static constexpr int WB = EVP_TJ + 2, HB = EVP_TI + 2;   // stage B (zeta, alphaC)
+    static constexpr int WC = EVP_TJ + 1, HC = EVP_TI + 1;   // R_C arrays and sigma12
+    static constexpr int NZ = WZ * HZ, NB = WB * HB, NC = WC * HC;
+    static constexpr int N_C_ARRAYS = 8;  // sig11 sig22 cd cb fvC fuC sp s12
+    static constexpr size_t bytes() {
+        return sizeof(T) * (size_t)(2 * NZ + 2 * NB + N_C_ARRAYS * NC);
+    }
+};
+
+template <class T, bool ADAPT, bool SIDE, bool BASAL>
+__global__ void __launch_bounds__(EVP_THREADS, 2)
+evp_subcycle_kernel(Ctx<T> c, HaloFill h, EvpIO<T> io) {
+    using S = EvpSmem<T>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *e12s = reinterpret_cast<T *>(smem_raw);
+    T *zqs = e12s + S::NZ;
+    T *zeta = zqs + S::NZ;
+    T *aCs = zeta + S::NB;
+    T *sig11 = aCs + S::NB;
+    T *sig22 = sig11 + S::NC;
+    T *cds = sig22 + S::NC;
+    T *cbs = cds + S::NC;
+    T *fvC = cbs + S::NC;
+    T *fuC = fvC + S::NC;
+    T *sps = fuC + S::NC;
+    T *s12s = sps + S::NC;
+
+    const Fields<T> &f = c.f;
+    const Dims &d = c.d;
+    const int i0 = blockIdx.y * EVP_TI, j0 = blockIdx.x * EVP_TJ;
+    const int tid = threadIdx.x;
+
+    // index helpers: stage A / B arrays are offset by one, R_C arrays by one,
+    // R_Z (sigma12) by zero
+#define ZA(li, lj) ((li) + 1) * S::WZ + ((lj) + 1)
+#define ZB(li, lj) ((li) + 1) * S::WB + ((lj) + 1)
+#define ZC(li, lj) ((li) + 1) * S::WC + ((lj) + 1)
+#define ZZ(li, lj) (li) * S::WC + (lj)
+
+    // ---- stage A: e12 at Z points
+    for (int idx = tid; idx < S::NZ; idx += EVP_THREADS) {
+        const int li = idx / S::WZ - 1, lj = idx % S::WZ - 1;
+        const int gi = i0 + li, gj = j0 + lj;
+        const T e = strain_z(c, io.u, io.v, gi, gj);
+        e12s[idx] = e;
+        zqs[idx] = c.ld(f.rAz, gi, gj) * (e * e);
+    }
+    __syncthreads();
+
+    // ---- stage B: viscosities and the C-point stress update
+    const T alpha = T(c.p.evpAlpha);
+    const T rdenom = T(1.0 / c.p.evpAlpha);
+    for (int idx = tid; idx < S::NB; idx += EVP_THREADS) {
+        const int li = idx / S::WB - 1, lj = idx % S::WB - 1;
+        const int gi = i0 + li, gj = j0 + lj;
+        T e11, e22;
+        strain_c(c, io.u, io.v, gi, gj, e11, e22);
+        T zt, et, pr, dl;
+        viscosity_c(c, gi, gj, e11, e22, zqs[ZA(li, lj)], zqs[ZA(li + 1, lj)], zqs[ZA(li, lj + 1)],
+                    zqs[ZA(li + 1, lj + 1)], zt, et, pr, dl);
+        zeta[idx] = zt;
+        const T mC = c.ld(f.iceMask, gi, gj);
+        T aC = alpha, d1 = rdenom;
+        if (ADAPT) {
+            const T mass = c.ld(f.SeaIceMassC, gi, gj);
+            aC = sqrt(zt * T(c.p.EVPcFac) / (mass > T(1e-4) ? mass : T(1e-4)) * c.ld(f.recip_rA, gi, gj)) * mC;
+            aC = aC > T(c.p.aEVPalphaMin) ? aC : T(c.p.aEVPalphaMin);
+            aCs[idx] = aC;
+            d1 = T(1.0) / aC;
+        }
+        if (li < EVP_TI && lj < EVP_TJ) {
+            const int k = ZC(li, lj);
+            const T ep = e11 + e22, em = e11 - e22;
+            const T div = T(2) * zt * ep - pr;
+            const T ten = T(2) * zt * em;
+            const T s1 = (c.ld(io.s1, gi, gj) * (aC - T(1)) + div) * d1 * mC;
+            const T s2 = (c.ld(io.s2, gi, gj) * (aC - T(1)) + ten * T(0.25)) * d1 * mC;
+            sig11[k] = T(0.5) * (s1 + s2);
+            sig22[k] = T(0.5) * (s1 - s2);
+            if (li >= 0 && lj >= 0 && gi < d.NX && gj < d.NY) {
+                const int64_t o = d.raw(gi, gj);
+                io.s1o[o] = s1;
+                io.s2o[o] = s2;
+            }
+            cds[k] = ocean_drag_c(c, io.u, io.v, gi, gj);
+            if (BASAL) cbs[k] = basal_drag_c(c, io.u, io.v, gi, gj);
+            const T mf = c.ld(f.SeaIceMassC, gi, gj) * c.ld(f.fCori, gi, gj) * T(0.5);
+            fvC[k] = mf * (c.ld(io.v, gi, gj) + c.ld(io.v, gi, gj + 1));
+            fuC[k] = mf * (c.ld(io.u, gi, gj) + c.ld(io.u, gi + 1, gj));
+            if (SIDE) sps[k] = ice_speed_c(c, io.u, io.v, gi, gj);
+        }
+    }
+    __syncthreads();
+
+    // ---- stage C: sigma12 at Z points
+    for (int idx = tid; idx < S::NC; idx += EVP_THREADS) {
+        const int li = idx / S::WC, lj = idx % S::WC;
+        const int gi = i0 + li, gj = j0 + lj;
+        const T zz = c2z_norm(c, gi, gj, true) *
+                     ((zeta[ZB(li, lj)] + zeta[ZB(li - 1, lj)]) + (zeta[ZB(li, lj - 1)] + zeta[ZB(li - 1, lj - 1)]));
+        T aZ = alpha, d2 = rdenom;
+        if (ADAPT) {
+            aZ = T(0.5) * (T(0.5) * (aCs[ZB(li, lj)] + aCs[ZB(li, lj - 1)]) +
+                           T(0.5) * (aCs[ZB(li - 1, lj)] + aCs[ZB(li - 1, lj - 1)]));
+            d2 = T(1.0) / aZ;
+        }
+        const T shr = T(2) * zz * e12s[ZA(li, lj)];
+        const T s12 = (c.ld(io.s12, gi, gj) * (aZ - T(1)) + shr * T(0.25)) * d2;
+        s12s[idx] = s12;
+        if (li < EVP_TI && lj < EVP_TJ && gi < d.NX && gj < d.NY) io.s12o[d.raw(gi, gj)] = s12;
+    }
+    __syncthreads();
+
+    // ---- stage D: momentum update at U and V points of the tile
+    const T rdt = T(c.p.recip_deltatDyn);
+    const T cosW = T(c.p.cosWat), sinW = T(c.p.sinWat);
+    const T beta = T(c.p.evpBeta);
+    for (int idx = tid; idx < EVP_TI * EVP_TJ; idx += EVP_THREADS) {
+        const int li = idx / EVP_TJ, lj = idx % EVP_TJ;
+        const int gi = i0 + li, gj = j0 + lj;
+        if (gi >= d.NX || gj >= d.NY) continue;
+        const int64_t o = d.raw(gi, gj);
+        const T sg = sgn(__ldg(f.fCori + o));
+        const T cd0 = cds[ZC(li, lj)], cdw = cds[ZC(li - 1, lj)], cdsou = cds[ZC(li, lj - 1)];
+        const T cb0 = BASAL ? cbs[ZC(li, lj)] : T(0);
+        const T cbw = BASAL ? cbs[ZC(li - 1, lj)] : T(0);
+        const T cbs_ = BASAL ? cbs[ZC(li, lj - 1)] : T(0);
+        const T u0 = __ldg(io.u + o), v0 = __ldg(io.v + o);
+
+        // U point
+        {
+            const T sdx = (sig11[ZC(li, lj)] * __ldg(f.dyV + o) - sig11[ZC(li - 1, lj)] * c.ld(f.dyV, gi - 1, gj) -
+                           s12s[ZZ(li, lj)] * __ldg(f.dxV + o) + s12s[ZZ(li, lj + 1)] * c.ld(f.dxV, gi, gj + 1)) *
+                          __ldg(f.recip_rAu + o);
+            const T mU = __ldg(f.SeaIceMassU + o);
+            const T lm = mU != T(0) ? T(1) : mU;
+            const T uo = __ldg(f.uOcean + o);
+            const T du0 = uo - u0;
+            const T dun = c.ld(f.uOcean, gi, gj + 1) - c.ld(io.u, gi, gj + 1);
+            const T duw = c.ld(f.uOcean, gi - 1, gj) - c.ld(io.u, gi - 1, gj);
+            const T duwn = c.ld(f.uOcean, gi - 1, gj + 1) - c.ld(io.u, gi - 1, gj + 1);
+            const T AW = __ldg(f.AreaW + o);
+            T fx = __ldg(f.WindForcingX + o) +
+                   (T(0.5) * (cd0 + cdw) * cosW * uo -
+                    sg * sinW * T(0.5) * (cd0 * T(0.5) * (du0 + dun) + cdw * T(0.5) * (duw + duwn)) * lm) * AW;
+            fx = fx + T(0.5) * (fvC[ZC(li, lj)] + fvC[ZC(li - 1, lj)]);
+            const T bU = (ADAPT ? T(0.5) * (aCs[ZB(li, lj)] + aCs[ZB(li - 1, lj)]) : beta) * rdt;
+            const T bU1 = bU + rdt;
+            T den = mU * bU1 + AW * (T(0.5) * (cd0 + cdw) * cosW + T(0.5) * (cb0 + cbw));
+            den = den == T(0) ? T(1) : den;
+            if (SIDE) den = den + side_drag_u(c, gi, gj, sps[ZC(li, lj)], sps[ZC(li - 1, lj)]);
+            const T un = __ldg(f.iceMaskU + o) * (bU * mU * u0 + mU * rdt * __ldg(io.uNm1 + o) + fx + sdx) / den;
+            store_filled(io.uo, d, h, gi, gj, un);
+        }
+        // V point
+        {
+            const T sdy = (sig22[ZC(li, lj)] * __ldg(f.dxU + o) - sig22[ZC(li, lj - 1)] * c.ld(f.dxU, gi, gj - 1) -
+                           s12s[ZZ(li, lj)] * __ldg(f.dyU + o) + s12s[ZZ(li + 1, lj)] * c.ld(f.dyU, gi + 1, gj)) *
+                          __ldg(f.recip_rAv + o);
+            const T mV = __ldg(f.SeaIceMassV + o);
+            const T lm = mV != T(0) ? T(1) : mV;
+            const T vo = __ldg(f.vOcean + o);
+            const T dv0 = vo - v0;
+            const T dve = c.ld(f.vOcean, gi + 1, gj) - c.ld(io.v, gi + 1, gj);
+            const T dvs = c.ld(f.vOcean, gi, gj - 1) - c.ld(io.v, gi, gj - 1);
+            const T dvse = c.ld(f.vOcean, gi + 1, gj - 1) - c.ld(io.v, gi + 1, gj - 1);
+            const T AS = __ldg(f.AreaS + o);
+            T fy = __ldg(f.WindForcingY + o) +
+                   (T(0.5) * (cd0 + cdsou) * cosW * vo +
+                    sg * sinW * T(0.5) * (cd0 * T(0.5) * (dv0 + dve) + cdsou * T(0.5) * (dvs + dvse)) * lm) * AS;
+            fy = fy - T(0.5) * (fuC[ZC(li, lj)] + fuC[ZC(li, lj - 1)]);
+            const T bV = (ADAPT ? T(0.5) * (aCs[ZB(li, lj)] + aCs[ZB(li, lj - 1)]) : beta) * rdt;
+            const T bV1 = bV + rdt;
+            T den = mV * bV1 + AS * (T(0.5) * (cd0 + cdsou) * cosW + T(0.5) * (cb0 + cbs_));
+            den = den == T(0) ? T(1) : den;
+            if (SIDE) den = den + side_drag_v(c, gi, gj, sps[ZC(li, lj)], sps[ZC(li, lj - 1)]);
+            const T vn = __ldg(f.iceMaskV + o) * (bV * mV * v0 + mV * rdt * __ldg(io.vNm1 + o) + fy + sdy) / den;
+            store_filled(io.vo, d, h, gi, gj, vn);
+        }
+    }
+#undef ZA
+#undef ZB
+#undef ZC
+#undef ZZ
+}
+
+template <class T, bool A, bool Sd, bool B>
+static int launch_subcycle(const Ctx<T> &c, const HaloFill &h, const EvpIO<T> &io, cudaStream_t st) {
+    auto kern = evp_subcycle_kernel<T, A, Sd, B>;
+    const size_t sm = EvpSmem<T>::bytes();
+    static bool configured = false;
+    if (!configured) {
+        if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess)
+            return VERIS_ERR_LAUNCH;
+        configured = true;
+    }
+    dim3 grid((c.d.NY + EVP_TJ - 1) / EVP_TJ, (c.d.NX + EVP_TI - 1) / EVP_TI);
+    kern<<<grid, EVP_THREADS, sm, st>>>(c, h, io);
+    return launch_status();
+}
+
+template <class T>
+static int dispatch_subcycle(const Ctx<T> &c, const HaloFill &h, const EvpIO<T> &io, cudaStream_t st) {
+    const bool A = c.p.useAdaptiveEVP != 0, Sd = c.p.noSlip == 0, B = c.p.basalDragK2 != 0.0;
+    if (A) {
+        if (Sd) return B ? launch_subcycle<T, true, true, true>(c, h, io, st) : launch_subcycle<T, true, true, false>(c, h, io, st);
+        return B ? launch_subcycle<T, true, false, true>(c, h, io, st) : launch_subcycle<T, true, false, false>(c, h, io, st);
+    }
+    if (Sd) return B ? launch_subcycle<T, false, true, true>(c, h, io, st) : launch_subcycle<T, false, true, false>(c, h, io, st);
+    return B ? launch_subcycle<T, false, false, true>(c, h, io, st) : launch_subcycle<T, false, false, false>(c, h, io, st);
+}
+
+static size_t field_bytes(const Dims &d, size_t elem) { return (size_t)d.NX * (size_t)d.ld * elem; }
+
+static size_t round_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+template <class T>
+static int evp_solver(const VerisGrid *g, const VerisParams *p, const Fields<T> *vs, int n, T *u, T *v,
+                      T *s1, T *s2, T *s12, void *ws, size_t ws_bytes, veris_stream_t s) {
+    Dims d;
+    VERIS_CHECK_GRID(g, d);
+    VERIS_REQUIRE(p && vs && u && v && s1 && s2 && s12, VERIS_ERR_ARG);
+    VERIS_REQUIRE(n >= 0, VERIS_ERR_ARG);
+    cudaStream_t st = (cudaStream_t)s;
+    const size_t fb = round_up(field_bytes(d, sizeof(T)), 256);
+    if (n == 0) {
+        const T *src[5] = {vs->uIce, vs->vIce, vs->sigma1, vs->sigma2, vs->sigma12};
+        T *dst[5] = {u, v, s1, s2, s12};
+        for (int q = 0; q < 5; ++q)
+            if (cudaMemcpyAsync(dst[q], src[q], field_bytes(d, sizeof(T)), cudaMemcpyDeviceToDevice, st) != cudaSuccess)
+                return VERIS_ERR_LAUNCH;
+        return VERIS_OK;
+    }
+    if (n > 1) VERIS_REQUIRE(ws && ws_bytes >= 5 * fb, VERIS_ERR_WORKSPACE);
+    Ctx<T> c;
+    c.f = *vs;
+    c.d = d;
+    c.p = *p;
+    const HaloFill h = halo_fill_of(*p);
+    T *buf[2][5] = {{u, v, s1, s2, s12}, {nullptr, nullptr, nullptr, nullptr, nullptr}};
+    if (n > 1)
+        for (int q = 0; q < 5; ++q) buf[1][q] = reinterpret_cast<T *>(static_cast<char *>(ws) + q * fb);
+    const T *cur[5] = {vs->uIce, vs->vIce, vs->sigma1, vs->sigma2, vs->sigma12};
+    for (int it = 0; it < n; ++it) {
+        T **dst = buf[(n - 1 - it) % 2];
+        EvpIO<T> io{cur[0], cur[1], cur[2], cur[3], cur[4], dst[0], dst[1], dst[2], dst[3], dst[4],
+                    vs->uIce, vs->vIce};
+        const int stt = dispatch_subcycle<T>(c, h, io, st);
+        if (stt != VERIS_OK) return stt;
+        for (int q = 0; q < 5; ++q) cur[q] = dst[q];
+    }
+    return VERIS_OK;
+}
+
+}  // namespace veris
+
+using namespace veris;
+
+extern "C" {
+
+size_t veris_evp_workspace_bytes(const VerisGrid *g, int32_t elem_size) {
+    Dims d;
+    if (check_grid(g, &d) != VERIS_OK || (elem_size != 4 && elem_size != 8)) return 0;
+    return 5 * round_up(field_bytes(d, (size_t)elem_size), 256);
+}
+
+int veris_evp_solver_f64(const VerisGrid *g, const VerisParams *p, const VerisFieldsF64 *vs, int32_t n,
+                         double *u, double *v, double *s1, double *s2, double *s12, void *ws,
+                         size_t ws_bytes, veris_stream_t s) {
+    return evp_solver<double>(g, p, reinterpret_cast<const Fields<double> *>(vs), n, u, v, s1, s2, s12, ws,
+                              ws_bytes, s);
+}
+
+int veris_evp_solver_f32(const VerisGrid *g, const VerisParams *p, const VerisFieldsF32 *vs, int32_t n,
+                         float *u, float *v, float *s1, float *s2, float *s12, void *ws, size_t ws_bytes,
+                         veris_stream_t s) {
+    return evp_solver<float>(g, p, reinterpret_cast<const Fields<float> *>(vs), n, u, v, s1, s2, s12, ws,
+                             ws_bytes, s);
+}
+
+}  // extern "C"

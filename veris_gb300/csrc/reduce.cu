@@ -1,0 +1,80 @@
+// Deterministic float64 sum over the interior of a field (optionally
+// weighted), for conservation diagnostics.  The reference's global_sum
+// (veris/global_sum.py:1-4) is the identity on one process; this is the sum
+// it would feed.  Fixed grid, fixed per-block tree, fixed final pass: the
+// result is bitwise reproducible run to run.
+#include "common.cuh"
+
+namespace veris {
+
+constexpr int RED_THREADS = 256;
+constexpr int RED_BLOCKS = 1024;
+
+template <class T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+template <class T>
+__device__ T block_sum(T v) {
+    __shared__ T part[RED_THREADS / 32];
+    v = warp_sum(v);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) part[warp] = v;
+    __syncthreads();
+    T r = 0;
+    if (warp == 0) {
+        r = lane < RED_THREADS / 32 ? part[lane] : T(0);
+        r = warp_sum(r);
+    }
+    __syncthreads();
+    return r;
+}
+
+__global__ void interior_partial_kernel(const double *A, const double *w, Dims d, int olx, int oly,
+                                        double *partial) {
+    const int64_t n = (int64_t)d.nx * d.ny;
+    double acc = 0.0;
+    for (int64_t k = blockIdx.x * (int64_t)RED_THREADS + threadIdx.x; k < n; k += (int64_t)RED_BLOCKS * RED_THREADS) {
+        const int i = (int)(k / d.ny) + olx, j = (int)(k % d.ny) + oly;
+        const int64_t o = d.raw(i, j);
+        acc += w ? A[o] * w[o] : A[o];
+    }
+    const double s = block_sum(acc);
+    if (threadIdx.x == 0) partial[blockIdx.x] = s;
+}
+
+__global__ void final_sum_kernel(const double *partial, double *result) {
+    double acc = 0.0;
+    for (int k = threadIdx.x; k < RED_BLOCKS; k += RED_THREADS) acc += partial[k];
+    const double s = block_sum(acc);
+    if (threadIdx.x == 0) *result = s;
+}
+
+}  // namespace veris
+
+using namespace veris;
+
+extern "C" {
+
+size_t veris_reduce_workspace_bytes(const VerisGrid *g) {
+    (void)g;
+    return RED_BLOCKS * sizeof(double);
+}
+
+int veris_global_sum_f64(const VerisGrid *g, const double *A, const double *w, double *result, void *ws,
+                         size_t ws_bytes, veris_stream_t s) {
+    Dims d;
+    VERIS_CHECK_GRID(g, d);
+    VERIS_REQUIRE(A && result, VERIS_ERR_ARG);
+    VERIS_REQUIRE(ws && ws_bytes >= RED_BLOCKS * sizeof(double), VERIS_ERR_WORKSPACE);
+    cudaStream_t st = (cudaStream_t)s;
+    double *partial = static_cast<double *>(ws);
+    interior_partial_kernel<<<RED_BLOCKS, RED_THREADS, 0, st>>>(A, w, d, g->olx, g->oly, partial);
+    final_sum_kernel<<<1, RED_THREADS, 0, st>>>(partial, result);
+    return launch_status();
+}
+
+}  // extern "C"

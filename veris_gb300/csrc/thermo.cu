@@ -1,0 +1,292 @@
+// Thermodynamics in float64: the surface-temperature Newton solve
+// (veris/solve4temp.py:5-174) and ice growth with the ocean budgets
+// (veris/growth.py:8-397).  Both are pointwise; one thread per padded point.
+#include "stencil.cuh"
+
+namespace veris {
+
+struct S4TIn {
+    double hI, hS, Tin, TempFrz;
+    double LWdown, ATemp, wSpeed, fCori, SWdown, aqh;
+};
+struct S4TOut {
+    double T, Fio, Fia, pen, fw;
+};
+
+__device__ __forceinline__ double dmax(double a, double b) { return a > b ? a : b; }
+__device__ __forceinline__ double dmin(double a, double b) { return a < b ? a : b; }
+
+// veris/solve4temp.py:5-174 for one point
+__device__ S4TOut solve4temp_point(const VerisParams &p, const S4TIn &x) {
+    const double aa1 = 2663.5, aa2 = 12.537, bb1 = 0.622;
+    const double Pa = 100000.0;
+    const double one_m_bb1 = 1.0 - bb1;
+    const double cc1 = p.s4t_cc1, cc2 = p.s4t_cc2, d1 = p.s4t_d1, d1i = p.s4t_d1i;
+    const double Tmelt = p.celsius2K;
+    const double SurfMeltTemp = Tmelt + p.wetAlbTemp;
+    double T = x.Tin;
+    const double lwc = dmax(p.minLWdown, x.LWdown);
+    const double Ta = dmax(p.celsius2K + p.minTAir, x.ATemp);
+    const double ug = dmax(p.wSpeedMin, x.wSpeed);
+    const bool ice = x.hI > 0, snow = x.hS > 0;
+    const double emiss = snow ? p.snowEmiss : p.iceEmiss;
+    const double d3 = emiss * p.stefBoltz;
+    const double lw = emiss * lwc;
+
+    double aI = ice ? p.dryIceAlb : 0.0;
+    double aS = ice ? p.drySnowAlb : 0.0;
+    const bool wet = ice && T >= SurfMeltTemp;
+    if (wet) { aI = p.wetIceAlb; aS = p.wetSnowAlb; }
+    const bool south = ice && x.fCori < 0;
+    if (south) { aI = p.dryIceAlb_south; aS = p.drySnowAlb_south; }
+    if (south && T >= SurfMeltTemp) { aI = p.wetIceAlb_south; aS = p.wetSnowAlb_south; }
+    double alb = ice ? aI + x.hS / p.hCut * (aS - aI) : 0.0;
+    if (x.hS > p.hCut) alb = aS;
+    if (x.hS == 0) alb = aI;
+
+    double pen = ice ? p.shortwave * exp(-1.5 * x.hI) : 0.0;
+    if (snow) pen = 0.0;
+    const double penSW = ice ? -(1 - alb) * pen * x.SWdown : 0.0;
+    const double absSW = ice ? (1 - alb) * (1 - pen) * x.SWdown : 0.0;
+    const double k = ice ? p.iceConduct * p.snowConduct / (p.snowConduct * x.hI + p.iceConduct * x.hS) : 0.0;
+
+    double Fc, Flh, Fia, dF;
+    auto fluxes = [&](double t1) {
+        const double t2 = t1 * t1, t3 = t2 * t1, t4 = t2 * t2;
+        const double svp = pow(10.0, -aa1 / t1 + aa2);
+        const double qs = ice ? bb1 * svp / (Pa - one_m_bb1 * svp) : 0.0;
+        const double c3 = pow(10.0, aa1 / t1);
+        const double den = cc2 - c3 * Pa;
+        const double dqs = ice ? cc1 * c3 / (den * den * t2) : 0.0;
+        Fc = ice ? k * (x.TempFrz - t1) : 0.0;
+        Flh = ice ? d1i * ug * (qs - x.aqh) : 0.0;
+        const double Flw = ice ? t4 * d3 : 0.0;
+        const double Fs = ice ? d1 * ug * (t1 - Ta) : 0.0;
+        Fia = ice ? (-lw - absSW + Flw + Fs + Flh) : 0.0;
+        dF = ice ? 4 * d3 * t3 + d1 * ug + d1i * ug * dqs : 0.0;
+    };
+    for (int it = 0; it < 6; ++it) {
+        fluxes(T);
+        T = ice ? T + (Fc - Fia) / (k + dF) : 0.0;
+        T = dmin(T, Tmelt);
+        T = dmax(T, p.celsius2K + p.minTIce);
+    }
+    fluxes(T);
+    S4TOut o;
+    const bool up = Fc > 0;
+    o.T = ice ? T : x.Tin;
+    o.Fio = up ? Fc : 0.0;
+    o.Fia = up ? 0.0 : Fia;
+    o.pen = penSW;
+    o.fw = ice ? Flh / p.lhSublim : 0.0;
+    return o;
+}
+
+struct GrowthOut {
+    double h, hs, A, TSurf, EmPmR, forc_salt, Qsw, Qnet, load, pen, rh;
+};
+
+// veris/growth.py:8-397 for one point
+__device__ GrowthOut growth_point(const VerisParams &p, const Fields<double> &f, int64_t o) {
+    const double qi = 1 / (p.rhoIce * p.lhFusion);
+    const double qs = 1 / (p.rhoSnow * p.lhFusion);
+    const double hIn = __ldg(f.hIceMean + o), hsIn = __ldg(f.hSnowMean + o), AIn = __ldg(f.Area + o);
+    const bool noIce = hIn == 0 || AIn == 0;
+    const double keep = noIce ? 0.0 : 1.0;
+    const double h0 = hIn * keep, hs0 = hsIn * keep, A0 = AIn * keep;
+    const bool isIce = h0 > 0;
+    const double regA = sqrt(A0 * A0 + p.Area_reg);
+    const double rregA = 1 / regA;
+    double hIa = isIce ? h0 * rregA : 0.0;
+    const double rhIa = A0 / sqrt(h0 * h0 + p.hIce_reg);
+    const double hSa = isIce ? hs0 * rregA : 0.0;
+    hIa = dmax(hIa, 0.05);
+
+    const double ocSalt = __ldg(f.ocSalt + o);
+    const double TempFrz = p.tempFrz + p.dtempFrz_dS * ocSalt + p.celsius2K;
+    const double TSurfIn = __ldg(f.TSurf + o);
+    S4TIn x;
+    x.Tin = TSurfIn;
+    x.TempFrz = TempFrz;
+    x.LWdown = __ldg(f.LWdown + o);
+    x.ATemp = __ldg(f.ATemp + o);
+    x.wSpeed = __ldg(f.wSpeed + o);
+    x.fCori = __ldg(f.fCori + o);
+    x.SWdown = __ldg(f.SWdown + o);
+    x.aqh = __ldg(f.aqh + o);
+    double Tsum = 0, Fio_sum = 0, Fia_sum = 0, pen_sum = 0;
+    for (int l = 0; l < p.nITC; ++l) {
+        const double pFac = (double)(2 * (l + 1) - 1) * p.recip_nITC;
+        x.hI = hIa * pFac;
+        x.hS = hSa * pFac;
+        const S4TOut r = solve4temp_point(p, x);
+        Tsum = Tsum + r.T;
+        Fio_sum = Fio_sum + r.Fio;
+        Fia_sum = Fia_sum + r.Fia;
+        pen_sum = pen_sum + r.pen;
+    }
+    GrowthOut g;
+    g.TSurf = Tsum * p.recip_nITC;
+    const double Fio = Fio_sum * p.recip_nITC * A0;
+    double Fia = Fia_sum * p.recip_nITC * A0;
+    const double pen = pen_sum * p.recip_nITC * A0;
+
+    const double snowfall = __ldg(f.snowfall + o), precip = __ldg(f.precip + o);
+    const bool cold = A0 > 0 && Tsum / (double)p.nITC < p.celsius2K;
+    const double snowAcc = (cold ? snowfall + precip : snowfall) * p.rhoFresh2rhoSnow;
+    const double rainToSea = cold ? 0.0 : precip;
+    const double snowAccOverIce = snowAcc * A0 * p.deltatTherm;
+
+    double gUnder = Fio * qi;
+    if (A0 == 0) gUnder = 0.0;
+    const double potMeltRate = -Fia * qs;
+    const double potMelt = potMeltRate * p.deltatTherm;
+    const bool allMelt = potMelt >= hs0;
+    const double meltRate = allMelt ? hs0 * p.recip_deltatTherm : potMeltRate;
+    const double toSnow = allMelt ? -hs0 * p.recip_deltatTherm / qs : Fia;
+    Fia = Fia - toSnow;
+    const double gSurf = Fia * qi;
+    const double gNet = (gUnder + gSurf) * rregA;
+
+    const double t0 = 0.4, t1 = 7 / t0;
+    const double t2 = p.stantonNr * p.uStarBase * p.rhoSea * p.cpWater;
+    const double sst = dmax(__ldg(f.theta + o), TempFrz);
+    const double mltf = 1 + (p.McPheeTaperFac - 1) / (1 + exp((A0 - t0) * t1));
+    const double gML = -t2 * (sst - TempFrz) * mltf * qi;
+    const double Qnet_in = __ldg(f.Qnet + o);
+    const double gOW = qi * Qnet_in;
+
+    const double dh = gNet * A0 + gOW * (1 - A0) + gML;
+    const double dhs = (snowAcc - meltRate) * A0;
+    const double half_rh = 0.5 * rhIa;
+    double dA_oa = half_rh * gOW * (1 - A0);
+    const bool grow = gOW > 0 && (A0 > 0 || dh > 0);
+    if (grow) dA_oa = gOW * (1 - A0);
+    const double fC = __ldg(f.fCori + o);
+    dA_oa = (grow && fC < 0) ? dA_oa * p.recip_h0_south : dA_oa * p.recip_h0;
+    const double dA_oi = gML <= 0 ? half_rh * gML : 0.0;
+    const double dA_ia = (gNet <= 0 && h0 > 0) ? half_rh * gNet * A0 : 0.0;
+    const double dA = dA_oa + dA_oi + dA_ia;
+
+    const double mask = __ldg(f.iceMask + o);
+    double A = A0 + dA * mask * p.deltatTherm;
+    double h = h0 + dh * mask * p.deltatTherm;
+    double hs = hs0 + dhs * mask * p.deltatTherm;
+    A = dmin(dmax(A, 0.0), 1.0);
+    h = dmax(h, 0.0);
+    hs = dmax(hs, 0.0);
+    const double alive = (h == 0 || A == 0) ? 0.0 : 1.0;
+    A = A * alive;
+    hs = hs * alive;
+    h = h * alive;
+    const double hsub = (hs * p.rhoSnow + h * p.rhoIce) * p.recip_rhoSea;
+    const double flood = dmax(0.0, hsub - h);
+    h = h + flood;
+    hs = hs - flood * p.rhoIce2rhoSnow;
+    g.rh = 1 / sqrt(h * h + p.hIce_reg);
+    g.h = h;
+    g.hs = hs;
+    g.A = A;
+
+    g.Qsw = pen * A0 + __ldg(f.Qsw + o) * (1 - A0);
+    const double dH = h - h0;
+    const double melted = hs0 + snowAccOverIce - hs;
+    const double E_ice = dH / qi;
+    const double E_out = (A0 * (Fia + Fio + pen) + (1 - A0) * Qnet_in) * p.deltatTherm;
+    g.Qnet = (E_out - E_ice) * p.recip_deltatTherm;
+    const double sal_fac = (ocSalt > 0 && ocSalt > p.saltIce_ref) ? (1 - p.saltIce_ref / ocSalt) : 1.0;
+    const double fw_ice = -dH * p.rhoIce2rhoFresh * sal_fac;
+    const double salt_ref = dmin(p.saltIce_ref, ocSalt);
+    const double osh = __ldg(f.os_hIceMean + o), oshs = __ldg(f.os_hSnowMean + o);
+    const double saltflux = (dH + osh) * salt_ref * mask * p.rhoIce * p.recip_deltatTherm;
+    const double fw_snow = melted / p.rhoFresh2rhoSnow;
+    g.EmPmR = mask * ((-__ldg(f.evap + o) - precip) * (1 - A0) - rainToSea * A0 - __ldg(f.runoff + o) -
+                      (fw_ice + fw_snow) / p.deltatTherm) * p.rhoFresh +
+              mask * (osh * p.rhoIce + oshs * p.rhoSnow) * p.recip_deltatTherm;
+    g.forc_salt = g.EmPmR * ocSalt / p.rhoFresh + saltflux;
+    g.load = h * p.rhoIce + hs * p.rhoSnow;
+    g.pen = pen;
+    return g;
+}
+
+__global__ void solve4temp_kernel(VerisParams p, Fields<double> f, Dims d, const double *hI, const double *hS,
+                                  const double *Tin, const double *TF, double *To, double *Fio, double *Fia,
+                                  double *pen, double *fw) {
+    const int j = blockIdx.x * 32 + threadIdx.x, i = blockIdx.y * 8 + threadIdx.y;
+    if (i >= d.NX || j >= d.NY) return;
+    const int64_t o = d.raw(i, j);
+    S4TIn x;
+    x.hI = hI[o];
+    x.hS = hS[o];
+    x.Tin = Tin[o];
+    x.TempFrz = TF[o];
+    x.LWdown = __ldg(f.LWdown + o);
+    x.ATemp = __ldg(f.ATemp + o);
+    x.wSpeed = __ldg(f.wSpeed + o);
+    x.fCori = __ldg(f.fCori + o);
+    x.SWdown = __ldg(f.SWdown + o);
+    x.aqh = __ldg(f.aqh + o);
+    const S4TOut r = solve4temp_point(p, x);
+    To[o] = r.T;
+    Fio[o] = r.Fio;
+    Fia[o] = r.Fia;
+    pen[o] = r.pen;
+    fw[o] = r.fw;
+}
+
+struct GrowthPtrs {
+    double *h, *hs, *A, *TSurf, *EmPmR, *forc_salt, *Qsw, *Qnet, *load, *pen, *rh;
+};
+
+__global__ void __launch_bounds__(128) growth_kernel(VerisParams p, Fields<double> f, Dims d, GrowthPtrs out) {
+    const int j = blockIdx.x * 32 + threadIdx.x, i = blockIdx.y * 4 + threadIdx.y;
+    if (i >= d.NX || j >= d.NY) return;
+    const int64_t o = d.raw(i, j);
+    const GrowthOut g = growth_point(p, f, o);
+    out.h[o] = g.h;
+    out.hs[o] = g.hs;
+    out.A[o] = g.A;
+    out.TSurf[o] = g.TSurf;
+    out.EmPmR[o] = g.EmPmR;
+    out.forc_salt[o] = g.forc_salt;
+    out.Qsw[o] = g.Qsw;
+    out.Qnet[o] = g.Qnet;
+    out.load[o] = g.load;
+    out.pen[o] = g.pen;
+    out.rh[o] = g.rh;
+}
+
+}  // namespace veris
+
+using namespace veris;
+
+extern "C" {
+
+int veris_solve4temp_f64(const VerisGrid *g, const VerisParams *p, const VerisFieldsF64 *vs,
+                         const double *hI, const double *hS, const double *Tin, const double *TF, double *To,
+                         double *Fio, double *Fia, double *pen, double *fw, veris_stream_t s) {
+    Dims d;
+    VERIS_CHECK_GRID(g, d);
+    VERIS_REQUIRE(p && vs && hI && hS && Tin && TF && To && Fio && Fia && pen && fw, VERIS_ERR_ARG);
+    dim3 gr((d.NY + 31) / 32, (d.NX + 7) / 8);
+    solve4temp_kernel<<<gr, dim3(32, 8), 0, (cudaStream_t)s>>>(
+        *p, *reinterpret_cast<const Fields<double> *>(vs), d, hI, hS, Tin, TF, To, Fio, Fia, pen, fw);
+    return launch_status();
+}
+
+int veris_growth_f64(const VerisGrid *g, const VerisParams *p, const VerisFieldsF64 *vs, double *h,
+                     double *hs, double *A, double *TSurf, double *EmPmR, double *forc_salt, double *Qsw,
+                     double *Qnet, double *load, double *pen, double *rh, veris_stream_t s) {
+    Dims d;
+    VERIS_CHECK_GRID(g, d);
+    VERIS_REQUIRE(p && vs && h && hs && A && TSurf && EmPmR && forc_salt && Qsw && Qnet && load && pen && rh,
+                  VERIS_ERR_ARG);
+    VERIS_REQUIRE(p->nITC >= 1 && p->nITC <= 64, VERIS_ERR_ARG);
+    GrowthPtrs out{h, hs, A, TSurf, EmPmR, forc_salt, Qsw, Qnet, load, pen, rh};
+    dim3 gr((d.NY + 31) / 32, (d.NX + 3) / 4);
+    growth_kernel<<<gr, dim3(32, 4), 0, (cudaStream_t)s>>>(*p, *reinterpret_cast<const Fields<double> *>(vs), d,
+                                                            out);
+    return launch_status();
+}
+
+}  // extern "C"

@@ -1,0 +1,38 @@
+"""Drop-in for veris/evp_solver.py: the mEVP subcycling loop on the GPU."""
+import torch
+
+from ._abi import check
+from .state import Call
+
+
+def evp_solver(state, n_subcycles=None):
+    """veris/evp_solver.py:257-319 -> (uIce, vIce, sigma1, sigma2, sigma12).
+
+    Runs ``settings.nEVPsteps`` subcycles (or ``n_subcycles``) from the
+    state's velocities and stresses in float64, one tiled kernel per
+    subcycle.  The residual diagnostics of the reference
+    (``computeEvpResidual``) read undefined names there
+    (veris/evp_solver.py:54-55) and are not part of this entry point.
+    """
+    s = state.settings
+    if s.computeEvpResidual:
+        raise NotImplementedError("computeEvpResidual: use veris_gb300.diagnostics.evp_residuals")
+    n = int(s.nEVPsteps if n_subcycles is None else n_subcycles)
+    c = Call(state)
+    out = c.empty(5)
+    ws, wsb = c.workspace(c.lib.veris_evp_workspace_bytes(c.refs()[0], 8))
+    check("evp_solver", c.lib.veris_evp_solver_f64(*c.refs(), n, *[t.data_ptr() for t in out], ws, wsb,
+                                                    c.stream))
+    return tuple(out)
+
+
+def evp_solver_f32(state32, n_subcycles=None):
+    """The same loop in float32 on a state whose variables are float32."""
+    s = state32.settings
+    n = int(s.nEVPsteps if n_subcycles is None else n_subcycles)
+    c = Call(state32, dtype=torch.float32)
+    out = c.empty(5)
+    ws, wsb = c.workspace(c.lib.veris_evp_workspace_bytes(c.refs()[0], 4))
+    check("evp_solver_f32", c.lib.veris_evp_solver_f32(*c.refs(), n, *[t.data_ptr() for t in out], ws,
+                                                        wsb, c.stream))
+    return tuple(out)
