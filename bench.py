@@ -1,0 +1,406 @@
+#!/usr/bin/env python
+"""Benchmark of the sea-ice step: EVP Gcell-subcycles/s on one GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Workload (default): the 0.25-degree single domain, 1440 x 720 interior cells,
+500 mEVP subcycles per step, dt = 1800 s, seeded synthetic fields.  One
+bench step is one full sea-ice time step (dynamics preparation, 500 EVP
+subcycles, ocean stress, advection, clean-up, growth, halo fills).
+
+The headline ``value`` runs the mixed-precision step (float32 EVP and
+advection, float64 thermodynamics and budgets) replayed as one CUDA graph,
+with inputs resident in HBM; L2 is flushed (a 512 MiB write) before every
+timed step and the flush is outside the timed events.  The metric counts
+interior cells x subcycles over the whole step time.  Also reported: the
+plain float64 step on the same inputs, the float32-vs-float64 errors per
+field, the end-to-end rate through host buffers, the EVP kernel's roofline
+and a CPU baseline (the NumPy oracle on one core, bounded sample).
+
+``--impl reference`` times the reference's CPU algorithm (the NumPy oracle,
+a restatement of the reference that is bit-identical to it on the golden
+fixtures) on the host cores, each step a bounded sample extrapolated to a
+full 500-subcycle step.
+
+With ``--gpus N > 1`` (under torchrun) every rank runs an independent replica
+(the workload does not shard: one domain per GPU), ``scaling`` is weak and
+``value`` sums the ranks' cells over the slowest rank's time.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+BYTES_PER_CELL_SUBCYCLE = {"f32": 83, "f64": 163}
+METRIC = "EVP Gcell-subcycles/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=("ours", "reference"))
+    ap.add_argument("--config", default="c2_quarterdeg")
+    ap.add_argument("--precision", default="f32", choices=("f32", "f64"))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the float64 comparison leg")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--subcycles", type=int, default=None, help="override the workload's subcycles")
+    ap.add_argument("--seed", type=int, default=0)
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------- distributed
+
+def dist_init(args):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, ws):
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# -------------------------------------------------------------------- clocks
+
+class ClockSampler:
+    """nvidia-smi samples of SM clocks and throttle reasons while running."""
+
+    QUERY = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for n, val in zip(names, parts[4:8]):
+                if val.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": float(max(smax)) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------- peaks
+
+def hbm_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def recorded_traffic(precision):
+    path = os.path.join(ROOT, "profiles", "roofline_traffic.json")
+    try:
+        with open(path) as f:
+            return json.load(f).get(f"evp_{precision}_c2_bytes_per_launch")
+    except (OSError, ValueError):
+        return None
+
+
+# ----------------------------------------------------------------- CPU legs
+
+def cpu_sample(arrays, sett, n_sub_sample, n_sub_full):
+    """Time the oracle (the reference's NumPy algorithm, one core) on a
+    bounded sample: ``n_sub_sample`` EVP subcycles, one advection, one
+    growth; extrapolated to a step of ``n_sub_full`` subcycles.  Returns
+    (seconds per full step, sample description)."""
+    from types import SimpleNamespace
+    import copy
+    from oracle import veris_oracle as O
+    st = SimpleNamespace(variables=SimpleNamespace(**{k: v.copy() for k, v in arrays.items()}),
+                         settings=copy.copy(sett))
+    v = st.variables
+    t0 = time.perf_counter()
+    v.SeaIceMassC, v.SeaIceMassU, v.SeaIceMassV = O.SeaIceMass(st)
+    v.AreaW, v.AreaS = O.AreaWS(st)
+    v.WindForcingX, v.WindForcingY = O.WindForcingXY(st)
+    v.SeaIceStrength = O.SeaIceStrength(st)
+    t1 = time.perf_counter()
+    c = O.evp_carry(st)
+    for _ in range(n_sub_sample):
+        O.evp_subcycle(st, c)
+    t2 = time.perf_counter()
+    v.uIce, v.vIce = c["u"], c["v"]
+    v.OceanStressU, v.OceanStressV = O.OceanStressUV(st)
+    v.hIceMean, v.hSnowMean, v.Area = O.Advection(st)
+    out = O.clean_up_advection(st)
+    v.hIceMean, v.hSnowMean, v.Area, v.TSurf, v.os_hIceMean, v.os_hSnowMean = out
+    v.Area = O.ridging(st)
+    O.Growth(st)
+    t3 = time.perf_counter()
+    per_sub = (t2 - t1) / n_sub_sample
+    full = (t1 - t0) + per_sub * n_sub_full + (t3 - t2)
+    desc = (f"NumPy oracle, 1 thread: {n_sub_sample} EVP subcycles + preparation + advection + "
+            f"growth timed ({t3 - t0:.1f} s), extrapolated to {n_sub_full} subcycles per step")
+    return full, desc
+
+
+def run_reference(args):
+    ws, rank, _ = int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")), 0
+    if rank != 0:
+        return 0
+    from veris_gb300.synthetic import CONFIGS, make_state, config_settings
+    c = CONFIGS[args.config]
+    n_full = args.subcycles or c["n_evp"]
+    arrays = make_state(c["nx"], c["ny"], seed=args.seed)
+    sett = config_settings(args.config)
+    cells = c["nx"] * c["ny"]
+    n_sample = 2
+    for _ in range(args.warmup):
+        cpu_sample(arrays, sett, n_sample, n_full)
+    times = []
+    desc = ""
+    for _ in range(args.steps):
+        t, desc = cpu_sample(arrays, sett, n_sample, n_full)
+        times.append(t)
+    sec = float(np.sum(times))
+    value = cells * n_full * args.steps / sec / 1e9
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "Gcell-subcycles/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": sec / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": args.config, "nx": c["nx"], "ny": c["ny"], "subcycles": n_full,
+                   "dt_s": c["dt"], "cells": cells, "parallelism": "replicas",
+                   "l2": "n/a (CPU)"},
+        "cpu_baseline": {"value": value, "unit": "Gcell-subcycles/s", "cores": 1, "kind": "port",
+                         "sample": desc, "host_cpus": os.cpu_count()},
+        "e2e": {"value": value, "unit": "Gcell-subcycles/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+# ----------------------------------------------------------------- our arm
+
+def rel_errors(a, b):
+    a = a.double()
+    b = b.double()
+    scale = float(b.abs().max())
+    if scale == 0:
+        scale = 1.0
+    d = (a - b).abs()
+    return {"max_rel": float(d.max()) / scale, "rms_rel": float(d.pow(2).mean().sqrt()) / scale}
+
+
+def run_ours(args):
+    import torch
+    ws, rank, local = dist_init(args)
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    from __graft_entry__ import build
+    if rank == 0 or ws == 1:
+        build()
+    barrier(ws)
+    from veris_gb300.engine import SeaIceStep
+    from veris_gb300.state import VerisState
+    from veris_gb300.synthetic import CONFIGS, make_state, config_settings
+
+    c = CONFIGS[args.config]
+    arrays = make_state(c["nx"], c["ny"], seed=args.seed + rank)
+    sett = config_settings(args.config)
+    if args.subcycles:
+        sett.nEVPsteps = args.subcycles
+    n_sub = sett.nEVPsteps
+    cells = c["nx"] * c["ny"]
+
+    state = VerisState.from_numpy(arrays, sett, device=dev)
+    eng = SeaIceStep(state, precision=args.precision)
+    eng.capture()
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    for _ in range(args.warmup):
+        eng.step()
+    torch.cuda.synchronize(dev)
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    barrier(ws)
+    torch.cuda.synchronize(dev)
+    t_wall0 = time.perf_counter()
+    for k in range(args.steps):
+        flush.zero_()
+        starts[k].record()
+        eng.step()
+        ends[k].record()
+    torch.cuda.synchronize(dev)
+    barrier(ws)
+    wall = time.perf_counter() - t_wall0
+    clk = clocks.stop()
+    ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
+    ms = max_over_ranks(ms, ws)
+    value = ws * cells * n_sub * args.steps / (ms / 1e3) / 1e9
+    launches = eng.launches_per_step * args.steps
+
+    # EVP kernel alone (eager, events around the subcycle loop on the launching stream)
+    evp_ms = []
+    for _ in range(3):
+        flush.zero_()
+        evp_ms.append(eng.timed_step())
+    evp_ms = float(np.median(evp_ms))
+    per_launch_s = evp_ms / 1e3 / n_sub
+    algo_bytes = BYTES_PER_CELL_SUBCYCLE[args.precision] * cells
+    achieved = algo_bytes / per_launch_s / 1e9
+    peak, peak_kind = hbm_peak()
+    traffic = recorded_traffic(args.precision)
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": traffic,
+                "kernel": f"evp_subcycle_kernel<{'float' if args.precision == 'f32' else 'double'}>",
+                "algorithmic_bytes_per_launch": algo_bytes, "avg_launch_us": per_launch_s * 1e6,
+                "peak_source": f"{peak_kind} HBM copy bandwidth"}
+
+    line = {"metric": METRIC, "value": value, "unit": "Gcell-subcycles/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": args.precision, "data": "synthetic",
+            "config": {"workload": args.config, "nx": c["nx"], "ny": c["ny"], "subcycles": n_sub,
+                       "dt_s": c["dt"], "cells": cells, "precision": args.precision,
+                       "parallelism": "replicas" if ws > 1 else "single-gpu",
+                       "l2": "flushed before every timed step (512 MiB write)",
+                       "graph": "one CUDA graph per step"},
+            "roofline": roofline, "gpu_launches": launches, "clocks": clk,
+            "wall_s_timed_region": wall, "evp_ms_per_step": evp_ms}
+
+    # end-to-end through host buffers
+    if not args.no_e2e:
+        from veris_gb300.host import HostCoupledStep
+        host = HostCoupledStep(eng)
+        h_in, h_out = host.host_buffers()
+        for _ in range(2):
+            host.step(h_in, h_out)
+        barrier(ws)
+        t0 = time.perf_counter()
+        ke = max(2, args.steps // 2)
+        for _ in range(ke):
+            host.step(h_in, h_out)
+        e2e_s = time.perf_counter() - t0
+        e2e_s = max_over_ranks(e2e_s, ws)
+        line["e2e"] = {"value": ws * cells * n_sub * ke / e2e_s / 1e9, "unit": "Gcell-subcycles/s",
+                       "h2d_bytes_per_step": host.h2d_bytes, "d2h_bytes_per_step": host.d2h_bytes,
+                       "steps": ke, "api": "veris_gb300.host.HostCoupledStep.step (pinned host arrays)"}
+
+    # float64 drop-in arithmetic on the same inputs, and the float32 error
+    if not args.no_fp64 and args.precision == "f32":
+        n_cmp = max(2, args.warmup + args.steps)
+        st64 = VerisState.from_numpy(arrays, sett, device=dev)
+        e64 = SeaIceStep(st64, precision="f64")
+        e64.capture()
+        torch.cuda.synchronize(dev)
+        t64 = []
+        for k in range(n_cmp - 1):
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            flush.zero_()
+            a.record()
+            e64.step()
+            b.record()
+            b.synchronize()
+            t64.append(a.elapsed_time(b))
+        fp64_ms = float(np.median(t64[-min(len(t64), args.steps):]))
+        fp64_value = cells * n_sub / (fp64_ms / 1e3) / 1e9
+        line["fp64"] = {"value": fp64_value, "ms_per_step": fp64_ms, "steps_compared": n_cmp}
+        line["fp32_over_fp64_speedup"] = (value / ws) / fp64_value
+        # rerun float32 from the initial state for exactly n_cmp steps
+        st32 = VerisState.from_numpy(arrays, sett, device=dev)
+        e32 = SeaIceStep(st32, precision="f32")
+        e32.capture()
+        for _ in range(n_cmp - 1):
+            e32.step()
+        torch.cuda.synchronize(dev)
+        errs = {}
+        for n in ("uIce", "vIce", "hIceMean", "hSnowMean", "Area", "TSurf", "Qnet"):
+            errs[n] = rel_errors(getattr(st32.variables, n), getattr(st64.variables, n))
+        line["fp32_error_vs_fp64"] = {"steps": n_cmp, "fields": errs}
+
+    if rank == 0 and not args.no_cpu_baseline:
+        sec, desc = cpu_sample(arrays, sett, 2, n_sub)
+        line["cpu_baseline"] = {"value": cells * n_sub / sec / 1e9, "unit": "Gcell-subcycles/s",
+                                "cores": 1, "kind": "port", "sample": desc,
+                                "host_cpus": os.cpu_count()}
+    if rank == 0:
+        print(json.dumps(line))
+    barrier(ws)
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,203 @@
+"""Persistent-buffer sea-ice step for repeated time stepping on one GPU.
+
+The drop-in routines (``veris_gb300.model.step``) allocate new output
+tensors on every call, like the reference's functional kernels.  The engine
+instead binds the C ABI once to fixed buffers and replays the same sequence
+of launches every step, which makes the step capturable as one CUDA graph.
+
+Precision modes:
+
+* ``"f64"``: every kernel in float64 (the drop-in arithmetic);
+* ``"f32"``: the EVP subcycles and the advection in float32 with float32
+  accumulation; the dynamics preparation, ocean stress, clean-up, growth
+  (with its solve4temp Newton solve and the heat/fresh-water/salt budgets)
+  and all conservation sums stay float64, and the float64 state remains the
+  master copy.
+
+The step order is the reference setup's (veris/setup/seaice_global_4deg/
+seaice_global_4deg.py:878-932), with all five EVP results stored back.
+"""
+import ctypes
+
+import torch
+
+from . import _abi
+from ._abi import check
+from .state import VerisState, require_device
+from .variables import ABI_ORDER
+
+# fields the float32 EVP and advection read that never change between steps
+STATIC32 = ("maskInC", "maskInU", "maskInV", "iceMask", "iceMaskU", "iceMaskV",
+            "k1AtC", "k2AtC", "k1AtZ", "k2AtZ", "Fu", "Fv", "fCori", "R_low",
+            "dxC", "dyC", "dxG", "dyG", "dxU", "dyU", "dxV", "dyV",
+            "recip_dxC", "recip_dyC", "recip_dxG", "recip_dyG",
+            "recip_dxU", "recip_dyU", "recip_dxV", "recip_dyV",
+            "rA", "rAu", "rAv", "rAz", "recip_rA", "recip_rAu", "recip_rAv", "recip_rAz")
+# fields converted to float32 after the float64 dynamics preparation
+DYNAMIC32 = ("uIce", "vIce", "sigma1", "sigma2", "sigma12",
+             "SeaIceMassC", "SeaIceMassU", "SeaIceMassV", "SeaIceStrength",
+             "AreaW", "AreaS", "WindForcingX", "WindForcingY", "uOcean", "vOcean",
+             "Area", "hIceMean", "hSnowMean")
+EVP_OUT = ("uIce", "vIce", "sigma1", "sigma2", "sigma12")
+GROWTH_OUT = ("hIceMean", "hSnowMean", "Area", "TSurf", "EmPmR", "forc_salt_surface_ice",
+              "Qsw", "Qnet", "SeaIceLoad", "IcePenetSW", "recip_hIceMean")
+FILLED_AFTER_GROWTH = ("hIceMean", "hSnowMean", "Area", "forc_salt_surface_ice", "Qnet")
+
+
+class SeaIceStep:
+    def __init__(self, state: VerisState, precision="f64", n_subcycles=None):
+        if precision not in ("f64", "f32"):
+            raise ValueError("precision must be 'f64' or 'f32'")
+        self.state = state
+        self.precision = precision
+        self.lib = _abi.load()
+        v = state.variables
+        s = state.settings
+        self.shape = tuple(v.iceMask.shape)
+        self.device = v.iceMask.device
+        NX, NY = self.shape
+        self.n_sub = int(s.nEVPsteps if n_subcycles is None else n_subcycles)
+        self.grid = _abi.VerisGrid(NX - 2 * s.olx, NY - 2 * s.oly, s.olx, s.oly, NY)
+        self.params = _abi.params_from_settings(s)
+        self.cells = (NX - 2 * s.olx) * (NY - 2 * s.oly)
+        for n in ABI_ORDER:
+            if getattr(v, n, None) is None:
+                setattr(v, n, torch.zeros(self.shape, dtype=torch.float64, device=self.device))
+            setattr(v, n, require_device(getattr(v, n), n, torch.float64, self.shape))
+        self.f64 = _abi.VerisFields(**{n: getattr(v, n).data_ptr() for n in ABI_ORDER})
+        e = lambda dt=torch.float64: torch.empty(self.shape, dtype=dt, device=self.device)
+        self.evp_out = [e() for _ in EVP_OUT]
+        self.tmp = [e() for _ in range(2)]
+        self.ws_evp = torch.empty(self.lib.veris_evp_workspace_bytes(ctypes.byref(self.grid), 8),
+                                  dtype=torch.uint8, device=self.device)
+        self.ws_adv = torch.empty(self.lib.veris_advection_workspace_bytes(ctypes.byref(self.grid), 8),
+                                  dtype=torch.uint8, device=self.device)
+        if precision == "f32":
+            self.v32 = {n: e(torch.float32) for n in STATIC32 + DYNAMIC32}
+            self.evp_out32 = [e(torch.float32) for _ in EVP_OUT]
+            self.adv_out32 = [e(torch.float32) for _ in range(3)]
+            # the EVP reads the velocities it starts from; the advection reads
+            # the new ones: two float32 tables differing only in uIce/vIce
+            self.f32 = _abi.VerisFields()
+            for n in ABI_ORDER:
+                if n in self.v32:
+                    setattr(self.f32, n, self.v32[n].data_ptr())
+            self.f32_adv = _abi.VerisFields.from_buffer_copy(self.f32)
+            self.f32_adv.uIce = self.evp_out32[0].data_ptr()
+            self.f32_adv.vIce = self.evp_out32[1].data_ptr()
+            for n in STATIC32:
+                self._to32(getattr(v, n), self.v32[n])
+        self.graph = None
+        self.launches_per_step = None
+
+    # ------------------------------------------------------------ helpers
+    @property
+    def stream(self):
+        return torch.cuda.current_stream(self.device).cuda_stream
+
+    def _refs(self, fields):
+        return ctypes.byref(self.grid), ctypes.byref(self.params), ctypes.byref(fields)
+
+    def _to32(self, src, dst):
+        check("convert", self.lib.veris_convert_f64_to_f32(src.data_ptr(), dst.data_ptr(), src.numel(),
+                                                           self.stream))
+
+    def _to64(self, src, dst):
+        check("convert", self.lib.veris_convert_f32_to_f64(src.data_ptr(), dst.data_ptr(), src.numel(),
+                                                           self.stream))
+
+    # --------------------------------------------------------------- step
+    def _enqueue(self, evp_events=None):
+        """Enqueue one step on the current stream; returns the launch count."""
+        lib, v, st = self.lib, self.state.variables, self.stream
+        r64 = self._refs(self.f64)
+        n = 0
+        check("SeaIceMass", lib.veris_sea_ice_mass_f64(*r64, v.SeaIceMassC.data_ptr(), v.SeaIceMassU.data_ptr(),
+                                                       v.SeaIceMassV.data_ptr(), st))
+        check("AreaWS", lib.veris_area_ws_f64(*r64, v.AreaW.data_ptr(), v.AreaS.data_ptr(), st))
+        check("WindForcingXY", lib.veris_wind_forcing_xy_f64(*r64, v.WindForcingX.data_ptr(),
+                                                             v.WindForcingY.data_ptr(), st))
+        check("SeaIceStrength", lib.veris_sea_ice_strength_f64(*r64, v.SeaIceStrength.data_ptr(), st))
+        n += 4
+        if evp_events:
+            evp_events[0].record()
+        if self.precision == "f64":
+            check("evp_solver", lib.veris_evp_solver_f64(*r64, self.n_sub, *[t.data_ptr() for t in self.evp_out],
+                                                         self.ws_evp.data_ptr(), self.ws_evp.numel(), st))
+            n += self.n_sub
+            if evp_events:
+                evp_events[1].record()
+            for name, t in zip(EVP_OUT, self.evp_out):
+                getattr(v, name).copy_(t)
+        else:
+            for name in DYNAMIC32:
+                self._to32(getattr(v, name), self.v32[name])
+            n += len(DYNAMIC32)
+            r32 = self._refs(self.f32)
+            check("evp_solver_f32", lib.veris_evp_solver_f32(*r32, self.n_sub,
+                                                             *[t.data_ptr() for t in self.evp_out32],
+                                                             self.ws_evp.data_ptr(), self.ws_evp.numel(), st))
+            n += self.n_sub
+            if evp_events:
+                evp_events[1].record()
+            for name, t in zip(EVP_OUT, self.evp_out32):
+                self._to64(t, getattr(v, name))
+            n += len(EVP_OUT)
+        check("OceanStressUV", lib.veris_ocean_stress_uv_f64(*r64, v.OceanStressU.data_ptr(),
+                                                             v.OceanStressV.data_ptr(), st))
+        n += 1
+        if self.precision == "f64":
+            # the last advection phase reads only its workspace: in place is safe
+            check("Advection", lib.veris_advection_f64(*r64, v.hIceMean.data_ptr(), v.hSnowMean.data_ptr(),
+                                                       v.Area.data_ptr(), self.ws_adv.data_ptr(),
+                                                       self.ws_adv.numel(), st))
+            n += 5
+        else:
+            check("Advection_f32", lib.veris_advection_f32(*self._refs(self.f32_adv),
+                                                           *[t.data_ptr() for t in self.adv_out32],
+                                                           self.ws_adv.data_ptr(), self.ws_adv.numel(), st))
+            n += 5
+            for name, t in zip(("hIceMean", "hSnowMean", "Area"), self.adv_out32):
+                self._to64(t, getattr(v, name))
+            n += 3
+        # pointwise routines run in place on the state
+        check("clean_up_advection", lib.veris_clean_up_advection_f64(
+            *r64, v.hIceMean.data_ptr(), v.hSnowMean.data_ptr(), v.Area.data_ptr(), v.TSurf.data_ptr(),
+            v.os_hIceMean.data_ptr(), v.os_hSnowMean.data_ptr(), st))
+        check("ridging", lib.veris_ridging_f64(*r64, v.Area.data_ptr(), st))
+        check("Growth", lib.veris_growth_f64(*r64, *[getattr(v, k).data_ptr() for k in GROWTH_OUT], st))
+        n += 3
+        for name in FILLED_AFTER_GROWTH:
+            check("fill_overlap", lib.veris_fill_overlap_f64(ctypes.byref(self.grid), ctypes.byref(self.params),
+                                                             getattr(v, name).data_ptr(), st))
+        n += len(FILLED_AFTER_GROWTH)
+        return n
+
+    def step(self):
+        """Run one step (replays the CUDA graph when one was captured)."""
+        if self.graph is not None:
+            self.graph.replay()
+        else:
+            self.launches_per_step = self._enqueue()
+
+    def capture(self):
+        """Capture one step as a CUDA graph (after one eager warm-up step)."""
+        self.step()
+        torch.cuda.synchronize(self.device)
+        g = torch.cuda.CUDAGraph()
+        s = torch.cuda.Stream(self.device)
+        s.wait_stream(torch.cuda.current_stream(self.device))
+        with torch.cuda.stream(s):
+            with torch.cuda.graph(g, stream=s):
+                self.launches_per_step = self._enqueue()
+        torch.cuda.current_stream(self.device).wait_stream(s)
+        self.graph = g
+        return g
+
+    def timed_step(self):
+        """One eager step with CUDA events around the EVP phase; returns the
+        EVP milliseconds after synchronising."""
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        self.launches_per_step = self._enqueue(evp_events=ev)
+        ev[1].synchronize()
+        return ev[0].elapsed_time(ev[1])
