@@ -56,6 +56,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--subcycles", type=int, default=None, help="override the workload's subcycles")
     ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--evp", default="auto", choices=("auto", "fast", "plain"))
     return ap.parse_args()
 
 
@@ -275,7 +276,7 @@ def run_ours(args):
     cells = c["nx"] * c["ny"]
 
     state = VerisState.from_numpy(arrays, sett, device=dev)
-    eng = SeaIceStep(state, precision=args.precision)
+    eng = SeaIceStep(state, precision=args.precision, evp=args.evp)
     eng.capture()
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
     for _ in range(args.warmup):
@@ -317,7 +318,8 @@ def run_ours(args):
     traffic = recorded_traffic(args.precision)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": traffic,
-                "kernel": f"evp_subcycle_kernel<{'float' if args.precision == 'f32' else 'double'}>",
+                "kernel": ("evp_fast_kernel" if eng.evp_form == "fast" else "evp_subcycle_kernel")
+                + f"<{'float' if args.precision == 'f32' else 'double'}>",
                 "algorithmic_bytes_per_launch": algo_bytes, "avg_launch_us": per_launch_s * 1e6,
                 "peak_source": f"{peak_kind} HBM copy bandwidth"}
 
@@ -329,7 +331,7 @@ def run_ours(args):
                        "dt_s": c["dt"], "cells": cells, "precision": args.precision,
                        "parallelism": "replicas" if ws > 1 else "single-gpu",
                        "l2": "flushed before every timed step (512 MiB write)",
-                       "graph": "one CUDA graph per step"},
+                       "graph": "one CUDA graph per step", "evp_form": eng.evp_form},
             "roofline": roofline, "gpu_launches": launches, "clocks": clk,
             "wall_s_timed_region": wall, "evp_ms_per_step": evp_ms}
 
@@ -355,7 +357,7 @@ def run_ours(args):
     if not args.no_fp64 and args.precision == "f32":
         n_cmp = max(2, args.warmup + args.steps)
         st64 = VerisState.from_numpy(arrays, sett, device=dev)
-        e64 = SeaIceStep(st64, precision="f64")
+        e64 = SeaIceStep(st64, precision="f64", evp=args.evp)
         e64.capture()
         torch.cuda.synchronize(dev)
         t64 = []
@@ -370,11 +372,12 @@ def run_ours(args):
             t64.append(a.elapsed_time(b))
         fp64_ms = float(np.median(t64[-min(len(t64), args.steps):]))
         fp64_value = cells * n_sub / (fp64_ms / 1e3) / 1e9
-        line["fp64"] = {"value": fp64_value, "ms_per_step": fp64_ms, "steps_compared": n_cmp}
+        line["fp64"] = {"value": fp64_value, "ms_per_step": fp64_ms, "steps_compared": n_cmp,
+                        "evp_form": e64.evp_form}
         line["fp32_over_fp64_speedup"] = (value / ws) / fp64_value
         # rerun float32 from the initial state for exactly n_cmp steps
         st32 = VerisState.from_numpy(arrays, sett, device=dev)
-        e32 = SeaIceStep(st32, precision="f32")
+        e32 = SeaIceStep(st32, precision="f32", evp=args.evp)
         e32.capture()
         for _ in range(n_cmp - 1):
             e32.step()

@@ -197,6 +197,41 @@ int veris_evp_solver_f32(const VerisGrid *g, const VerisParams *p, const VerisFi
                          float *sigma2, float *sigma12, void *workspace,
                          size_t workspace_bytes, veris_stream_t s);
 
+/*
+ * The same loop (veris/evp_solver.py:21-319), fast form: a prep kernel folds
+ * the step constants of the float64 state into compact arrays of the
+ * arithmetic type, then one shared-memory-staged kernel per subcycle.  Reads
+ * the float64 field table; writes the five results in the arithmetic type.
+ * Covers the default rheology: veris_evp_fast_settings_check() returns the
+ * settings it does not cover (0 = all covered) and veris_evp_fast_check()
+ * ORs into *violations_device the state properties it does not cover
+ * (non-zero k1/k2 metric terms, masks other than 0/1, grid lengths varying
+ * along both axes).  A non-zero answer means: use the plain form.
+ */
+size_t veris_evp_fast_workspace_bytes(const VerisGrid *g, int32_t elem_size);
+int veris_evp_fast_settings_check(const VerisParams *p);
+int veris_evp_fast_check(const VerisGrid *g, const VerisParams *p, const VerisFieldsF64 *vs,
+                         int32_t *violations_device, veris_stream_t s);
+int veris_evp_fast_solver_f32(const VerisGrid *g, const VerisParams *p, const VerisFieldsF64 *vs,
+                              int32_t n_subcycles, float *uIce, float *vIce, float *sigma1,
+                              float *sigma2, float *sigma12, void *workspace,
+                              size_t workspace_bytes, veris_stream_t s);
+int veris_evp_fast_solver_f64(const VerisGrid *g, const VerisParams *p, const VerisFieldsF64 *vs,
+                              int32_t n_subcycles, double *uIce, double *vIce, double *sigma1,
+                              double *sigma2, double *sigma12, void *workspace,
+                              size_t workspace_bytes, veris_stream_t s);
+/* the float32 fast form without TMA staging (the shared-memory kernel only) */
+int veris_evp_smem_solver_f32(const VerisGrid *g, const VerisParams *p, const VerisFieldsF64 *vs,
+                              int32_t n_subcycles, float *uIce, float *vIce, float *sigma1,
+                              float *sigma2, float *sigma12, void *workspace,
+                              size_t workspace_bytes, veris_stream_t s);
+/*
+ * Device status word of the last fast solve on this workspace (0 = clean;
+ * bit 0: a bounded TMA wait gave up and the affected tiles were skipped).
+ * Synchronises the stream.
+ */
+int veris_evp_fast_status(const void *workspace, int32_t *status_host, veris_stream_t s);
+
 /* veris/ocean_stress.py:8-40 OceanStressUV */
 int veris_ocean_stress_uv_f64(const VerisGrid *g, const VerisParams *p,
                               const VerisFieldsF64 *vs, double *OceanStressU,

@@ -71,12 +71,12 @@ __host__ __device__ __forceinline__ bool in_yhalo(const Dims &d, int oly, int j)
 }
 
 template <class T>
-__device__ __forceinline__ void store_filled(T *out, const Dims &d, const HaloFill &h, int i,
-                                             int j, T val) {
+__device__ __forceinline__ void store_filled_ld(T *out, int64_t ld, const Dims &d, const HaloFill &h, int i,
+                                                int j, T val) {
     const bool hx = h.x_fill && in_xhalo(d, h.olx, i);
     const bool hy = h.y_fill && in_yhalo(d, h.oly, j);
     if (hx || hy) return;
-    out[d.raw(i, j)] = val;
+    out[(int64_t)i * ld + j] = val;
     // image columns inside the x halo
     int ix[2] = {i, -1};
     if (h.x_fill) {
@@ -94,8 +94,13 @@ __device__ __forceinline__ void store_filled(T *out, const Dims &d, const HaloFi
         for (int b = 0; b < 2; ++b) {
             if (a == 0 && b == 0) continue;
             if (ix[a] < 0 || jy[b] < 0) continue;
-            out[d.raw(ix[a], jy[b])] = val;
+            out[(int64_t)ix[a] * ld + jy[b]] = val;
         }
+}
+
+template <class T>
+__device__ __forceinline__ void store_filled(T *out, const Dims &d, const HaloFill &h, int i, int j, T val) {
+    store_filled_ld(out, d.ld, d, h, i, j, val);
 }
 
 inline HaloFill halo_fill_of(const VerisParams &p) {

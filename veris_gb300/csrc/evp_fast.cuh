@@ -1,0 +1,135 @@
+// Shared pieces of the fast EVP forms (veris/evp_solver.py:21-319): the
+// folded step constants, their once-per-step prep kernel, the support check
+// and the launch interface of the TMA-staged kernel.
+//
+// Internal arrays (constants and the ping-pong state) use their own pitch
+// `lp`, a multiple of 8 elements, so that every row starts on a 32-byte
+// boundary (TMA needs 16); the caller's arrays keep the caller's pitch.
+#pragma once
+
+#include "stencil.cuh"
+
+namespace veris {
+
+// flag bits of the per-cell 32-bit word
+enum : uint32_t {
+    F_MC = 1u << 0,    // iceMask
+    F_INC = 1u << 1,   // maskInC
+    F_MU = 1u << 2,    // iceMaskU
+    F_INU = 1u << 3,   // maskInU
+    F_MV = 1u << 4,    // iceMaskV
+    F_INV = 1u << 5,   // maskInV
+    F_LMU = 1u << 6,   // SeaIceMassU != 0
+    F_LMV = 1u << 7,   // SeaIceMassV != 0
+    F_SOUTH = 1u << 8, // fCori < 0
+    F_SPOS = 1u << 9,  // sign(fCori) = +1
+    F_SNEG = 1u << 10, // sign(fCori) = -1
+};
+
+// settings and state properties the fast forms do not cover
+enum : int {
+    V_ADAPT = 1, V_SLIP = 2, V_SECOND = 4, V_PRESS = 8, V_KTERMS = 16, V_MASKS = 32, V_METRIC = 64
+};
+
+// device status word bits (first word of the fast workspace)
+enum : int { S_TMA_TIMEOUT = 1 };
+
+template <class T>
+struct FastConsts {
+    // C points
+    T *Ph;     // 0.5 * P * (1 + tensileStrFac)
+    T *mfC;    // 0.5 * SeaIceMassC * fCori
+    T *qrA;    // 0.25 / rA
+    T *rAz;    // rAz (Z points)
+    T *bfac;   // basal drag factor (only with basalDragK2 != 0)
+    // U points
+    T *mU, *cU, *AW, *uOc, *rrAu;   // cU = mU/dt * u^{n-1} + WindForcingX
+    // V points
+    T *mV, *cV, *AS, *vOc, *rrAv;
+    uint32_t *flags;
+    T *rdxU_x, *rdxV_x, *dxV_x, *dxU_x;   // grid lengths varying with i
+    T *rdyV_y, *rdyU_y, *dyV_y, *dyU_y;   // grid lengths varying with j
+};
+constexpr int N_FAST_2D = 15;
+
+__host__ __device__ inline int64_t internal_pitch(int NY) { return ((int64_t)NY + 7) / 8 * 8; }
+
+inline size_t rup256(size_t x) { return (x + 255) / 256 * 256; }
+
+// Carves the fast workspace: status word, constants, two state buffers.
+template <class T>
+size_t fast_layout(const Dims &d, char *base, FastConsts<T> *c, T *state[2][5], int **status) {
+    const int64_t lp = internal_pitch(d.NY);
+    const size_t f2 = rup256((size_t)d.NX * lp * sizeof(T));
+    const size_t fl = rup256((size_t)d.NX * lp * sizeof(uint32_t));
+    const size_t fx = rup256((size_t)d.NX * sizeof(T)), fy = rup256((size_t)d.NY * sizeof(T));
+    size_t off = 0;
+    auto take = [&](size_t n) { char *p = base ? base + off : nullptr; off += n; return p; };
+    *status = reinterpret_cast<int *>(take(256));
+    T **two[N_FAST_2D] = {&c->Ph, &c->mfC, &c->qrA, &c->rAz, &c->bfac, &c->mU, &c->cU, &c->AW,
+                          &c->uOc, &c->rrAu, &c->mV, &c->cV, &c->AS, &c->vOc, &c->rrAv};
+    for (int q = 0; q < N_FAST_2D; ++q) *two[q] = reinterpret_cast<T *>(take(f2));
+    c->flags = reinterpret_cast<uint32_t *>(take(fl));
+    T **xs[4] = {&c->rdxU_x, &c->rdxV_x, &c->dxV_x, &c->dxU_x};
+    T **ys[4] = {&c->rdyV_y, &c->rdyU_y, &c->dyV_y, &c->dyU_y};
+    for (int q = 0; q < 4; ++q) *xs[q] = reinterpret_cast<T *>(take(fx));
+    for (int q = 0; q < 4; ++q) *ys[q] = reinterpret_cast<T *>(take(fy));
+    for (int b = 0; b < 2; ++b)
+        for (int q = 0; q < 5; ++q) state[b][q] = reinterpret_cast<T *>(take(f2));
+    return off;
+}
+
+template <class T>
+struct FastScalars {
+    T alpha_m1, ralpha, rsq, deltaMin, kp;   // rheology
+    T bU, bU1;                               // beta/dt, (beta+1)/dt
+    T halfCos, sinW;                         // 0.5 cos(turning angle), sin(turning angle)
+    T dN, dS, dN2, dS2, cmin, cmin2;         // ocean drag
+    T U02;                                   // basal U0^2
+};
+
+template <class T>
+FastScalars<T> fast_scalars(const VerisParams &p) {
+    FastScalars<T> s;
+    s.alpha_m1 = (T)(p.evpAlpha - 1.0);
+    s.ralpha = (T)(1.0 / p.evpAlpha);
+    s.rsq = (T)(1.0 / (p.PlasDefCoeff * p.PlasDefCoeff));
+    s.deltaMin = (T)p.deltaMin;
+    s.kp = (T)(2.0 * (1.0 - p.tensileStrFac) / (1.0 + p.tensileStrFac));
+    s.bU = (T)(p.evpBeta * p.recip_deltatDyn);
+    s.bU1 = (T)(p.evpBeta * p.recip_deltatDyn + p.recip_deltatDyn);
+    s.halfCos = (T)(0.5 * p.cosWat);
+    s.sinW = (T)p.sinWat;
+    const double dN = p.waterIceDrag * p.rhoSea, dS = p.waterIceDrag_south * p.rhoSea;
+    s.dN = (T)dN;
+    s.dS = (T)dS;
+    s.dN2 = (T)(dN * dN);
+    s.dS2 = (T)(dS * dS);
+    s.cmin = (T)p.cDragMin;
+    s.cmin2 = (T)(p.cDragMin * p.cDragMin);
+    s.U02 = (T)(p.basalDragU0 * p.basalDragU0);
+    return s;
+}
+
+template <class T>
+struct FastIO {
+    const T *u, *v, *s1, *s2, *s12;   // state at the start of the subcycle (internal pitch)
+    T *uo, *vo, *s1o, *s2o, *s12o;    // state at its end
+    int64_t ldo;                      // pitch of the outputs
+};
+
+int fast_support(const VerisParams &p);
+
+// n float32 subcycles with the TMA-staged kernel, reading state[0] first and
+// writing the last subcycle into outs.  Returns VERIS_ERR_UNSUPPORTED (having
+// launched nothing) when the tensor maps cannot be built; the caller then
+// uses the shared-memory form.
+int evp_tma_subcycles(const Dims &d, const HaloFill &h, const FastConsts<float> &c, const FastScalars<float> &k,
+                      float *const state[2][5], float *const outs[5], int64_t ldo, int n, int *status, bool basal,
+                      bool turn, cudaStream_t st);
+bool evp_tma_available();
+
+template <class T>
+__device__ __forceinline__ T one_if(uint32_t f, uint32_t bit) { return (f & bit) ? T(1) : T(0); }
+
+}  // namespace veris

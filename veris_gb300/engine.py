@@ -45,9 +45,11 @@ FILLED_AFTER_GROWTH = ("hIceMean", "hSnowMean", "Area", "forc_salt_surface_ice",
 
 
 class SeaIceStep:
-    def __init__(self, state: VerisState, precision="f64", n_subcycles=None):
+    def __init__(self, state: VerisState, precision="f64", n_subcycles=None, evp="auto"):
         if precision not in ("f64", "f32"):
             raise ValueError("precision must be 'f64' or 'f32'")
+        if evp not in ("auto", "fast", "plain"):
+            raise ValueError("evp must be 'auto', 'fast' or 'plain'")
         self.state = state
         self.precision = precision
         self.lib = _abi.load()
@@ -68,8 +70,14 @@ class SeaIceStep:
         e = lambda dt=torch.float64: torch.empty(self.shape, dtype=dt, device=self.device)
         self.evp_out = [e() for _ in EVP_OUT]
         self.tmp = [e() for _ in range(2)]
-        self.ws_evp = torch.empty(self.lib.veris_evp_workspace_bytes(ctypes.byref(self.grid), 8),
-                                  dtype=torch.uint8, device=self.device)
+        self.fast_violations = self._fast_violations()
+        if evp == "fast" and self.fast_violations:
+            raise ValueError(f"the fast EVP form does not cover this state (violations {self.fast_violations:#x})")
+        self.evp_form = "plain" if (evp == "plain" or self.fast_violations) else "fast"
+        esize = 8 if precision == "f64" else 4
+        wsb = (self.lib.veris_evp_fast_workspace_bytes(ctypes.byref(self.grid), esize) if self.evp_form == "fast"
+               else self.lib.veris_evp_workspace_bytes(ctypes.byref(self.grid), esize))
+        self.ws_evp = torch.empty(wsb, dtype=torch.uint8, device=self.device)
         self.ws_adv = torch.empty(self.lib.veris_advection_workspace_bytes(ctypes.byref(self.grid), 8),
                                   dtype=torch.uint8, device=self.device)
         if precision == "f32":
@@ -89,6 +97,14 @@ class SeaIceStep:
                 self._to32(getattr(v, n), self.v32[n])
         self.graph = None
         self.launches_per_step = None
+
+    def _fast_violations(self):
+        """Settings and state properties the fast EVP form does not cover (0: none)."""
+        bits = int(self.lib.veris_evp_fast_settings_check(ctypes.byref(self.params)))
+        flag = torch.zeros(1, dtype=torch.int32, device=self.device)
+        check("evp_fast_check", self.lib.veris_evp_fast_check(*self._refs(self.f64), flag.data_ptr(),
+                                                              self.stream))
+        return bits | int(flag.item())
 
     # ------------------------------------------------------------ helpers
     @property
@@ -121,23 +137,27 @@ class SeaIceStep:
         n += 4
         if evp_events:
             evp_events[0].record()
+        ws = (self.ws_evp.data_ptr(), self.ws_evp.numel(), st)
         if self.precision == "f64":
-            check("evp_solver", lib.veris_evp_solver_f64(*r64, self.n_sub, *[t.data_ptr() for t in self.evp_out],
-                                                         self.ws_evp.data_ptr(), self.ws_evp.numel(), st))
-            n += self.n_sub
+            fn = lib.veris_evp_fast_solver_f64 if self.evp_form == "fast" else lib.veris_evp_solver_f64
+            check("evp_solver", fn(*r64, self.n_sub, *[t.data_ptr() for t in self.evp_out], *ws))
+            n += self.n_sub + (1 if self.evp_form == "fast" else 0)
             if evp_events:
                 evp_events[1].record()
             for name, t in zip(EVP_OUT, self.evp_out):
                 getattr(v, name).copy_(t)
         else:
-            for name in DYNAMIC32:
+            conv = DYNAMIC32 if self.evp_form == "plain" else ("hIceMean", "hSnowMean", "Area")
+            for name in conv:
                 self._to32(getattr(v, name), self.v32[name])
-            n += len(DYNAMIC32)
-            r32 = self._refs(self.f32)
-            check("evp_solver_f32", lib.veris_evp_solver_f32(*r32, self.n_sub,
-                                                             *[t.data_ptr() for t in self.evp_out32],
-                                                             self.ws_evp.data_ptr(), self.ws_evp.numel(), st))
-            n += self.n_sub
+            n += len(conv)
+            outs = [t.data_ptr() for t in self.evp_out32]
+            if self.evp_form == "fast":
+                check("evp_fast_f32", lib.veris_evp_fast_solver_f32(*r64, self.n_sub, *outs, *ws))
+                n += self.n_sub + 1
+            else:
+                check("evp_solver_f32", lib.veris_evp_solver_f32(*self._refs(self.f32), self.n_sub, *outs, *ws))
+                n += self.n_sub
             if evp_events:
                 evp_events[1].record()
             for name, t in zip(EVP_OUT, self.evp_out32):
