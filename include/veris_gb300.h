@@ -45,7 +45,8 @@ enum VerisStatus {
     VERIS_ERR_LAUNCH = 5,      /* a CUDA launch or API call failed */
     VERIS_ERR_ARG = 6,         /* a NULL pointer or an invalid argument */
     VERIS_ERR_UNSUPPORTED = 7, /* settings this entry point does not cover */
-    VERIS_ERR_WORKSPACE = 8    /* workspace missing or too small */
+    VERIS_ERR_WORKSPACE = 8,   /* workspace missing or too small */
+    VERIS_ERR_TOO_LARGE = 9    /* grid larger than a fixed-size entry point's scratch */
 };
 
 typedef struct {
@@ -231,6 +232,27 @@ int veris_evp_smem_solver_f32(const VerisGrid *g, const VerisParams *p, const Ve
  * Synchronises the stream.
  */
 int veris_evp_fast_status(const void *workspace, int32_t *status_host, veris_stream_t s);
+
+/*
+ * No counterpart in the reference: an allocation-free form of
+ * veris_evp_solver_f64 for callers that cannot allocate device memory, e.g.
+ * a host model's time loop driving the step through this C ABI with no
+ * device allocator of its own, or running under a device-memory budget fixed
+ * at start-up.  Same kernels and results as veris_evp_solver_f64; the
+ * ping-pong scratch is a fixed array inside the library (VERIS_NOALLOC_MAX_CELLS
+ * padded cells, (nx+4) * ld <= 262144, i.e. 10 MiB of device memory held by
+ * every GPU that loads the library until the process exits).  Larger grids
+ * return VERIS_ERR_TOO_LARGE without launching anything.  The first call on a
+ * device looks up the scratch's device address (cudaGetSymbolAddress) with
+ * that device current: make that first call before any stream capture.
+ * Calls share the scratch: calls that overlap on the GPU (different streams,
+ * or host threads) race on it and must be serialised by the caller.
+ */
+#define VERIS_NOALLOC_MAX_CELLS 262144
+int veris_evp_solver_f64_noalloc(const VerisGrid *g, const VerisParams *p,
+                                 const VerisFieldsF64 *vs, int32_t n_subcycles, double *uIce,
+                                 double *vIce, double *sigma1, double *sigma2, double *sigma12,
+                                 veris_stream_t s);
 
 /* veris/ocean_stress.py:8-40 OceanStressUV */
 int veris_ocean_stress_uv_f64(const VerisGrid *g, const VerisParams *p,

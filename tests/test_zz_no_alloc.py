@@ -1,0 +1,70 @@
+"""The allocation-free EVP entry point, through the C ABI.
+
+veris_evp_solver_f64_noalloc exists for callers that cannot allocate device
+memory (a host model's time loop calling the C ABI without a device allocator
+of its own, or a caller held to a device-memory budget fixed at start-up): it
+keeps its scratch in a fixed array inside the library instead of a
+caller-provided workspace.  This test runs it twice in a row on the same
+inputs and checks both results against the workspace-taking
+veris_evp_solver_f64, at the 1e-10 relative max-norm the parity tests use.
+
+The file is named so that pytest collects it last: a run that stops at the
+first failure has then already run every other test.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+from tests import golden_io as G
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-10
+
+
+@pytest.fixture(scope="module")
+def lib():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from veris_gb300 import _abi
+    return _abi.load()
+
+
+def _call_args(case):
+    from veris_gb300.state import VerisState, Call
+    g = G.load(case)
+    first_evp = [i for i, r, _o in G.sequence(g) if r == "IceVelocities"][0]
+    st0 = G.state_before(g, first_evp)
+    st = VerisState.from_numpy(vars(st0.variables), st0.settings)
+    return Call(st), int(st.settings.nEVPsteps)
+
+
+@pytest.mark.parametrize("case", ("c1", "moving", "small_a"))
+def test_noalloc_matches_workspace_entry_point_twice(lib, case):
+    c, n = _call_args(case)
+    ref = c.empty(5)
+    ws, wsb = c.workspace(lib.veris_evp_workspace_bytes(c.refs()[0], 8))
+    assert lib.veris_evp_solver_f64(*c.refs(), n, *[t.data_ptr() for t in ref], ws, wsb, c.stream) == 0
+    for call in range(2):
+        out = c.empty(5)
+        for t in out:
+            t.fill_(np.nan)
+        st = lib.veris_evp_solver_f64_noalloc(*c.refs(), n, *[t.data_ptr() for t in out], c.stream)
+        assert st == 0, lib.veris_status_string(st)
+        torch.cuda.synchronize()
+        for name, a, b in zip(("uIce", "vIce", "sigma1", "sigma2", "sigma12"), out, ref):
+            e = G.rel_err(a.cpu().numpy(), b.cpu().numpy())
+            assert e <= TOL, f"{case} call {call} {name}: {e:.3e}"
+
+
+def test_noalloc_rejects_grids_beyond_its_scratch(lib):
+    from veris_gb300 import _abi
+    c, n = _call_args("c1")
+    big = _abi.VerisGrid(1024, 512, 2, 2, 516)     # 1028 * 516 padded cells > 262144
+    out = c.empty(5)
+    st = lib.veris_evp_solver_f64_noalloc(ctypes.byref(big), *c.refs()[1:], n, *[t.data_ptr() for t in out],
+                                          c.stream)
+    assert st == 9
+    assert b"fixed scratch" in lib.veris_status_string(st)

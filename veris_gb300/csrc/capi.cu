@@ -75,6 +75,7 @@ const char *veris_status_string(int status) {
         case VERIS_ERR_ARG: return "invalid argument";
         case VERIS_ERR_UNSUPPORTED: return "settings not supported by this entry point";
         case VERIS_ERR_WORKSPACE: return "workspace missing or too small";
+        case VERIS_ERR_TOO_LARGE: return "grid larger than the fixed scratch of the allocation-free entry point";
         default: return "unknown status";
     }
 }

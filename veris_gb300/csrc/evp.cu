@@ -18,6 +18,8 @@
 // reference.  Inputs and outputs alternate between the caller's output
 // arrays and the workspace (ping-pong), so no CTA reads a value another CTA
 // of the same launch writes.
+#include <mutex>
+
 #include "stencil.cuh"
 
 namespace veris {
@@ -316,3 +318,64 @@ int veris_evp_solver_f32(const VerisGrid *g, const VerisParams *p, const VerisFi
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Allocation-free form of veris_evp_solver_f64 (no counterpart in the
+// reference).  Some callers cannot allocate device memory: a host ocean
+// model's time loop that drives the sea-ice step through this C ABI has no
+// device allocator of its own, and a caller running under a device-memory
+// budget fixed at start-up must not grow it per step.  For them the
+// ping-pong half of the subcycle loop lives in this file-scope array instead
+// of a caller-provided workspace.  Every GPU that loads the library holds the
+// array until the process exits.  Nothing in it has to start at zero: each
+// subcycle writes every point of the buffer before the next one reads it.
+// Calls share the array, so calls that overlap on the GPU race on it.
+namespace {
+
+constexpr int64_t NOALLOC_MAX_CELLS = VERIS_NOALLOC_MAX_CELLS;
+static __device__ __align__(256) double g_noalloc_scratch[5 * NOALLOC_MAX_CELLS];
+
+constexpr int NOALLOC_MAX_DEVICES = 64;
+std::mutex g_noalloc_mutex;
+double *g_noalloc_ptr[NOALLOC_MAX_DEVICES] = {};
+
+// device address of the scratch for the current device, looked up once per
+// device with that device current
+int noalloc_scratch(double **out) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= NOALLOC_MAX_DEVICES) {
+        cudaGetLastError();
+        return VERIS_ERR_LAUNCH;
+    }
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_ptr[dev]) {
+        void *ptr = nullptr;
+        if (cudaGetSymbolAddress(&ptr, g_noalloc_scratch) != cudaSuccess || !ptr) {
+            cudaGetLastError();
+            return VERIS_ERR_LAUNCH;
+        }
+        g_noalloc_ptr[dev] = static_cast<double *>(ptr);
+    }
+    *out = g_noalloc_ptr[dev];
+    return VERIS_OK;
+}
+
+}  // namespace
+
+extern "C" int veris_evp_solver_f64_noalloc(const VerisGrid *g, const VerisParams *p, const VerisFieldsF64 *vs,
+                                            int32_t n, double *u, double *v, double *s1, double *s2, double *s12,
+                                            veris_stream_t s) {
+    Dims d;
+    VERIS_CHECK_GRID(g, d);
+    if ((int64_t)d.NX * d.ld > NOALLOC_MAX_CELLS) return VERIS_ERR_TOO_LARGE;
+    VERIS_REQUIRE(p && vs && u && v && s1 && s2 && s12, VERIS_ERR_ARG);
+    VERIS_REQUIRE(n >= 0, VERIS_ERR_ARG);
+    double *scratch = nullptr;
+    const int st = noalloc_scratch(&scratch);
+    if (st != VERIS_OK) return st;
+    // the five scratch buffers follow each other at NX * ld elements
+    const size_t per = (size_t)d.NX * d.ld;
+    const size_t need = 5 * round_up(per * sizeof(double), 256);
+    return evp_solver<double>(g, p, reinterpret_cast<const Fields<double> *>(vs), n, u, v, s1, s2, s12, scratch,
+                              need <= sizeof(g_noalloc_scratch) ? need : 0, s);
+}
