@@ -311,6 +311,8 @@ def run_ours(args):
         flush.zero_()
         evp_ms.append(eng.timed_step())
     evp_ms = float(np.median(evp_ms))
+    flush.zero_()
+    phases = eng.phase_times()
     per_launch_s = evp_ms / 1e3 / n_sub
     algo_bytes = BYTES_PER_CELL_SUBCYCLE[args.precision] * cells
     achieved = algo_bytes / per_launch_s / 1e9
@@ -333,7 +335,8 @@ def run_ours(args):
                        "l2": "flushed before every timed step (512 MiB write)",
                        "graph": "one CUDA graph per step", "evp_form": eng.evp_form},
             "roofline": roofline, "gpu_launches": launches, "clocks": clk,
-            "wall_s_timed_region": wall, "evp_ms_per_step": evp_ms}
+            "wall_s_timed_region": wall, "evp_ms_per_step": evp_ms,
+            "phase_ms": {k: round(v, 4) for k, v in phases.items()}}
 
     # end-to-end through host buffers
     if not args.no_e2e:

@@ -82,6 +82,85 @@ __device__ S4TOut solve4temp_point(const VerisParams &p, const S4TIn &x) {
     return o;
 }
 
+// veris/solve4temp.py:5-174 for NC thickness categories of one cell at once.
+// The categories differ only in their ice and snow thickness; their Newton
+// iterations are independent, so they advance in lockstep and the float64
+// dependency chains interleave.  Per flux evaluation one exp10 gives both
+// 10^(aa1/T) and the saturation vapour pressure 10^(aa2 - aa1/T) =
+// 10^aa2 / 10^(aa1/T), and one reciprocal of T serves every division by T.
+template <int NC>
+__device__ void solve4temp_multi(const VerisParams &p, const S4TIn &x, const double *hI, const double *hS,
+                                 S4TOut *o) {
+    const double aa1 = 2663.5, bb1 = 0.622, Pa = 100000.0;
+    const double one_m_bb1 = 1.0 - bb1;
+    const double cc0 = p.s4t_cc0, cc1 = p.s4t_cc1, cc2 = p.s4t_cc2, d1 = p.s4t_d1, d1i = p.s4t_d1i;
+    const double Tmelt = p.celsius2K, Tmin = p.celsius2K + p.minTIce;
+    const double SurfMeltTemp = Tmelt + p.wetAlbTemp;
+    const double lwc = dmax(p.minLWdown, x.LWdown);
+    const double Ta = dmax(p.celsius2K + p.minTAir, x.ATemp);
+    const double ug = dmax(p.wSpeedMin, x.wSpeed);
+    const double d1ug = d1 * ug, d1iug = d1i * ug;
+    double T[NC], k[NC], d3[NC], lwabs[NC];
+    bool ice[NC];
+#pragma unroll
+    for (int l = 0; l < NC; ++l) {
+        ice[l] = hI[l] > 0;
+        const bool snow = hS[l] > 0;
+        const double emiss = snow ? p.snowEmiss : p.iceEmiss;
+        d3[l] = emiss * p.stefBoltz;
+        const double lw = emiss * lwc;
+        double aI = ice[l] ? p.dryIceAlb : 0.0;
+        double aS = ice[l] ? p.drySnowAlb : 0.0;
+        if (ice[l] && x.Tin >= SurfMeltTemp) { aI = p.wetIceAlb; aS = p.wetSnowAlb; }
+        const bool south = ice[l] && x.fCori < 0;
+        if (south) { aI = p.dryIceAlb_south; aS = p.drySnowAlb_south; }
+        if (south && x.Tin >= SurfMeltTemp) { aI = p.wetIceAlb_south; aS = p.wetSnowAlb_south; }
+        double alb = ice[l] ? aI + hS[l] / p.hCut * (aS - aI) : 0.0;
+        if (hS[l] > p.hCut) alb = aS;
+        if (hS[l] == 0) alb = aI;
+        double pen = ice[l] ? p.shortwave * exp(-1.5 * hI[l]) : 0.0;
+        if (snow) pen = 0.0;
+        o[l].pen = ice[l] ? -(1 - alb) * pen * x.SWdown : 0.0;
+        const double absSW = ice[l] ? (1 - alb) * (1 - pen) * x.SWdown : 0.0;
+        k[l] = ice[l] ? p.iceConduct * p.snowConduct / (p.snowConduct * hI[l] + p.iceConduct * hS[l]) : 0.0;
+        lwabs[l] = -lw - absSW;
+        T[l] = x.Tin;
+    }
+    double Fc[NC], Fia[NC], Flh[NC];
+    auto fluxes = [&](bool newton) {
+#pragma unroll
+        for (int l = 0; l < NC; ++l) {
+            const double t1 = T[l];
+            const double rt = 1.0 / t1;
+            const double t2 = t1 * t1, t3 = t2 * t1, t4 = t2 * t2;
+            const double c3 = exp10(aa1 * rt);
+            const double svp = cc0 / c3;
+            const double qs = bb1 * svp / (Pa - one_m_bb1 * svp);
+            const double den = cc2 - c3 * Pa;
+            const double dqs = cc1 * c3 / (den * den * t2);
+            Fc[l] = ice[l] ? k[l] * (x.TempFrz - t1) : 0.0;
+            Flh[l] = ice[l] ? d1iug * (qs - x.aqh) : 0.0;
+            Fia[l] = ice[l] ? (lwabs[l] + t4 * d3[l] + d1ug * (t1 - Ta) + Flh[l]) : 0.0;
+            if (newton) {
+                const double dF = ice[l] ? 4 * d3[l] * t3 + d1ug + d1iug * dqs : 0.0;
+                double Tn = ice[l] ? t1 + (Fc[l] - Fia[l]) / (k[l] + dF) : 0.0;
+                Tn = dmin(Tn, Tmelt);
+                T[l] = dmax(Tn, Tmin);
+            }
+        }
+    };
+    for (int it = 0; it < 6; ++it) fluxes(true);
+    fluxes(false);
+#pragma unroll
+    for (int l = 0; l < NC; ++l) {
+        const bool up = Fc[l] > 0;
+        o[l].T = ice[l] ? T[l] : x.Tin;
+        o[l].Fio = up ? Fc[l] : 0.0;
+        o[l].Fia = up ? 0.0 : Fia[l];
+        o[l].fw = ice[l] ? Flh[l] / p.lhSublim : 0.0;
+    }
+}
+
 struct GrowthOut {
     double h, hs, A, TSurf, EmPmR, forc_salt, Qsw, Qnet, load, pen, rh;
 };
@@ -115,15 +194,34 @@ __device__ GrowthOut growth_point(const VerisParams &p, const Fields<double> &f,
     x.SWdown = __ldg(f.SWdown + o);
     x.aqh = __ldg(f.aqh + o);
     double Tsum = 0, Fio_sum = 0, Fia_sum = 0, pen_sum = 0;
-    for (int l = 0; l < p.nITC; ++l) {
-        const double pFac = (double)(2 * (l + 1) - 1) * p.recip_nITC;
-        x.hI = hIa * pFac;
-        x.hS = hSa * pFac;
-        const S4TOut r = solve4temp_point(p, x);
-        Tsum = Tsum + r.T;
-        Fio_sum = Fio_sum + r.Fio;
-        Fia_sum = Fia_sum + r.Fia;
-        pen_sum = pen_sum + r.pen;
+    if (p.nITC == 5) {
+        double hIc[5], hSc[5];
+        S4TOut r[5];
+#pragma unroll
+        for (int l = 0; l < 5; ++l) {
+            const double pFac = (double)(2 * (l + 1) - 1) * p.recip_nITC;
+            hIc[l] = hIa * pFac;
+            hSc[l] = hSa * pFac;
+        }
+        solve4temp_multi<5>(p, x, hIc, hSc, r);
+#pragma unroll
+        for (int l = 0; l < 5; ++l) {
+            Tsum = Tsum + r[l].T;
+            Fio_sum = Fio_sum + r[l].Fio;
+            Fia_sum = Fia_sum + r[l].Fia;
+            pen_sum = pen_sum + r[l].pen;
+        }
+    } else {
+        for (int l = 0; l < p.nITC; ++l) {
+            const double pFac = (double)(2 * (l + 1) - 1) * p.recip_nITC;
+            x.hI = hIa * pFac;
+            x.hS = hSa * pFac;
+            const S4TOut r = solve4temp_point(p, x);
+            Tsum = Tsum + r.T;
+            Fio_sum = Fio_sum + r.Fio;
+            Fia_sum = Fia_sum + r.Fia;
+            pen_sum = pen_sum + r.pen;
+        }
     }
     GrowthOut g;
     g.TSurf = Tsum * p.recip_nITC;

@@ -123,11 +123,14 @@ class SeaIceStep:
                                                            self.stream))
 
     # --------------------------------------------------------------- step
-    def _enqueue(self, evp_events=None):
-        """Enqueue one step on the current stream; returns the launch count."""
+    def _enqueue(self, evp_events=None, marks=None):
+        """Enqueue one step on the current stream; returns the launch count.
+        ``marks(name)`` is called between phases (for event timing)."""
         lib, v, st = self.lib, self.state.variables, self.stream
         r64 = self._refs(self.f64)
+        mark = marks if marks is not None else (lambda name: None)
         n = 0
+        mark("start")
         check("SeaIceMass", lib.veris_sea_ice_mass_f64(*r64, v.SeaIceMassC.data_ptr(), v.SeaIceMassU.data_ptr(),
                                                        v.SeaIceMassV.data_ptr(), st))
         check("AreaWS", lib.veris_area_ws_f64(*r64, v.AreaW.data_ptr(), v.AreaS.data_ptr(), st))
@@ -135,6 +138,7 @@ class SeaIceStep:
                                                              v.WindForcingY.data_ptr(), st))
         check("SeaIceStrength", lib.veris_sea_ice_strength_f64(*r64, v.SeaIceStrength.data_ptr(), st))
         n += 4
+        mark("preparation")
         if evp_events:
             evp_events[0].record()
         ws = (self.ws_evp.data_ptr(), self.ws_evp.numel(), st)
@@ -163,9 +167,11 @@ class SeaIceStep:
             for name, t in zip(EVP_OUT, self.evp_out32):
                 self._to64(t, getattr(v, name))
             n += len(EVP_OUT)
+        mark("evp")
         check("OceanStressUV", lib.veris_ocean_stress_uv_f64(*r64, v.OceanStressU.data_ptr(),
                                                              v.OceanStressV.data_ptr(), st))
         n += 1
+        mark("ocean_stress")
         if self.precision == "f64":
             # the last advection phase reads only its workspace: in place is safe
             check("Advection", lib.veris_advection_f64(*r64, v.hIceMean.data_ptr(), v.hSnowMean.data_ptr(),
@@ -180,17 +186,21 @@ class SeaIceStep:
             for name, t in zip(("hIceMean", "hSnowMean", "Area"), self.adv_out32):
                 self._to64(t, getattr(v, name))
             n += 3
+        mark("advection")
         # pointwise routines run in place on the state
         check("clean_up_advection", lib.veris_clean_up_advection_f64(
             *r64, v.hIceMean.data_ptr(), v.hSnowMean.data_ptr(), v.Area.data_ptr(), v.TSurf.data_ptr(),
             v.os_hIceMean.data_ptr(), v.os_hSnowMean.data_ptr(), st))
         check("ridging", lib.veris_ridging_f64(*r64, v.Area.data_ptr(), st))
+        mark("clean_up")
         check("Growth", lib.veris_growth_f64(*r64, *[getattr(v, k).data_ptr() for k in GROWTH_OUT], st))
         n += 3
+        mark("growth")
         for name in FILLED_AFTER_GROWTH:
             check("fill_overlap", lib.veris_fill_overlap_f64(ctypes.byref(self.grid), ctypes.byref(self.params),
                                                              getattr(v, name).data_ptr(), st))
         n += len(FILLED_AFTER_GROWTH)
+        mark("fill")
         return n
 
     def step(self):
@@ -221,3 +231,17 @@ class SeaIceStep:
         self.launches_per_step = self._enqueue(evp_events=ev)
         ev[1].synchronize()
         return ev[0].elapsed_time(ev[1])
+
+    def phase_times(self):
+        """One eager step with CUDA events between its phases; returns
+        {phase: milliseconds} after synchronising."""
+        evs = []
+
+        def mark(name):
+            e = torch.cuda.Event(enable_timing=True)
+            e.record()
+            evs.append((name, e))
+
+        self._enqueue(marks=mark)
+        evs[-1][1].synchronize()
+        return {evs[k][0]: evs[k - 1][1].elapsed_time(evs[k][1]) for k in range(1, len(evs))}
