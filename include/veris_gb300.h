@@ -254,6 +254,27 @@ int veris_evp_solver_f64_noalloc(const VerisGrid *g, const VerisParams *p,
                                  double *vIce, double *sigma1, double *sigma2, double *sigma12,
                                  veris_stream_t s);
 
+/*
+ * Adjoint of veris/evp_solver.py:257-319 (fast form, float64): given the
+ * adjoints of the five outputs of n subcycles (caller pitch), writes the
+ * adjoints of the five inputs (uIce, vIce, sigma1, sigma2, sigma12 at the
+ * start; the uIce/vIce ones include the u^{n-1} terms), ADDS the adjoints of
+ * the step-constant fields the loop reads into *lfields (a table of adjoint
+ * arrays: SeaIceStrength, SeaIceMassC/U/V, WindForcingX/Y, AreaW/S,
+ * uOcean/vOcean, and hIceMean/Area through the basal drag; NULL members are
+ * skipped), and writes d/d waterIceDrag and d/d waterIceDrag_south to
+ * lscalars[0..1].  States are checkpointed every K subcycles (K <= 0: all)
+ * and recomputed segment by segment.
+ */
+size_t veris_evp_adjoint_workspace_bytes(const VerisGrid *g, int32_t elem_size, int32_t n_subcycles,
+                                         int32_t K);
+int veris_evp_adjoint_f64(const VerisGrid *g, const VerisParams *p, const VerisFieldsF64 *vs,
+                          int32_t n_subcycles, int32_t K, const double *l_uIce, const double *l_vIce,
+                          const double *l_sigma1, const double *l_sigma2, const double *l_sigma12,
+                          double *l_uIce0, double *l_vIce0, double *l_sigma10, double *l_sigma20,
+                          double *l_sigma120, const VerisFieldsF64 *lfields, double *lscalars,
+                          void *workspace, size_t workspace_bytes, veris_stream_t s);
+
 /* veris/ocean_stress.py:8-40 OceanStressUV */
 int veris_ocean_stress_uv_f64(const VerisGrid *g, const VerisParams *p,
                               const VerisFieldsF64 *vs, double *OceanStressU,

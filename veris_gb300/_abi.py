@@ -140,6 +140,8 @@ SIGNATURES = {
     "veris_evp_smem_solver_f32": ([_G, _Pa, _F, ctypes.c_int32, _P, _P, _P, _P, _P, _P, _S, _P], _I),
     "veris_evp_fast_status": ([_P, ctypes.POINTER(ctypes.c_int32), _P], _I),
     "veris_evp_solver_f64_noalloc": ([_G, _Pa, _F, ctypes.c_int32, _P, _P, _P, _P, _P, _P], _I),
+    "veris_evp_adjoint_workspace_bytes": ([_G, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32], _S),
+    "veris_evp_adjoint_f64": ([_G, _Pa, _F, ctypes.c_int32, ctypes.c_int32] + [_P] * 10 + [_F, _P, _P, _S, _P], _I),
     "veris_ocean_stress_uv_f64": ([_G, _Pa, _F, _P, _P, _P], _I),
     "veris_limiter_f64": ([_P, _P, _L, _P], _I),
     "veris_calc_zonal_flux_f64": ([_G, _Pa, _F, _P, _P, _P, _P], _I),

@@ -345,6 +345,38 @@ static int launch_fast(const Dims &d, int64_t lp, const HaloFill &h, const FastC
 }
 
 template <class T>
+int fast_prep(const Dims &d, const VerisParams &p, const Fields<double> &f, const FastConsts<T> &c,
+              T *const state0[5], cudaStream_t st) {
+    const int64_t lp = internal_pitch(d.NY);
+    dim3 g2((d.NY + 31) / 32, (d.NX + 7) / 8);
+    if (p.basalDragK2 != 0.0)
+        fast_prep_kernel<T, true><<<g2, dim3(32, 8), 0, st>>>(p, f, d, lp, c, state0[0], state0[1], state0[2],
+                                                              state0[3], state0[4]);
+    else
+        fast_prep_kernel<T, false><<<g2, dim3(32, 8), 0, st>>>(p, f, d, lp, c, state0[0], state0[1], state0[2],
+                                                               state0[3], state0[4]);
+    return launch_status();
+}
+
+template <class T>
+int fast_subcycle(const Dims &d, const HaloFill &h, const FastConsts<T> &c, const FastScalars<T> &k,
+                  const FastIO<T> &io, bool basal, bool turn, cudaStream_t st) {
+    const int64_t lp = internal_pitch(d.NY);
+    if (basal)
+        return turn ? launch_fast<T, true, true>(d, lp, h, c, k, io, st) : launch_fast<T, true, false>(d, lp, h, c, k, io, st);
+    return turn ? launch_fast<T, false, true>(d, lp, h, c, k, io, st) : launch_fast<T, false, false>(d, lp, h, c, k, io, st);
+}
+
+template int fast_prep<float>(const Dims &, const VerisParams &, const Fields<double> &, const FastConsts<float> &,
+                              float *const[5], cudaStream_t);
+template int fast_prep<double>(const Dims &, const VerisParams &, const Fields<double> &, const FastConsts<double> &,
+                               double *const[5], cudaStream_t);
+template int fast_subcycle<float>(const Dims &, const HaloFill &, const FastConsts<float> &, const FastScalars<float> &,
+                                  const FastIO<float> &, bool, bool, cudaStream_t);
+template int fast_subcycle<double>(const Dims &, const HaloFill &, const FastConsts<double> &,
+                                   const FastScalars<double> &, const FastIO<double> &, bool, bool, cudaStream_t);
+
+template <class T>
 static int evp_fast(const VerisGrid *g, const VerisParams *p, const VerisFieldsF64 *vs64, int n, T *uo, T *vo,
                     T *s1o, T *s2o, T *s12o, void *ws, size_t wsb, int allow_tma, veris_stream_t s) {
     Dims d;

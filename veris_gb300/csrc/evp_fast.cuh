@@ -120,6 +120,16 @@ struct FastIO {
 
 int fast_support(const VerisParams &p);
 
+// Host helpers of the fast forms (instantiated for float and double):
+// the once-per-step fold of the constants (and of the initial state into
+// state0), and one shared-memory-form subcycle.
+template <class T>
+int fast_prep(const Dims &d, const VerisParams &p, const Fields<double> &f, const FastConsts<T> &c,
+              T *const state0[5], cudaStream_t st);
+template <class T>
+int fast_subcycle(const Dims &d, const HaloFill &h, const FastConsts<T> &c, const FastScalars<T> &k,
+                  const FastIO<T> &io, bool basal, bool turn, cudaStream_t st);
+
 // n float32 subcycles with the TMA-staged kernel, reading state[0] first and
 // writing the last subcycle into outs.  Returns VERIS_ERR_UNSUPPORTED (having
 // launched nothing) when the tensor maps cannot be built; the caller then
