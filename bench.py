@@ -320,8 +320,9 @@ def run_ours(args):
     traffic = recorded_traffic(args.precision)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": traffic,
-                "kernel": ("evp_fast_kernel" if eng.evp_form == "fast" else "evp_subcycle_kernel")
-                + f"<{'float' if args.precision == 'f32' else 'double'}>",
+                "kernel": ("evp_tma_kernel" if eng.evp_form == "fast" and args.precision == "f32" else
+                           ("evp_fast_kernel" if eng.evp_form == "fast" else "evp_subcycle_kernel")
+                           + f"<{'float' if args.precision == 'f32' else 'double'}>"),
                 "algorithmic_bytes_per_launch": algo_bytes, "avg_launch_us": per_launch_s * 1e6,
                 "peak_source": f"{peak_kind} HBM copy bandwidth"}
 
