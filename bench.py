@@ -57,6 +57,11 @@ def parse():
     ap.add_argument("--subcycles", type=int, default=None, help="override the workload's subcycles")
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--evp", default="auto", choices=("auto", "fast", "plain"))
+    ap.add_argument("--adjoint", action="store_true",
+                    help="time a trajectory's forward + adjoint against its forward (float64)")
+    ap.add_argument("--adjoint-config", default="c3_1deg")
+    ap.add_argument("--adjoint-steps", type=int, default=None)
+    ap.add_argument("--snapshots", type=int, default=None, help="step snapshots (default: all)")
     return ap.parse_args()
 
 
@@ -402,8 +407,112 @@ def run_ours(args):
     return 0
 
 
+def run_adjoint(args):
+    """Gradient of a tracking loss through a float64 trajectory.
+
+    The target is the end state of the same trajectory with P* x 1.2 and the
+    winds of seed + 1; the loss is the interior sum of (u - u*)^2 + (v - v*)^2
+    + (A - A*)^2 at the end.  Times, with CUDA events: the forward alone
+    (graph replays), and the forward with snapshots plus the adjoint sweep.
+    Also checks dL/dP* against a centred difference."""
+    import torch
+    torch.cuda.set_device(0)
+    from __graft_entry__ import build
+    build()
+    from veris_gb300.state import VerisState
+    from veris_gb300.synthetic import CONFIGS, make_state, config_settings
+    from veris_gb300.trajectory import Trajectory, tracking_loss_adjoint
+
+    name = args.adjoint_config
+    c = CONFIGS[name]
+    n_steps = args.adjoint_steps or c["steps"]
+    arrays = make_state(c["nx"], c["ny"], seed=args.seed)
+    winds1 = make_state(c["nx"], c["ny"], seed=args.seed + 1)
+    sett = config_settings(name)
+    if args.subcycles:
+        sett.nEVPsteps = args.subcycles
+    st = VerisState.from_numpy(arrays, sett)
+    v = st.variables
+    tr = Trajectory(st, n_steps, snapshots=args.snapshots)
+    x0 = tr._save()
+    p0 = float(sett.pStar)
+
+    # target: P* x 1.2 and the other seed's winds
+    wind0 = (v.uWind.clone(), v.vWind.clone())
+    v.uWind.copy_(torch.as_tensor(winds1["uWind"]))
+    v.vWind.copy_(torch.as_tensor(winds1["vWind"]))
+    tr.set_coefficients(pStar=1.2 * p0)
+    tr.forward()
+    target = {k: getattr(v, k).clone() for k in ("uIce", "vIce", "Area")}
+    v.uWind.copy_(wind0[0])
+    v.vWind.copy_(wind0[1])
+    tr.set_coefficients(pStar=p0)
+    tr._load(x0)
+
+    def ev():
+        return torch.cuda.Event(enable_timing=True)
+
+    # forward alone: graph replays
+    tr._ensure_graph()
+    fw = []
+    for _ in range(max(1, args.warmup) + 2):
+        tr._load(x0)
+        torch.cuda.synchronize()
+        a, b = ev(), ev()
+        a.record()
+        for _k in range(n_steps):
+            tr.eng.step()
+        b.record()
+        b.synchronize()
+        fw.append(a.elapsed_time(b))
+    t_fwd = float(np.median(fw[1:]))
+
+    # forward with snapshots, then the adjoint
+    res = []
+    for _ in range(2):
+        tr._load(x0)
+        torch.cuda.synchronize()
+        a, m, b = ev(), ev(), ev()
+        a.record()
+        tr.forward()
+        L, lam = tracking_loss_adjoint(st, target)
+        m.record()
+        grads, coeffs, _ = tr.backward(lam)
+        b.record()
+        b.synchronize()
+        res.append((a.elapsed_time(m), m.elapsed_time(b), float(L), float(coeffs["pStar"]), dict(tr.stats)))
+    t_f2, t_adj, L0, dLdP, stats = res[-1]
+
+    # centred difference in P*
+    hP = 1e-6 * p0
+    Ls = []
+    for pv in (p0 + hP, p0 - hP):
+        tr.set_coefficients(pStar=pv)
+        tr._load(x0)
+        tr.forward()
+        Ls.append(float(tracking_loss_adjoint(st, target)[0]))
+    tr.set_coefficients(pStar=p0)
+    fd = (Ls[0] - Ls[1]) / (2 * hP)
+
+    line = {"metric": "trajectory (forward + adjoint) / forward time", "value": (t_f2 + t_adj) / t_fwd,
+            "unit": "x", "higher_is_better": False, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": name, "nx": c["nx"], "ny": c["ny"], "steps": n_steps,
+                       "subcycles": int(sett.nEVPsteps), "dt_s": c["dt"],
+                       "snapshots": tr.snaps, "evp_checkpoint_every": tr.K,
+                       "target": "P* x 1.2 and seed+1 winds", "loss": "interior sum (u-u*)^2+(v-v*)^2+(A-A*)^2"},
+            "forward_ms": t_fwd, "forward_with_snapshots_ms": t_f2, "adjoint_ms": t_adj,
+            "stats": stats, "loss": L0,
+            "dL_dpStar": {"adjoint": dLdP, "centred_difference": fd,
+                          "rel_diff": abs(dLdP - fd) / max(abs(fd), 1e-300)},
+            "gpu_launches_per_forward_step": tr.eng.launches_per_step}
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     args = parse()
+    if args.adjoint:
+        return run_adjoint(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

@@ -328,6 +328,64 @@ int veris_growth_f64(const VerisGrid *g, const VerisParams *p, const VerisFields
                      double *SeaIceLoad, double *IcePenetSW, double *recip_hIceMean,
                      veris_stream_t s);
 
+/* ---- adjoints of the step's other routines (float64) ------------------ */
+/*
+ * Each takes the adjoints of its routine's outputs and the table of the
+ * routine's INPUT state (the same vs its forward call read); the Jacobians
+ * are evaluated at that state, branches (limiters, clipping, masks, the
+ * solve4temp Newton iterations) following the values as in the forward.
+ */
+/* transpose of veris/fill_overlap.py:6-18: lam_out = F^T lam_in (out of place) */
+int veris_fill_overlap_adjoint_f64(const VerisGrid *g, const VerisParams *p,
+                                   const double *lam_in, double *lam_out, veris_stream_t s);
+/*
+ * Adjoint of veris/advection.py:15-91 Advection(state) for hIceMean,
+ * hSnowMean and Area.  l_* are the adjoints of the three outputs; the
+ * adjoints of the three inputs are ADDED into lin_* and those of uIce and
+ * vIce (through the transports and the Courant numbers) into l_u, l_v.
+ */
+size_t veris_advection_adjoint_workspace_bytes(const VerisGrid *g);
+int veris_advection_adjoint_f64(const VerisGrid *g, const VerisParams *p,
+                                const VerisFieldsF64 *vs, const double *l_hIceMean,
+                                const double *l_hSnowMean, const double *l_Area,
+                                double *lin_hIceMean, double *lin_hSnowMean, double *lin_Area,
+                                double *l_uIce, double *l_vIce, void *workspace,
+                                size_t workspace_bytes, veris_stream_t s);
+/*
+ * Adjoint of veris/clean_up.py:5-47 (clean_up_advection then ridging) for
+ * (hIceMean, hSnowMean, Area, TSurf): writes J^T l into o_*.
+ */
+int veris_cleanup_adjoint_f64(const VerisGrid *g, const VerisParams *p, const VerisFieldsF64 *vs,
+                              const double *l_hIceMean, const double *l_hSnowMean,
+                              const double *l_Area, const double *l_TSurf, double *o_hIceMean,
+                              double *o_hSnowMean, double *o_Area, double *o_TSurf,
+                              veris_stream_t s);
+/*
+ * Adjoint of veris/growth.py:8-397 Growth(state) for the ice state
+ * (hIceMean, hSnowMean, Area, TSurf) in -> out: writes J^T l into o_*.
+ * The forcing fields of vs (Qnet, Qsw, ...) must hold the values the
+ * forward call read.
+ */
+int veris_growth_adjoint_f64(const VerisGrid *g, const VerisParams *p, const VerisFieldsF64 *vs,
+                             const double *l_hIceMean, const double *l_hSnowMean,
+                             const double *l_Area, const double *l_TSurf, double *o_hIceMean,
+                             double *o_hSnowMean, double *o_Area, double *o_TSurf,
+                             veris_stream_t s);
+/*
+ * Adjoint of the dynamics preparation: veris/area_mass.py:5-28 SeaIceMass and
+ * AreaWS, veris/dynsolver.py:7-84 WindForcingXY (with tauXY) and
+ * veris/dynamics_routines.py:5-18 SeaIceStrength, for useRealFreshWaterFlux
+ * off.  *lprep holds the adjoints of SeaIceStrength, SeaIceMassC/U/V, AreaW/S
+ * and WindForcingX/Y; the adjoints of hIceMean, hSnowMean, Area, uIce and vIce
+ * are ADDED into l_*, and d/d pStar, d/d airIceDrag and d/d airIceDrag_south
+ * into scalars[0..2].
+ */
+size_t veris_prep_adjoint_workspace_bytes(const VerisGrid *g);
+int veris_prep_adjoint_f64(const VerisGrid *g, const VerisParams *p, const VerisFieldsF64 *vs,
+                           const VerisFieldsF64 *lprep, double *l_hIceMean, double *l_hSnowMean,
+                           double *l_Area, double *l_uIce, double *l_vIce, double *scalars,
+                           void *workspace, size_t workspace_bytes, veris_stream_t s);
+
 /* ---- reductions and conversions -------------------------------------- */
 /*
  * veris/global_sum.py:1-4 is an identity on one process; this is the

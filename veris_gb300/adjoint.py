@@ -3,7 +3,11 @@
 ``evp_adjoint`` is the reverse-mode derivative of the EVP subcycle loop
 (veris/evp_solver.py:257-319) in float64: the adjoints of its five outputs
 in, the adjoints of its five inputs, of the step-constant fields it reads and
-of the water drag coefficients out.
+of the water drag coefficients out.  The other routines of the step have one
+function each (``fill_overlap_adjoint``, ``advection_adjoint``,
+``cleanup_adjoint``, ``growth_adjoint``, ``prep_adjoint``); each takes the
+state its forward read and the adjoints of its outputs.  ``trajectory``
+chains them over many steps.
 """
 import ctypes
 
@@ -41,3 +45,70 @@ def evp_adjoint(state, lam_out, n_subcycles=None, checkpoint_every=0):
         scal.data_ptr(), ws, wsb, c.stream))
     return (dict(zip(EVP_STATE, li)), lf,
             {"waterIceDrag": scal[0], "waterIceDrag_south": scal[1]})
+
+
+ICE = ("hIceMean", "hSnowMean", "Area", "TSurf")
+PREP_OUT = ("SeaIceStrength", "SeaIceMassC", "SeaIceMassU", "SeaIceMassV", "AreaW", "AreaS",
+            "WindForcingX", "WindForcingY")
+
+
+def fill_overlap_adjoint(state, lam):
+    """Transpose of veris/fill_overlap.py:6-18 applied to ``lam``."""
+    c = Call(state)
+    out = c.empty()
+    check("fill_overlap_adjoint", c.lib.veris_fill_overlap_adjoint_f64(
+        c.refs()[0], c.refs()[1], c.arg(lam, "lam"), out.data_ptr(), c.stream))
+    return out
+
+
+def advection_adjoint(state, lam_out):
+    """Adjoint of veris/advection.py:15-91 at ``state``.  ``lam_out``: adjoints
+    of the advected (hIceMean, hSnowMean, Area).  Returns ({hIceMean,
+    hSnowMean, Area: adjoint of the input}, {uIce, vIce: adjoint})."""
+    c = Call(state)
+    lo = [c.arg(lam_out[k], "lam_" + k) for k in ICE[:3]]
+    z = lambda: torch.zeros(c.shape, dtype=torch.float64, device=c.device)
+    li, lu, lv = [z() for _ in range(3)], z(), z()
+    ws, wsb = c.workspace(c.lib.veris_advection_adjoint_workspace_bytes(c.refs()[0]))
+    check("advection_adjoint", c.lib.veris_advection_adjoint_f64(
+        *c.refs(), *lo, *[t.data_ptr() for t in li], lu.data_ptr(), lv.data_ptr(), ws, wsb, c.stream))
+    return dict(zip(ICE[:3], li)), {"uIce": lu, "vIce": lv}
+
+
+def _pointwise4(name, fn, state, lam_out):
+    c = Call(state)
+    lo = [c.arg(lam_out[k], "lam_" + k) for k in ICE]
+    out = c.empty(4)
+    check(name, fn(*c.refs(), *lo, *[t.data_ptr() for t in out], c.stream))
+    return dict(zip(ICE, out))
+
+
+def cleanup_adjoint(state, lam_out):
+    """Adjoint of clean_up_advection followed by ridging (veris/clean_up.py:5-47)
+    for (hIceMean, hSnowMean, Area, TSurf) at ``state``."""
+    return _pointwise4("cleanup_adjoint", Call(state).lib.veris_cleanup_adjoint_f64, state, lam_out)
+
+
+def growth_adjoint(state, lam_out):
+    """Adjoint of Growth (veris/growth.py:8-397) for (hIceMean, hSnowMean, Area,
+    TSurf) at ``state``, whose forcing fields must be the ones Growth read."""
+    return _pointwise4("growth_adjoint", Call(state).lib.veris_growth_adjoint_f64, state, lam_out)
+
+
+def prep_adjoint(state, lam_prep):
+    """Adjoint of SeaIceMass, AreaWS, WindForcingXY and SeaIceStrength at
+    ``state``.  ``lam_prep``: {name in PREP_OUT: adjoint}.  Returns
+    ({hIceMean, hSnowMean, Area, uIce, vIce: adjoint},
+    {pStar, airIceDrag, airIceDrag_south: 0-d tensor})."""
+    c = Call(state)
+    z = lambda: torch.zeros(c.shape, dtype=torch.float64, device=c.device)
+    lp = {k: (lam_prep[k] if k in lam_prep else z()) for k in PREP_OUT}
+    table = VerisFields(**{k: c.arg(t, "lam_" + k) for k, t in lp.items()})
+    names = ("hIceMean", "hSnowMean", "Area", "uIce", "vIce")
+    out = {k: z() for k in names}
+    scal = torch.zeros(3, dtype=torch.float64, device=c.device)
+    ws, wsb = c.workspace(c.lib.veris_prep_adjoint_workspace_bytes(c.refs()[0]))
+    check("prep_adjoint", c.lib.veris_prep_adjoint_f64(
+        *c.refs(), ctypes.byref(table), *[out[k].data_ptr() for k in names], scal.data_ptr(), ws, wsb,
+        c.stream))
+    return out, {"pStar": scal[0], "airIceDrag": scal[1], "airIceDrag_south": scal[2]}

@@ -728,7 +728,7 @@ static int evp_adjoint(const VerisGrid *g, const VerisParams *p, const VerisFiel
         if (cudaMemcpy2DAsync(lin[q], d.ld * sizeof(T), l0[q], lp * sizeof(T), d.NY * sizeof(T), d.NX,
                               cudaMemcpyDeviceToDevice, st) != cudaSuccess)
             return VERIS_ERR_LAUNCH;
-    // scalar gradients: add to the caller's accumulators
+    // scalar gradients: written to the caller's two values
     if (cudaMemcpyAsync(lscal, pl.a.dragN, 2 * sizeof(double), cudaMemcpyDeviceToDevice, st) != cudaSuccess)
         return VERIS_ERR_LAUNCH;
     return VERIS_OK;

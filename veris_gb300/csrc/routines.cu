@@ -55,6 +55,33 @@ static int fill_overlap(const VerisGrid *g, const VerisParams *p, T *A, veris_st
     return launch_status();
 }
 
+// transpose of the halo fill, out of place: the adjoint held by each halo
+// image moves onto its interior source and the image's own becomes zero
+__global__ void fill_adjoint_kernel(const double *lin, double *lout, Dims d, HaloFill h) {
+    const int j = blockIdx.x * BX + threadIdx.x;
+    const int i = blockIdx.y * BY + threadIdx.y;
+    if (i >= d.NX || j >= d.NY) return;
+    const int64_t o = d.raw(i, j);
+    if ((h.x_fill && in_xhalo(d, h.olx, i)) || (h.y_fill && in_yhalo(d, h.oly, j))) {
+        lout[o] = 0.0;
+        return;
+    }
+    int ix = -1, jy = -1;
+    if (h.x_fill) {
+        if (i + d.nx < d.NX && in_xhalo(d, h.olx, i + d.nx)) ix = i + d.nx;
+        else if (i - d.nx >= 0 && in_xhalo(d, h.olx, i - d.nx)) ix = i - d.nx;
+    }
+    if (h.y_fill) {
+        if (j + d.ny < d.NY && in_yhalo(d, h.oly, j + d.ny)) jy = j + d.ny;
+        else if (j - d.ny >= 0 && in_yhalo(d, h.oly, j - d.ny)) jy = j - d.ny;
+    }
+    double acc = lin[o];
+    if (ix >= 0) acc += lin[d.raw(ix, j)];
+    if (jy >= 0) acc += lin[d.raw(i, jy)];
+    if (ix >= 0 && jy >= 0) acc += lin[d.raw(ix, jy)];
+    lout[o] = acc;
+}
+
 // ------------------------------------------------------- step preparation
 template <class T>
 __global__ void sea_ice_mass_kernel(Ctx<T> c, T *mC, T *mU, T *mV) {
@@ -244,6 +271,105 @@ __global__ void ocean_stress_kernel(Ctx<T> c, HaloFill h, T *su, T *sv) {
     store_filled(sv, c.d, h, i, j, ov);
 }
 
+// ------------------------------------------------ dynamics-preparation adjoint
+// Reverse of SeaIceMass, AreaWS, WindForcingXY (with tauXY) and SeaIceStrength
+// (veris/area_mass.py:5-28, veris/dynsolver.py:7-84,
+// veris/dynamics_routines.py:5-18), in float64, as three gather passes.
+struct PrepAdj {
+    // adjoints of the preparation's outputs (inputs of this pass)
+    const double *lP, *lmC, *lmU, *lmV, *lAW, *lAS, *lWX, *lWY;
+    // scratch: totals at U/V points and the wind-stress adjoints at C points
+    double *ltX, *ltY, *lAWt, *lASt, *lmUt, *lmVt, *lur, *lvr;
+    // accumulated adjoints of the ice state
+    double *lh, *lhs, *lA, *lu, *lv;
+    double *scal;   // [0] P*, [1] airIceDrag, [2] airIceDrag_south
+};
+
+__global__ void prep_adj_uv_kernel(Ctx<double> c, PrepAdj a) {
+    POINT_IJ
+    double tX, tY;
+    tau_uv(c, i, j, tX, tY);
+    const double phi = phi_surf(c, i, j);
+    const double lwx = a.lWX[k], lwy = a.lWY[k];
+    // AreaW/AreaS of this state (the table's may be another step's)
+    const double A0 = c.ld(c.f.Area, i, j);
+    a.ltX[k] = 0.5 * (A0 + c.ld(c.f.Area, i - 1, j)) * lwx;
+    a.ltY[k] = 0.5 * (A0 + c.ld(c.f.Area, i, j - 1)) * lwy;
+    a.lAWt[k] = a.lAW[k] + tX * lwx;
+    a.lASt[k] = a.lAS[k] + tY * lwy;
+    a.lmUt[k] = a.lmU[k] - c.ld(c.f.recip_dxC, i, j) * (phi - phi_surf(c, i - 1, j)) * lwx;
+    a.lmVt[k] = a.lmV[k] - c.ld(c.f.recip_dyC, i, j) * (phi - phi_surf(c, i, j - 1)) * lwy;
+}
+
+__global__ void prep_adj_c_kernel(Ctx<double> c, PrepAdj a) {
+    const int j = blockIdx.x * BX + threadIdx.x;
+    const int i = blockIdx.y * BY + threadIdx.y;
+    double sP = 0.0, sN = 0.0, sS = 0.0;
+    if (i < c.d.NX && j < c.d.NY) {
+        const int64_t k = c.d.raw(i, j);
+        const Fields<double> &f = c.f;
+        // wind stress at C: tauX(U i) = 0.5 (tx(i) + tx(i-1)) mskU(i)
+        const double ltx = 0.5 * (c.ld(f.iceMaskU, i, j) * a.ltX[k] + c.ld(f.iceMaskU, i + 1, j) * a.ltX[c.d.at(i + 1, j)]);
+        const double lty = 0.5 * (c.ld(f.iceMaskV, i, j) * a.ltY[k] + c.ld(f.iceMaskV, i, j + 1) * a.ltY[c.d.at(i, j + 1)]);
+        double urel, vrel;
+        if (c.p.useRelativeWind) {
+            urel = c.ld(f.uWind, i, j) - 0.5 * (c.ld(f.uIce, i, j) + c.ld(f.uIce, i + 1, j));
+            vrel = c.ld(f.vWind, i, j) - 0.5 * (c.ld(f.vIce, i, j) + c.ld(f.vIce, i, j + 1));
+        } else {
+            urel = c.ld(f.uWind, i, j);
+            vrel = c.ld(f.vWind, i, j);
+        }
+        const double ws2 = urel * urel + vrel * vrel;
+        const bool floored = ws2 < c.p.wSpeedMin * c.p.wSpeedMin;
+        const double speed = floored ? c.p.wSpeedMin : sqrt(ws2);
+        const double fc = c.ld(f.fCori, i, j);
+        const bool south = fc < 0;
+        const double D = (south ? c.p.airIceDrag_south : c.p.airIceDrag) * c.p.rhoAir;
+        const double sg = sgn(fc), cw = c.p.cosWin, sw = c.p.sinWin;
+        const double ax = cw * urel - sg * sw * vrel, ay = cw * vrel + sg * sw * urel;
+        const double su = floored ? 0.0 : urel / speed, sv = floored ? 0.0 : vrel / speed;
+        // tx = D speed ax, ty = D speed ay
+        a.lur[k] = D * (ltx * (su * ax + speed * cw) + lty * (su * ay + speed * sg * sw));
+        a.lvr[k] = D * (ltx * (sv * ax - speed * sg * sw) + lty * (sv * ay + speed * cw));
+        const double lD = c.p.rhoAir * speed * (ltx * ax + lty * ay);
+        if (south) sS = lD; else sN = lD;
+        // ice strength P = P* h exp(-C* (1 - A)) mask
+        const double h = c.ld(f.hIceMean, i, j), A = c.ld(f.Area, i, j), m = c.ld(f.iceMask, i, j);
+        const double e = exp(-c.p.cStar * (1.0 - A));
+        const double lP = a.lP[k];
+        sP = lP * h * e * m;
+        double lh = lP * c.p.pStar * e * m, lA = lP * c.p.pStar * h * e * c.p.cStar * m;
+        // masses: mU(i) = (mC(i) + mC(i-1))/2, mV(j) = (mC(j) + mC(j-1))/2
+        const double lmC = a.lmC[k] + 0.5 * (a.lmUt[k] + a.lmUt[c.d.at(i + 1, j)]) +
+                           0.5 * (a.lmVt[k] + a.lmVt[c.d.at(i, j + 1)]);
+        lh += c.p.rhoIce * lmC;
+        a.lhs[k] += c.p.rhoSnow * lmC;
+        // areas: AW(i) = (A(i) + A(i-1))/2, AS(j) = (A(j) + A(j-1))/2
+        lA += 0.5 * (a.lAWt[k] + a.lAWt[c.d.at(i + 1, j)]) + 0.5 * (a.lASt[k] + a.lASt[c.d.at(i, j + 1)]);
+        a.lh[k] += lh;
+        a.lA[k] += lA;
+    }
+    // scalar sums: warp shuffles, one atomic per warp
+    for (int off = 16; off > 0; off >>= 1) {
+        sP += __shfl_down_sync(0xffffffffu, sP, off);
+        sN += __shfl_down_sync(0xffffffffu, sN, off);
+        sS += __shfl_down_sync(0xffffffffu, sS, off);
+    }
+    if (threadIdx.x == 0) {
+        if (sP != 0.0) atomicAdd(a.scal + 0, sP);
+        if (sN != 0.0) atomicAdd(a.scal + 1, sN);
+        if (sS != 0.0) atomicAdd(a.scal + 2, sS);
+    }
+}
+
+__global__ void prep_adj_vel_kernel(Ctx<double> c, PrepAdj a) {
+    POINT_IJ
+    if (!c.p.useRelativeWind) return;
+    // urel(C i) = uWind - (u(i) + u(i+1))/2: u(i) enters C(i) and C(i-1)
+    a.lu[k] += -0.5 * (a.lur[k] + a.lur[c.d.at(i - 1, j)]);
+    a.lv[k] += -0.5 * (a.lvr[k] + a.lvr[c.d.at(i, j - 1)]);
+}
+
 }  // namespace veris
 
 using namespace veris;
@@ -260,6 +386,14 @@ extern "C" {
 
 int veris_fill_overlap_f64(const VerisGrid *g, const VerisParams *p, double *A, veris_stream_t s) {
     return fill_overlap<double>(g, p, A, s);
+}
+int veris_fill_overlap_adjoint_f64(const VerisGrid *g, const VerisParams *p, const double *lam_in,
+                                   double *lam_out, veris_stream_t s) {
+    Dims d;
+    VERIS_CHECK_GRID(g, d);
+    VERIS_REQUIRE(p && lam_in && lam_out && lam_in != lam_out, VERIS_ERR_ARG);
+    fill_adjoint_kernel<<<grid2d(d), dim3(BX, BY), 0, (cudaStream_t)s>>>(lam_in, lam_out, d, halo_fill_of(*p));
+    return launch_status();
 }
 int veris_fill_overlap_f32(const VerisGrid *g, const VerisParams *p, float *A, veris_stream_t s) {
     return fill_overlap<float>(g, p, A, s);
@@ -361,6 +495,47 @@ int veris_stressdiv_f64(const VerisGrid *g, const VerisParams *p, const VerisFie
     PREP_BEGIN(double, VerisFieldsF64)
     VERIS_REQUIRE(s11 && s22 && s12 && dX && dY, VERIS_ERR_ARG);
     stressdiv_kernel<double><<<gr, bl, 0, st>>>(c, s11, s22, s12, dX, dY);
+    return launch_status();
+}
+
+size_t veris_prep_adjoint_workspace_bytes(const VerisGrid *g) {
+    Dims d;
+    if (check_grid(g, &d) != VERIS_OK) return 0;
+    return 8 * (((size_t)d.NX * d.ld * sizeof(double) + 255) / 256 * 256);
+}
+
+int veris_prep_adjoint_f64(const VerisGrid *g, const VerisParams *p, const VerisFieldsF64 *vs,
+                           const VerisFieldsF64 *lprep, double *lh, double *lhs, double *lA, double *lu, double *lv,
+                           double *scalars, void *ws, size_t wsb, veris_stream_t s) {
+    PREP_BEGIN(double, VerisFieldsF64)
+    VERIS_REQUIRE(lprep && lh && lhs && lA && lu && lv && scalars, VERIS_ERR_ARG);
+    VERIS_REQUIRE(!p->useRealFreshWaterFlux, VERIS_ERR_UNSUPPORTED);
+    const size_t fb = ((size_t)d.NX * d.ld * sizeof(double) + 255) / 256 * 256;
+    VERIS_REQUIRE(ws && wsb >= 8 * fb, VERIS_ERR_WORKSPACE);
+    const VerisFieldsF64 &L = *lprep;
+    VERIS_REQUIRE(L.SeaIceStrength && L.SeaIceMassC && L.SeaIceMassU && L.SeaIceMassV && L.AreaW && L.AreaS &&
+                      L.WindForcingX && L.WindForcingY,
+                  VERIS_ERR_ARG);
+    PrepAdj a;
+    a.lP = L.SeaIceStrength;
+    a.lmC = L.SeaIceMassC;
+    a.lmU = L.SeaIceMassU;
+    a.lmV = L.SeaIceMassV;
+    a.lAW = L.AreaW;
+    a.lAS = L.AreaS;
+    a.lWX = L.WindForcingX;
+    a.lWY = L.WindForcingY;
+    double **scr[8] = {&a.ltX, &a.ltY, &a.lAWt, &a.lASt, &a.lmUt, &a.lmVt, &a.lur, &a.lvr};
+    for (int q = 0; q < 8; ++q) *scr[q] = reinterpret_cast<double *>(static_cast<char *>(ws) + q * fb);
+    a.lh = lh;
+    a.lhs = lhs;
+    a.lA = lA;
+    a.lu = lu;
+    a.lv = lv;
+    a.scal = scalars;
+    prep_adj_uv_kernel<<<gr, bl, 0, st>>>(c, a);
+    prep_adj_c_kernel<<<gr, bl, 0, st>>>(c, a);
+    prep_adj_vel_kernel<<<gr, bl, 0, st>>>(c, a);
     return launch_status();
 }
 

@@ -2,6 +2,7 @@
 // (veris/solve4temp.py:5-174) and ice growth with the ocean budgets
 // (veris/growth.py:8-397).  Both are pointwise; one thread per padded point.
 #include "stencil.cuh"
+#include "dual.cuh"
 
 namespace veris {
 
@@ -88,9 +89,11 @@ __device__ S4TOut solve4temp_point(const VerisParams &p, const S4TIn &x) {
 // dependency chains interleave.  Per flux evaluation one exp10 gives both
 // 10^(aa1/T) and the saturation vapour pressure 10^(aa2 - aa1/T) =
 // 10^aa2 / 10^(aa1/T), and one reciprocal of T serves every division by T.
-template <int NC>
-__device__ void solve4temp_multi(const VerisParams &p, const S4TIn &x, const double *hI, const double *hS,
-                                 S4TOut *o) {
+// S is double, or a dual number when the adjoint needs the derivatives with
+// respect to the ice state (branches follow the values either way).
+template <int NC, class S>
+__device__ void solve4temp_multi(const VerisParams &p, const S4TIn &x, const S &Tin, const S *hI, const S *hS,
+                                 S *oT, S *oFio, S *oFia, S *oPen) {
     const double aa1 = 2663.5, bb1 = 0.622, Pa = 100000.0;
     const double one_m_bb1 = 1.0 - bb1;
     const double cc0 = p.s4t_cc0, cc1 = p.s4t_cc1, cc2 = p.s4t_cc2, d1 = p.s4t_d1, d1i = p.s4t_d1i;
@@ -100,7 +103,8 @@ __device__ void solve4temp_multi(const VerisParams &p, const S4TIn &x, const dou
     const double Ta = dmax(p.celsius2K + p.minTAir, x.ATemp);
     const double ug = dmax(p.wSpeedMin, x.wSpeed);
     const double d1ug = d1 * ug, d1iug = d1i * ug;
-    double T[NC], k[NC], d3[NC], lwabs[NC];
+    S T[NC], k[NC], lwabs[NC];
+    double d3[NC];
     bool ice[NC];
 #pragma unroll
     for (int l = 0; l < NC; ++l) {
@@ -111,41 +115,41 @@ __device__ void solve4temp_multi(const VerisParams &p, const S4TIn &x, const dou
         const double lw = emiss * lwc;
         double aI = ice[l] ? p.dryIceAlb : 0.0;
         double aS = ice[l] ? p.drySnowAlb : 0.0;
-        if (ice[l] && x.Tin >= SurfMeltTemp) { aI = p.wetIceAlb; aS = p.wetSnowAlb; }
+        if (ice[l] && Tin >= SurfMeltTemp) { aI = p.wetIceAlb; aS = p.wetSnowAlb; }
         const bool south = ice[l] && x.fCori < 0;
         if (south) { aI = p.dryIceAlb_south; aS = p.drySnowAlb_south; }
-        if (south && x.Tin >= SurfMeltTemp) { aI = p.wetIceAlb_south; aS = p.wetSnowAlb_south; }
-        double alb = ice[l] ? aI + hS[l] / p.hCut * (aS - aI) : 0.0;
-        if (hS[l] > p.hCut) alb = aS;
-        if (hS[l] == 0) alb = aI;
-        double pen = ice[l] ? p.shortwave * exp(-1.5 * hI[l]) : 0.0;
-        if (snow) pen = 0.0;
-        o[l].pen = ice[l] ? -(1 - alb) * pen * x.SWdown : 0.0;
-        const double absSW = ice[l] ? (1 - alb) * (1 - pen) * x.SWdown : 0.0;
-        k[l] = ice[l] ? p.iceConduct * p.snowConduct / (p.snowConduct * hI[l] + p.iceConduct * hS[l]) : 0.0;
+        if (south && Tin >= SurfMeltTemp) { aI = p.wetIceAlb_south; aS = p.wetSnowAlb_south; }
+        S alb = ice[l] ? aI + hS[l] / p.hCut * (aS - aI) : S(0.0);
+        if (hS[l] > p.hCut) alb = S(aS);
+        if (hS[l] == 0) alb = S(aI);
+        S pen = ice[l] ? p.shortwave * vexp(-1.5 * hI[l]) : S(0.0);
+        if (snow) pen = S(0.0);
+        oPen[l] = ice[l] ? -(1 - alb) * pen * x.SWdown : S(0.0);
+        const S absSW = ice[l] ? (1 - alb) * (1 - pen) * x.SWdown : S(0.0);
+        k[l] = ice[l] ? p.iceConduct * p.snowConduct / (p.snowConduct * hI[l] + p.iceConduct * hS[l]) : S(0.0);
         lwabs[l] = -lw - absSW;
-        T[l] = x.Tin;
+        T[l] = Tin;
     }
-    double Fc[NC], Fia[NC], Flh[NC];
+    S Fc[NC], Fia[NC];
     auto fluxes = [&](bool newton) {
 #pragma unroll
         for (int l = 0; l < NC; ++l) {
-            const double t1 = T[l];
-            const double rt = 1.0 / t1;
-            const double t2 = t1 * t1, t3 = t2 * t1, t4 = t2 * t2;
-            const double c3 = exp10(aa1 * rt);
-            const double svp = cc0 / c3;
-            const double qs = bb1 * svp / (Pa - one_m_bb1 * svp);
-            const double den = cc2 - c3 * Pa;
-            const double dqs = cc1 * c3 / (den * den * t2);
-            Fc[l] = ice[l] ? k[l] * (x.TempFrz - t1) : 0.0;
-            Flh[l] = ice[l] ? d1iug * (qs - x.aqh) : 0.0;
-            Fia[l] = ice[l] ? (lwabs[l] + t4 * d3[l] + d1ug * (t1 - Ta) + Flh[l]) : 0.0;
+            const S t1 = T[l];
+            const S rt = 1.0 / t1;
+            const S t2 = t1 * t1, t3 = t2 * t1, t4 = t2 * t2;
+            const S c3 = vexp10(aa1 * rt);
+            const S svp = cc0 / c3;
+            const S qs = bb1 * svp / (Pa - one_m_bb1 * svp);
+            const S den = cc2 - c3 * Pa;
+            const S dqs = cc1 * c3 / (den * den * t2);
+            Fc[l] = ice[l] ? k[l] * (x.TempFrz - t1) : S(0.0);
+            const S Flh = ice[l] ? d1iug * (qs - x.aqh) : S(0.0);
+            Fia[l] = ice[l] ? (lwabs[l] + t4 * d3[l] + d1ug * (t1 - Ta) + Flh) : S(0.0);
             if (newton) {
-                const double dF = ice[l] ? 4 * d3[l] * t3 + d1ug + d1iug * dqs : 0.0;
-                double Tn = ice[l] ? t1 + (Fc[l] - Fia[l]) / (k[l] + dF) : 0.0;
-                Tn = dmin(Tn, Tmelt);
-                T[l] = dmax(Tn, Tmin);
+                const S dF = ice[l] ? 4 * d3[l] * t3 + d1ug + d1iug * dqs : S(0.0);
+                S Tn = ice[l] ? t1 + (Fc[l] - Fia[l]) / (k[l] + dF) : S(0.0);
+                Tn = smin(Tn, S(Tmelt));
+                T[l] = smax(Tn, S(Tmin));
             }
         }
     };
@@ -154,38 +158,39 @@ __device__ void solve4temp_multi(const VerisParams &p, const S4TIn &x, const dou
 #pragma unroll
     for (int l = 0; l < NC; ++l) {
         const bool up = Fc[l] > 0;
-        o[l].T = ice[l] ? T[l] : x.Tin;
-        o[l].Fio = up ? Fc[l] : 0.0;
-        o[l].Fia = up ? 0.0 : Fia[l];
-        o[l].fw = ice[l] ? Flh[l] / p.lhSublim : 0.0;
+        oT[l] = ice[l] ? T[l] : Tin;
+        oFio[l] = up ? Fc[l] : S(0.0);
+        oFia[l] = up ? S(0.0) : Fia[l];
     }
 }
 
+template <class S>
 struct GrowthOut {
-    double h, hs, A, TSurf, EmPmR, forc_salt, Qsw, Qnet, load, pen, rh;
+    S h, hs, A, TSurf, EmPmR, forc_salt, Qsw, Qnet, load, pen, rh;
 };
 
-// veris/growth.py:8-397 for one point
-__device__ GrowthOut growth_point(const VerisParams &p, const Fields<double> &f, int64_t o) {
+// veris/growth.py:8-397 for one point, from the ice state (h, hs, A, TSurf)
+// and the forcing of point o
+template <class S>
+__device__ GrowthOut<S> growth_point(const VerisParams &p, const Fields<double> &f, int64_t o, S hIn, S hsIn,
+                                     S AIn, S TSurfIn) {
     const double qi = 1 / (p.rhoIce * p.lhFusion);
     const double qs = 1 / (p.rhoSnow * p.lhFusion);
-    const double hIn = __ldg(f.hIceMean + o), hsIn = __ldg(f.hSnowMean + o), AIn = __ldg(f.Area + o);
     const bool noIce = hIn == 0 || AIn == 0;
     const double keep = noIce ? 0.0 : 1.0;
-    const double h0 = hIn * keep, hs0 = hsIn * keep, A0 = AIn * keep;
+    const S h0 = hIn * keep, hs0 = hsIn * keep, A0 = AIn * keep;
     const bool isIce = h0 > 0;
-    const double regA = sqrt(A0 * A0 + p.Area_reg);
-    const double rregA = 1 / regA;
-    double hIa = isIce ? h0 * rregA : 0.0;
-    const double rhIa = A0 / sqrt(h0 * h0 + p.hIce_reg);
-    const double hSa = isIce ? hs0 * rregA : 0.0;
-    hIa = dmax(hIa, 0.05);
+    const S regA = vsqrt(A0 * A0 + p.Area_reg);
+    const S rregA = 1 / regA;
+    S hIa = isIce ? h0 * rregA : S(0.0);
+    const S rhIa = A0 / vsqrt(h0 * h0 + p.hIce_reg);
+    const S hSa = isIce ? hs0 * rregA : S(0.0);
+    hIa = smax(hIa, S(0.05));
 
     const double ocSalt = __ldg(f.ocSalt + o);
     const double TempFrz = p.tempFrz + p.dtempFrz_dS * ocSalt + p.celsius2K;
-    const double TSurfIn = __ldg(f.TSurf + o);
     S4TIn x;
-    x.Tin = TSurfIn;
+    x.Tin = val(TSurfIn);
     x.TempFrz = TempFrz;
     x.LWdown = __ldg(f.LWdown + o);
     x.ATemp = __ldg(f.ATemp + o);
@@ -193,111 +198,109 @@ __device__ GrowthOut growth_point(const VerisParams &p, const Fields<double> &f,
     x.fCori = __ldg(f.fCori + o);
     x.SWdown = __ldg(f.SWdown + o);
     x.aqh = __ldg(f.aqh + o);
-    double Tsum = 0, Fio_sum = 0, Fia_sum = 0, pen_sum = 0;
+    S Tsum = 0, Fio_sum = 0, Fia_sum = 0, pen_sum = 0;
     if (p.nITC == 5) {
-        double hIc[5], hSc[5];
-        S4TOut r[5];
+        S hIc[5], hSc[5], rT[5], rFio[5], rFia[5], rPen[5];
 #pragma unroll
         for (int l = 0; l < 5; ++l) {
             const double pFac = (double)(2 * (l + 1) - 1) * p.recip_nITC;
             hIc[l] = hIa * pFac;
             hSc[l] = hSa * pFac;
         }
-        solve4temp_multi<5>(p, x, hIc, hSc, r);
+        solve4temp_multi<5, S>(p, x, TSurfIn, hIc, hSc, rT, rFio, rFia, rPen);
 #pragma unroll
         for (int l = 0; l < 5; ++l) {
-            Tsum = Tsum + r[l].T;
-            Fio_sum = Fio_sum + r[l].Fio;
-            Fia_sum = Fia_sum + r[l].Fia;
-            pen_sum = pen_sum + r[l].pen;
+            Tsum = Tsum + rT[l];
+            Fio_sum = Fio_sum + rFio[l];
+            Fia_sum = Fia_sum + rFia[l];
+            pen_sum = pen_sum + rPen[l];
         }
     } else {
         for (int l = 0; l < p.nITC; ++l) {
             const double pFac = (double)(2 * (l + 1) - 1) * p.recip_nITC;
-            x.hI = hIa * pFac;
-            x.hS = hSa * pFac;
-            const S4TOut r = solve4temp_point(p, x);
-            Tsum = Tsum + r.T;
-            Fio_sum = Fio_sum + r.Fio;
-            Fia_sum = Fia_sum + r.Fia;
-            pen_sum = pen_sum + r.pen;
+            S hIc[1] = {hIa * pFac}, hSc[1] = {hSa * pFac}, rT[1], rFio[1], rFia[1], rPen[1];
+            solve4temp_multi<1, S>(p, x, TSurfIn, hIc, hSc, rT, rFio, rFia, rPen);
+            Tsum = Tsum + rT[0];
+            Fio_sum = Fio_sum + rFio[0];
+            Fia_sum = Fia_sum + rFia[0];
+            pen_sum = pen_sum + rPen[0];
         }
     }
-    GrowthOut g;
+    GrowthOut<S> g;
     g.TSurf = Tsum * p.recip_nITC;
-    const double Fio = Fio_sum * p.recip_nITC * A0;
-    double Fia = Fia_sum * p.recip_nITC * A0;
-    const double pen = pen_sum * p.recip_nITC * A0;
+    const S Fio = Fio_sum * p.recip_nITC * A0;
+    S Fia = Fia_sum * p.recip_nITC * A0;
+    const S pen = pen_sum * p.recip_nITC * A0;
 
     const double snowfall = __ldg(f.snowfall + o), precip = __ldg(f.precip + o);
     const bool cold = A0 > 0 && Tsum / (double)p.nITC < p.celsius2K;
     const double snowAcc = (cold ? snowfall + precip : snowfall) * p.rhoFresh2rhoSnow;
     const double rainToSea = cold ? 0.0 : precip;
-    const double snowAccOverIce = snowAcc * A0 * p.deltatTherm;
+    const S snowAccOverIce = snowAcc * A0 * p.deltatTherm;
 
-    double gUnder = Fio * qi;
-    if (A0 == 0) gUnder = 0.0;
-    const double potMeltRate = -Fia * qs;
-    const double potMelt = potMeltRate * p.deltatTherm;
+    S gUnder = Fio * qi;
+    if (A0 == 0) gUnder = S(0.0);
+    const S potMeltRate = -Fia * qs;
+    const S potMelt = potMeltRate * p.deltatTherm;
     const bool allMelt = potMelt >= hs0;
-    const double meltRate = allMelt ? hs0 * p.recip_deltatTherm : potMeltRate;
-    const double toSnow = allMelt ? -hs0 * p.recip_deltatTherm / qs : Fia;
+    const S meltRate = allMelt ? hs0 * p.recip_deltatTherm : potMeltRate;
+    const S toSnow = allMelt ? -hs0 * p.recip_deltatTherm / qs : Fia;
     Fia = Fia - toSnow;
-    const double gSurf = Fia * qi;
-    const double gNet = (gUnder + gSurf) * rregA;
+    const S gSurf = Fia * qi;
+    const S gNet = (gUnder + gSurf) * rregA;
 
     const double t0 = 0.4, t1 = 7 / t0;
     const double t2 = p.stantonNr * p.uStarBase * p.rhoSea * p.cpWater;
     const double sst = dmax(__ldg(f.theta + o), TempFrz);
-    const double mltf = 1 + (p.McPheeTaperFac - 1) / (1 + exp((A0 - t0) * t1));
-    const double gML = -t2 * (sst - TempFrz) * mltf * qi;
+    const S mltf = 1 + (p.McPheeTaperFac - 1) / (1 + vexp((A0 - t0) * t1));
+    const S gML = -t2 * (sst - TempFrz) * mltf * qi;
     const double Qnet_in = __ldg(f.Qnet + o);
     const double gOW = qi * Qnet_in;
 
-    const double dh = gNet * A0 + gOW * (1 - A0) + gML;
-    const double dhs = (snowAcc - meltRate) * A0;
-    const double half_rh = 0.5 * rhIa;
-    double dA_oa = half_rh * gOW * (1 - A0);
+    const S dh = gNet * A0 + gOW * (1 - A0) + gML;
+    const S dhs = (snowAcc - meltRate) * A0;
+    const S half_rh = 0.5 * rhIa;
+    S dA_oa = half_rh * gOW * (1 - A0);
     const bool grow = gOW > 0 && (A0 > 0 || dh > 0);
     if (grow) dA_oa = gOW * (1 - A0);
     const double fC = __ldg(f.fCori + o);
     dA_oa = (grow && fC < 0) ? dA_oa * p.recip_h0_south : dA_oa * p.recip_h0;
-    const double dA_oi = gML <= 0 ? half_rh * gML : 0.0;
-    const double dA_ia = (gNet <= 0 && h0 > 0) ? half_rh * gNet * A0 : 0.0;
-    const double dA = dA_oa + dA_oi + dA_ia;
+    const S dA_oi = gML <= 0 ? half_rh * gML : S(0.0);
+    const S dA_ia = (gNet <= 0 && h0 > 0) ? half_rh * gNet * A0 : S(0.0);
+    const S dA = dA_oa + dA_oi + dA_ia;
 
     const double mask = __ldg(f.iceMask + o);
-    double A = A0 + dA * mask * p.deltatTherm;
-    double h = h0 + dh * mask * p.deltatTherm;
-    double hs = hs0 + dhs * mask * p.deltatTherm;
-    A = dmin(dmax(A, 0.0), 1.0);
-    h = dmax(h, 0.0);
-    hs = dmax(hs, 0.0);
+    S A = A0 + dA * mask * p.deltatTherm;
+    S h = h0 + dh * mask * p.deltatTherm;
+    S hs = hs0 + dhs * mask * p.deltatTherm;
+    A = smin(smax(A, S(0.0)), S(1.0));
+    h = smax(h, S(0.0));
+    hs = smax(hs, S(0.0));
     const double alive = (h == 0 || A == 0) ? 0.0 : 1.0;
     A = A * alive;
     hs = hs * alive;
     h = h * alive;
-    const double hsub = (hs * p.rhoSnow + h * p.rhoIce) * p.recip_rhoSea;
-    const double flood = dmax(0.0, hsub - h);
+    const S hsub = (hs * p.rhoSnow + h * p.rhoIce) * p.recip_rhoSea;
+    const S flood = smax(S(0.0), hsub - h);
     h = h + flood;
     hs = hs - flood * p.rhoIce2rhoSnow;
-    g.rh = 1 / sqrt(h * h + p.hIce_reg);
+    g.rh = 1 / vsqrt(h * h + p.hIce_reg);
     g.h = h;
     g.hs = hs;
     g.A = A;
 
     g.Qsw = pen * A0 + __ldg(f.Qsw + o) * (1 - A0);
-    const double dH = h - h0;
-    const double melted = hs0 + snowAccOverIce - hs;
-    const double E_ice = dH / qi;
-    const double E_out = (A0 * (Fia + Fio + pen) + (1 - A0) * Qnet_in) * p.deltatTherm;
+    const S dH = h - h0;
+    const S melted = hs0 + snowAccOverIce - hs;
+    const S E_ice = dH / qi;
+    const S E_out = (A0 * (Fia + Fio + pen) + (1 - A0) * Qnet_in) * p.deltatTherm;
     g.Qnet = (E_out - E_ice) * p.recip_deltatTherm;
     const double sal_fac = (ocSalt > 0 && ocSalt > p.saltIce_ref) ? (1 - p.saltIce_ref / ocSalt) : 1.0;
-    const double fw_ice = -dH * p.rhoIce2rhoFresh * sal_fac;
+    const S fw_ice = -dH * p.rhoIce2rhoFresh * sal_fac;
     const double salt_ref = dmin(p.saltIce_ref, ocSalt);
     const double osh = __ldg(f.os_hIceMean + o), oshs = __ldg(f.os_hSnowMean + o);
-    const double saltflux = (dH + osh) * salt_ref * mask * p.rhoIce * p.recip_deltatTherm;
-    const double fw_snow = melted / p.rhoFresh2rhoSnow;
+    const S saltflux = (dH + osh) * salt_ref * mask * p.rhoIce * p.recip_deltatTherm;
+    const S fw_snow = melted / p.rhoFresh2rhoSnow;
     g.EmPmR = mask * ((-__ldg(f.evap + o) - precip) * (1 - A0) - rainToSea * A0 - __ldg(f.runoff + o) -
                       (fw_ice + fw_snow) / p.deltatTherm) * p.rhoFresh +
               mask * (osh * p.rhoIce + oshs * p.rhoSnow) * p.recip_deltatTherm;
@@ -340,7 +343,8 @@ __global__ void __launch_bounds__(128) growth_kernel(VerisParams p, Fields<doubl
     const int j = blockIdx.x * 32 + threadIdx.x, i = blockIdx.y * 4 + threadIdx.y;
     if (i >= d.NX || j >= d.NY) return;
     const int64_t o = d.raw(i, j);
-    const GrowthOut g = growth_point(p, f, o);
+    const GrowthOut<double> g = growth_point<double>(p, f, o, __ldg(f.hIceMean + o), __ldg(f.hSnowMean + o),
+                                                     __ldg(f.Area + o), __ldg(f.TSurf + o));
     out.h[o] = g.h;
     out.hs[o] = g.hs;
     out.A[o] = g.A;
@@ -352,6 +356,27 @@ __global__ void __launch_bounds__(128) growth_kernel(VerisParams p, Fields<doubl
     out.load[o] = g.load;
     out.pen[o] = g.pen;
     out.rh[o] = g.rh;
+}
+
+// adjoint of growth for the ice state: l_in = J^T l_out over (h, hs, A, TSurf)
+__global__ void __launch_bounds__(128) growth_adjoint_kernel(VerisParams p, Fields<double> f, Dims d,
+                                                             const double *lh, const double *lhs, const double *lA,
+                                                             const double *lT, double *oh, double *ohs, double *oA,
+                                                             double *oT) {
+    const int j = blockIdx.x * 32 + threadIdx.x, i = blockIdx.y * 4 + threadIdx.y;
+    if (i >= d.NX || j >= d.NY) return;
+    const int64_t o = d.raw(i, j);
+    using D = Dual<4>;
+    const GrowthOut<D> g = growth_point<D>(p, f, o, D::var(f.hIceMean[o], 0), D::var(f.hSnowMean[o], 1),
+                                           D::var(f.Area[o], 2), D::var(f.TSurf[o], 3));
+    const double l0 = lh[o], l1 = lhs[o], l2 = lA[o], l3 = lT[o];
+    double r[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) r[k] = l0 * g.h.d[k] + l1 * g.hs.d[k] + l2 * g.A.d[k] + l3 * g.TSurf.d[k];
+    oh[o] = r[0];
+    ohs[o] = r[1];
+    oA[o] = r[2];
+    oT[o] = r[3];
 }
 
 }  // namespace veris
@@ -369,6 +394,19 @@ int veris_solve4temp_f64(const VerisGrid *g, const VerisParams *p, const VerisFi
     dim3 gr((d.NY + 31) / 32, (d.NX + 7) / 8);
     solve4temp_kernel<<<gr, dim3(32, 8), 0, (cudaStream_t)s>>>(
         *p, *reinterpret_cast<const Fields<double> *>(vs), d, hI, hS, Tin, TF, To, Fio, Fia, pen, fw);
+    return launch_status();
+}
+
+int veris_growth_adjoint_f64(const VerisGrid *g, const VerisParams *p, const VerisFieldsF64 *vs, const double *lh,
+                             const double *lhs, const double *lA, const double *lT, double *oh, double *ohs,
+                             double *oA, double *oT, veris_stream_t s) {
+    Dims d;
+    VERIS_CHECK_GRID(g, d);
+    VERIS_REQUIRE(p && vs && lh && lhs && lA && lT && oh && ohs && oA && oT, VERIS_ERR_ARG);
+    VERIS_REQUIRE(p->nITC >= 1 && p->nITC <= 64, VERIS_ERR_ARG);
+    dim3 gr((d.NY + 31) / 32, (d.NX + 3) / 4);
+    growth_adjoint_kernel<<<gr, dim3(32, 4), 0, (cudaStream_t)s>>>(*p, *reinterpret_cast<const Fields<double> *>(vs),
+                                                                   d, lh, lhs, lA, lT, oh, ohs, oA, oT);
     return launch_status();
 }
 

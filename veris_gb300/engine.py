@@ -42,10 +42,11 @@ EVP_OUT = ("uIce", "vIce", "sigma1", "sigma2", "sigma12")
 GROWTH_OUT = ("hIceMean", "hSnowMean", "Area", "TSurf", "EmPmR", "forc_salt_surface_ice",
               "Qsw", "Qnet", "SeaIceLoad", "IcePenetSW", "recip_hIceMean")
 FILLED_AFTER_GROWTH = ("hIceMean", "hSnowMean", "Area", "forc_salt_surface_ice", "Qnet")
+HELD_FORCING = ("Qnet", "Qsw")
 
 
 class SeaIceStep:
-    def __init__(self, state: VerisState, precision="f64", n_subcycles=None, evp="auto"):
+    def __init__(self, state: VerisState, precision="f64", n_subcycles=None, evp="auto", hold_forcing=False):
         if precision not in ("f64", "f32"):
             raise ValueError("precision must be 'f64' or 'f32'")
         if evp not in ("auto", "fast", "plain"):
@@ -95,8 +96,19 @@ class SeaIceStep:
             self.f32_adv.vIce = self.evp_out32[1].data_ptr()
             for n in STATIC32:
                 self._to32(getattr(v, n), self.v32[n])
+        # Growth overwrites Qnet and Qsw with the ocean's budgets; a run
+        # with fixed surface forcing restores them before every step
+        self.forcing = ({n: getattr(v, n).clone() for n in HELD_FORCING} if hold_forcing else None)
         self.graph = None
         self.launches_per_step = None
+
+    def set_settings(self, **kw):
+        """Change scalar settings (e.g. pStar, airIceDrag) between steps;
+        drops a captured graph, whose launches hold the old values."""
+        for k, val in kw.items():
+            setattr(self.state.settings, k, val)
+        self.params = _abi.params_from_settings(self.state.settings)
+        self.graph = None
 
     def _fast_violations(self):
         """Settings and state properties the fast EVP form does not cover (0: none)."""
@@ -131,6 +143,9 @@ class SeaIceStep:
         mark = marks if marks is not None else (lambda name: None)
         n = 0
         mark("start")
+        if self.forcing is not None:
+            for name, t in self.forcing.items():
+                getattr(v, name).copy_(t)
         check("SeaIceMass", lib.veris_sea_ice_mass_f64(*r64, v.SeaIceMassC.data_ptr(), v.SeaIceMassU.data_ptr(),
                                                        v.SeaIceMassV.data_ptr(), st))
         check("AreaWS", lib.veris_area_ws_f64(*r64, v.AreaW.data_ptr(), v.AreaS.data_ptr(), st))

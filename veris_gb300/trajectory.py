@@ -1,0 +1,339 @@
+"""Gradients through many sea-ice steps on one GPU.
+
+``Trajectory`` runs n float64 steps of the sea-ice step (the engine's fast
+EVP form, surface forcing held fixed: Qnet and Qsw are restored before every
+step, since Growth overwrites them with the ocean's budgets) and propagates
+adjoints back through them with the hand-written adjoint kernels of every
+routine of the step:
+
+    prep -> EVP -> ocean stress -> advection -> clean-up + ridging -> Growth -> fills
+
+The state one step hands to the next is CARRIED (velocities, stresses, ice
+thickness, snow, concentration, surface temperature).  Step states are kept as
+snapshots under a binomial checkpointing schedule: with s snapshot slots the
+first split of every step range is the one that minimises the total number of
+recomputed steps (a dynamic programme over (steps, slots)); with s >= n - 1
+every step state is kept and nothing is recomputed.
+
+Inside a step the adjoint recomputes the cheap routines (preparation,
+advection, clean-up) from the step's start state; the new velocities come
+from the next step's state (they are stored back unchanged), and the EVP
+adjoint checkpoints its own subcycles.
+
+``sea_ice_trajectory`` wraps this as a ``torch.autograd.Function`` with
+gradients with respect to the initial hIceMean and Area and the coefficients
+pStar, airIceDrag, airIceDrag_south, waterIceDrag and waterIceDrag_south.
+"""
+import ctypes
+
+import torch
+
+from ._abi import VerisFields, check
+from .adjoint import EVP_STATE, EVP_FIELDS, ICE, PREP_OUT
+from .engine import SeaIceStep
+
+CARRIED = EVP_STATE + ICE
+COEFFS = ("pStar", "airIceDrag", "airIceDrag_south", "waterIceDrag", "waterIceDrag_south")
+
+
+def binomial_schedule(n, s):
+    """Optimal first splits for reversing n steps with s snapshot slots.
+
+    cost[k][t]: fewest step advances that reverse k steps starting from a held
+    state with t free slots; split[k][t]: the number of steps to advance
+    before storing the next snapshot.  cost[k][0] = k (k - 1) / 2 (recompute
+    from the held state for every step) and
+    cost[k][t] = min over m of m + cost[k - m][t - 1] + cost[m][t].
+    """
+    s = max(0, min(s, n - 1))
+    cost = [[0] * (s + 1) for _ in range(n + 1)]
+    split = [[1] * (s + 1) for _ in range(n + 1)]
+    for k in range(2, n + 1):
+        cost[k][0] = k * (k - 1) // 2
+        for t in range(1, s + 1):
+            if t >= k - 1:
+                cost[k][t], split[k][t] = k - 1, 1
+                continue
+            best, bm = None, 1
+            for m in range(1, k):
+                c = m + cost[k - m][t - 1] + cost[m][t]
+                if best is None or c < best:
+                    best, bm = c, m
+            cost[k][t], split[k][t] = best, bm
+    return cost, split
+
+
+def interior_mask(shape, olx=2, oly=2, device="cuda"):
+    m = torch.zeros(shape, dtype=torch.float64, device=device)
+    m[olx:shape[0] - olx, oly:shape[1] - oly] = 1.0
+    return m
+
+
+class Trajectory:
+    """n float64 steps from the state's current values and their adjoint."""
+
+    def __init__(self, state, n_steps, n_subcycles=None, snapshots=None, evp_checkpoint_every=0):
+        if state.settings.useRealFreshWaterFlux:
+            raise ValueError("the step adjoint covers useRealFreshWaterFlux = False only")
+        self.state = state
+        self.n = int(n_steps)
+        if self.n < 1:
+            raise ValueError("n_steps must be >= 1")
+        self.eng = SeaIceStep(state, "f64", n_subcycles, evp="fast", hold_forcing=True)
+        self.lib = self.eng.lib
+        self.snaps = self.n - 1 if snapshots is None else max(0, min(int(snapshots), self.n - 1))
+        self.K = int(evp_checkpoint_every)
+        self.cost, self.split = binomial_schedule(self.n, self.snaps)
+        sh, dev = self.eng.shape, self.eng.device
+        e = lambda: torch.empty(sh, dtype=torch.float64, device=dev)
+        v = state.variables
+        # recomputed intermediates of one step
+        self.uv_next = [e(), e()]
+        self.adv = [e() for _ in range(3)]                 # after advection
+        self.cln = [e() for _ in range(4)]                 # after clean-up + ridging
+        self.os = [e(), e()]
+        # adjoints: the carried state at the step's end and start, and scratch
+        self.lam = {k: e() for k in CARRIED}
+        self.lam_new = {k: e() for k in CARRIED}
+        self.lg = [e() for _ in range(3)]
+        self.lc = {k: e() for k in ICE}
+        self.la = [e() for _ in range(3)]
+        self.lf = {k: e() for k in EVP_FIELDS if k not in ("hIceMean", "Area")}
+        self.lscal = torch.zeros(len(COEFFS), dtype=torch.float64, device=dev)
+        self.evp_scal = torch.zeros(2, dtype=torch.float64, device=dev)
+        self.ocean_grad = {"uOcean": torch.zeros(sh, dtype=torch.float64, device=dev),
+                           "vOcean": torch.zeros(sh, dtype=torch.float64, device=dev)}
+        # field tables: the step's start state, the advection (new velocities),
+        # the clean-up (advected ice), the ridging and the Growth (cleaned ice)
+        base = self.eng.f64
+        self.t_adv = VerisFields.from_buffer_copy(base)
+        self.t_adv.uIce, self.t_adv.vIce = self.uv_next[0].data_ptr(), self.uv_next[1].data_ptr()
+        self.t_cln = VerisFields.from_buffer_copy(base)
+        self.t_cln.hIceMean, self.t_cln.hSnowMean, self.t_cln.Area = [t.data_ptr() for t in self.adv]
+        self.t_rdg = VerisFields.from_buffer_copy(base)
+        self.t_rdg.Area = self.cln[2].data_ptr()
+        self.t_gro = VerisFields.from_buffer_copy(base)
+        self.t_gro.hIceMean, self.t_gro.hSnowMean, self.t_gro.Area, self.t_gro.TSurf = \
+            [t.data_ptr() for t in self.cln]
+        self.t_gro.os_hIceMean, self.t_gro.os_hSnowMean = [t.data_ptr() for t in self.os]
+        self.t_lf = VerisFields(**{k: t.data_ptr() for k, t in self.lf.items()})
+        self.t_lprep = VerisFields(**{k: self.lf[k].data_ptr() for k in PREP_OUT})
+        g = ctypes.byref(self.eng.grid)
+        mk = lambda nbytes: torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device=dev)
+        self.ws_adv = mk(self.lib.veris_advection_adjoint_workspace_bytes(g))
+        self.ws_prep = mk(self.lib.veris_prep_adjoint_workspace_bytes(g))
+        self.ws_evp = mk(self.lib.veris_evp_adjoint_workspace_bytes(g, 8, self.eng.n_sub, self.K))
+        self.snap = {}
+        self.stats = {"forward_steps": 0, "recomputed_steps": 0, "adjoint_steps": 0}
+        self._x0 = None
+        self._graph_ok = False
+
+    # ------------------------------------------------------------ state
+    def _save(self):
+        v = self.state.variables
+        return [getattr(v, k).clone() for k in CARRIED]
+
+    def _load(self, snap):
+        v = self.state.variables
+        for k, t in zip(CARRIED, snap):
+            getattr(v, k).copy_(t)
+
+    def _advance(self, m):
+        for _ in range(m):
+            self.eng.step()
+
+    def set_coefficients(self, **kw):
+        """Set any of COEFFS (plain floats) for the next forward/backward."""
+        bad = set(kw) - set(COEFFS)
+        if bad:
+            raise KeyError(f"unknown coefficients {sorted(bad)}")
+        self.eng.set_settings(**{k: float(x) for k, x in kw.items()})
+        self._graph_ok = False
+
+    def _ensure_graph(self):
+        if not self._graph_ok:
+            x = self._save()
+            self.eng.capture()          # its eager warm-up step moves the state
+            self._load(x)
+            self._graph_ok = True
+
+    # ---------------------------------------------------------- forward
+    def forward(self):
+        """Run the n steps from the state's current carried values, storing
+        the snapshots of the schedule's first descent.  Leaves the final
+        state in the state's variables."""
+        self._ensure_graph()
+        self.snap = {0: self._save()}
+        keep, pos, left, t = set(), 0, self.n, self.snaps
+        while left > 1 and t > 0:
+            m = self.split[left][t]
+            pos += m
+            keep.add(pos)
+            left -= m
+            t -= 1
+        for k in range(1, self.n + 1):
+            self.eng.step()
+            if k in keep:
+                self.snap[k] = self._save()
+        v = self.state.variables
+        self.uv_final = (v.uIce.clone(), v.vIce.clone())
+        self.stats = {"forward_steps": self.n, "recomputed_steps": 0, "adjoint_steps": 0}
+
+    # ---------------------------------------------------------- backward
+    def backward(self, lam_final):
+        """Adjoints at the start from ``lam_final`` ({name in CARRIED: tensor},
+        missing names zero) at the end.  Returns ({name: adjoint of the
+        initial value}, {coefficient: d/d coefficient}, {uOcean, vOcean:
+        adjoint of the (constant) ocean velocities})."""
+        if 0 not in self.snap:
+            raise RuntimeError("backward() needs a forward() first")
+        self._ensure_graph()
+        for k in CARRIED:
+            src = lam_final.get(k)
+            if src is None:
+                self.lam[k].zero_()
+            else:
+                self.lam[k].copy_(src)
+        self.lscal.zero_()
+        for t in self.ocean_grad.values():
+            t.zero_()
+        self.uv_next[0].copy_(self.uv_final[0])
+        self.uv_next[1].copy_(self.uv_final[1])
+        stack = [("rev", 0, self.n, self.snaps)]
+        while stack:
+            task = stack.pop()
+            if task[0] == "free":
+                self.snap.pop(task[1], None)
+                continue
+            _, lo, hi, t = task
+            if hi - lo == 1:
+                self._load(self.snap[lo])
+                self._step_adjoint()
+                continue
+            if t == 0:
+                for k in range(hi - 1, lo - 1, -1):
+                    self._load(self.snap[lo])
+                    self._advance(k - lo)
+                    self.stats["recomputed_steps"] += k - lo
+                    self._step_adjoint()
+                continue
+            mid = lo + self.split[hi - lo][t]
+            if mid not in self.snap:
+                self._load(self.snap[lo])
+                self._advance(mid - lo)
+                self.stats["recomputed_steps"] += mid - lo
+                self.snap[mid] = self._save()
+            stack.append(("rev", lo, mid, t))
+            stack.append(("free", mid))
+            stack.append(("rev", mid, hi, t - 1))
+        self._load(self.snap[0])
+        grads = {k: self.lam[k].clone() for k in CARRIED}
+        coeffs = {k: self.lscal[i].clone() for i, k in enumerate(COEFFS)}
+        return grads, coeffs, {k: t.clone() for k, t in self.ocean_grad.items()}
+
+    def _refs(self, table):
+        return ctypes.byref(self.eng.grid), ctypes.byref(self.eng.params), ctypes.byref(table)
+
+    def _step_adjoint(self):
+        """self.lam (end of step k) -> self.lam (start of step k); the state's
+        variables hold step k's start state, uv_next the velocities at its end."""
+        lib, eng, v = self.lib, self.eng, self.state.variables
+        st = eng.stream
+        base = self._refs(eng.f64)
+        for name, t in eng.forcing.items():
+            getattr(v, name).copy_(t)
+        # recompute: preparation (into the state), advection, clean-up, ridging
+        check("SeaIceMass", lib.veris_sea_ice_mass_f64(*base, v.SeaIceMassC.data_ptr(), v.SeaIceMassU.data_ptr(),
+                                                       v.SeaIceMassV.data_ptr(), st))
+        check("AreaWS", lib.veris_area_ws_f64(*base, v.AreaW.data_ptr(), v.AreaS.data_ptr(), st))
+        check("WindForcingXY", lib.veris_wind_forcing_xy_f64(*base, v.WindForcingX.data_ptr(),
+                                                             v.WindForcingY.data_ptr(), st))
+        check("SeaIceStrength", lib.veris_sea_ice_strength_f64(*base, v.SeaIceStrength.data_ptr(), st))
+        check("Advection", lib.veris_advection_f64(*self._refs(self.t_adv), *[t.data_ptr() for t in self.adv],
+                                                   eng.ws_adv.data_ptr(), eng.ws_adv.numel(), st))
+        check("clean_up", lib.veris_clean_up_advection_f64(*self._refs(self.t_cln),
+                                                           *[t.data_ptr() for t in self.cln],
+                                                           *[t.data_ptr() for t in self.os], st))
+        check("ridging", lib.veris_ridging_f64(*self._refs(self.t_rdg), self.cln[2].data_ptr(), st))
+
+        lam, new = self.lam, self.lam_new
+        # final fills of hIceMean, hSnowMean, Area
+        for q, k in enumerate(ICE[:3]):
+            check("fill_adjoint", lib.veris_fill_overlap_adjoint_f64(
+                base[0], base[1], lam[k].data_ptr(), self.lg[q].data_ptr(), st))
+        # Growth, at the cleaned state
+        lc = [self.lc[k].data_ptr() for k in ICE]
+        check("growth_adjoint", lib.veris_growth_adjoint_f64(
+            *self._refs(self.t_gro), *[t.data_ptr() for t in self.lg], lam["TSurf"].data_ptr(), *lc, st))
+        # clean-up + ridging, at the advected state; TSurf's adjoint is final
+        check("cleanup_adjoint", lib.veris_cleanup_adjoint_f64(
+            *self._refs(self.t_cln), *lc, *[t.data_ptr() for t in self.la], new["TSurf"].data_ptr(), st))
+        # advection: into the start-state ice, and the new velocities' adjoints
+        for k in ICE[:3]:
+            new[k].zero_()
+        check("advection_adjoint", lib.veris_advection_adjoint_f64(
+            *self._refs(self.t_adv), *[t.data_ptr() for t in self.la], *[new[k].data_ptr() for k in ICE[:3]],
+            lam["uIce"].data_ptr(), lam["vIce"].data_ptr(), self.ws_adv.data_ptr(), self.ws_adv.numel(), st))
+        # EVP subcycles (adds hIceMean/Area through the basal drag into new)
+        for t in self.lf.values():
+            t.zero_()
+        self.t_lf.hIceMean, self.t_lf.Area = new["hIceMean"].data_ptr(), new["Area"].data_ptr()
+        check("evp_adjoint", lib.veris_evp_adjoint_f64(
+            *base, eng.n_sub, self.K, *[lam[k].data_ptr() for k in EVP_STATE],
+            *[new[k].data_ptr() for k in EVP_STATE], ctypes.byref(self.t_lf), self.evp_scal.data_ptr(),
+            self.ws_evp.data_ptr(), self.ws_evp.numel(), st))
+        self.lscal[3:5] += self.evp_scal
+        self.ocean_grad["uOcean"] += self.lf["uOcean"]
+        self.ocean_grad["vOcean"] += self.lf["vOcean"]
+        # preparation: masses, areas, wind forcing, strength
+        check("prep_adjoint", lib.veris_prep_adjoint_f64(
+            *base, ctypes.byref(self.t_lprep), *[new[k].data_ptr() for k in ("hIceMean", "hSnowMean", "Area",
+                                                                             "uIce", "vIce")],
+            self.lscal.data_ptr(), self.ws_prep.data_ptr(), self.ws_prep.numel(), st))
+        self.lam, self.lam_new = new, lam
+        # this step's start velocities are the previous step's new ones
+        self.uv_next[0].copy_(v.uIce)
+        self.uv_next[1].copy_(v.vIce)
+        self.stats["adjoint_steps"] += 1
+
+
+def tracking_loss_adjoint(state, target, names=("uIce", "vIce", "Area")):
+    """L = sum over the interior of (x - x*)^2 for x in ``names``; returns
+    (L as a 0-d tensor, {name: dL/dx})."""
+    v, s = state.variables, state.settings
+    m = interior_mask(tuple(v.iceMask.shape), int(s.olx), int(s.oly), v.iceMask.device)
+    L = torch.zeros((), dtype=torch.float64, device=v.iceMask.device)
+    lam = {}
+    for k in names:
+        r = (getattr(v, k) - target[k]) * m
+        L = L + (r * r).sum()
+        lam[k] = 2.0 * r
+    return L, lam
+
+
+class _TrajectoryFn(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, hIceMean0, Area0, coeffs, traj):
+        v = traj.state.variables
+        traj.set_coefficients(**{k: float(coeffs[i]) for i, k in enumerate(COEFFS)})
+        v.hIceMean.copy_(hIceMean0)
+        v.Area.copy_(Area0)
+        traj.forward()
+        ctx.traj = traj
+        ctx.coeffs_dtype = coeffs.dtype
+        return v.uIce.clone(), v.vIce.clone(), v.Area.clone()
+
+    @staticmethod
+    def backward(ctx, gu, gv, gA):
+        traj = ctx.traj
+        lam = {k: g for k, g in zip(("uIce", "vIce", "Area"), (gu, gv, gA)) if g is not None}
+        grads, coeffs, _ = traj.backward(lam)
+        gc = torch.stack([coeffs[k] for k in COEFFS]).to(ctx.coeffs_dtype)
+        return grads["hIceMean"], grads["Area"], gc, None
+
+
+def sea_ice_trajectory(traj, hIceMean0, Area0, coeffs):
+    """(uIce, vIce, Area) after ``traj.n`` steps from the state with hIceMean
+    and Area replaced by ``hIceMean0``, ``Area0``; ``coeffs``: 1-D float64
+    tensor of COEFFS.  Differentiable in all three (torch.autograd)."""
+    return _TrajectoryFn.apply(hIceMean0, Area0, coeffs, traj)
