@@ -386,6 +386,45 @@ int veris_prep_adjoint_f64(const VerisGrid *g, const VerisParams *p, const Veris
                            double *l_Area, double *l_uIce, double *l_vIce, double *scalars,
                            void *workspace, size_t workspace_bytes, veris_stream_t s);
 
+/* ---- batched ensemble (float32 fast form) ----------------------------- */
+/*
+ * n independent domains of uneven sizes (grids[0..n-1], one VerisParams for
+ * all) advanced together: per subcycle ONE launch of a persistent kernel
+ * whose CTAs pull tiles from a global work queue over all members' tiles
+ * (veris/evp_solver.py:21-254 per member, the fast form's arithmetic, so a
+ * member's values equal the single-domain shared-memory form's).  The caller
+ * provides one device workspace of veris_batch_workspace_bytes().
+ *   veris_batch_init            builds the member table (synchronous; call
+ *                               it outside any stream capture)
+ *   veris_batch_prep_member_f32 folds member m's float64 state (after the
+ *                               dynamics preparation) into buffer 0
+ *   veris_batch_evp_f32         n_subcycles for all members from buffer
+ *                               start_buf; the result is in
+ *                               start_buf ^ (n_subcycles & 1).  refold != 0
+ *                               first re-forms the momentum constant from
+ *                               the current velocities (a new step).  shape
+ *                               picks the tile (0: 32x32, 1: 16x32, 2: 32x16,
+ *                               3: 16x16), blocks_per_sm the persistent grid
+ *                               (0: 2 per SM).  A memset and kernel launches
+ *                               only: capturable in a CUDA graph.
+ *   veris_batch_copy_state_f32  member m's five state arrays (buffer buf) into
+ *                               caller arrays of the member's pitch
+ */
+size_t veris_batch_workspace_bytes(int32_t n, const VerisGrid *grids);
+int veris_batch_init(int32_t n, const VerisGrid *grids, const VerisParams *p, void *workspace,
+                     size_t workspace_bytes);
+int veris_batch_tiles(int32_t n, const VerisGrid *grids, int32_t shape);
+int veris_batch_prep_member_f32(int32_t n, const VerisGrid *grids, const VerisParams *p,
+                                void *workspace, size_t workspace_bytes, int32_t m,
+                                const VerisFieldsF64 *vs, veris_stream_t s);
+int veris_batch_evp_f32(int32_t n, const VerisGrid *grids, const VerisParams *p, void *workspace,
+                        size_t workspace_bytes, int32_t n_subcycles, int32_t start_buf,
+                        int32_t refold, int32_t shape, int32_t blocks_per_sm, veris_stream_t s);
+int veris_batch_copy_state_f32(int32_t n, const VerisGrid *grids, const VerisParams *p,
+                               const void *workspace, size_t workspace_bytes, int32_t m,
+                               int32_t buf, float *uIce, float *vIce, float *sigma1,
+                               float *sigma2, float *sigma12, veris_stream_t s);
+
 /* ---- reductions and conversions -------------------------------------- */
 /*
  * veris/global_sum.py:1-4 is an identity on one process; this is the

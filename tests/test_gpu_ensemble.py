@@ -1,0 +1,107 @@
+"""Batched ensemble: members of uneven sizes advanced by one persistent,
+work-queue kernel per subcycle equal the single-domain shared-memory form
+bit for bit, under every tile shape, eagerly and as a captured graph."""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+SIZES = ((64, 64), (96, 64), (64, 128), (160, 96), (128, 160))
+N_SUB = 7
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _lib():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from veris_gb300 import _abi
+    return _abi.load()
+
+
+def _members(seed=0):
+    from veris_gb300.state import VerisState
+    from veris_gb300.synthetic import config_settings, make_state
+    sett = config_settings("c4_ensemble")
+    out = []
+    for k, (nx, ny) in enumerate(SIZES):
+        arrays = make_state(nx, ny, seed=seed + k, wind_scale=0.5 + 0.25 * k, init_velocity=0.05)
+        out.append(VerisState.from_numpy(arrays, sett))
+    return out
+
+
+def _single(member, n):
+    from veris_gb300.evp_solver import evp_solver_fast
+    return evp_solver_fast(member, "f32", form="smem", n_subcycles=n)
+
+
+@pytest.mark.parametrize("shape", (0, 1, 2, 3))
+def test_batch_equals_single_domain(shape):
+    from veris_gb300.ensemble import EVP_STATE, Ensemble
+    members = _members()
+    ens = Ensemble(members, N_SUB, shape=shape, blocks_per_sm=2)
+    ens.step()
+    torch.cuda.synchronize()
+    for m, st in enumerate(members):
+        ref = _single(st, N_SUB)
+        got = ens.state(m)
+        for k, r in zip(EVP_STATE, ref):
+            assert torch.equal(got[k], r), (shape, m, k, float((got[k] - r).abs().max()))
+
+
+def test_graph_steps_equal_eager_steps():
+    from veris_gb300.ensemble import EVP_STATE, Ensemble
+    a = Ensemble(_members(1), N_SUB, shape=1)
+    b = Ensemble(_members(1), N_SUB, shape=1)
+    for _ in range(3):
+        a.step()
+    b.step()            # first step eagerly (no refold), then the captured one
+    b.capture()
+    b.step()
+    b.step()
+    torch.cuda.synchronize()
+    assert a.buf == b.buf
+    for m in range(len(SIZES)):
+        sa, sb = a.state(m), b.state(m)
+        for k in EVP_STATE:
+            assert torch.equal(sa[k], sb[k]), (m, k)
+
+
+def test_refold_matches_a_fresh_single_domain_step():
+    """After one ensemble step the refold re-forms the momentum constant from
+    the new velocities, as a new single-domain call's preparation does (up to
+    the float32 rounding of that fold)."""
+    from veris_gb300.ensemble import EVP_STATE, Ensemble
+    members = _members(2)
+    ens = Ensemble(members, N_SUB, shape=0)
+    ens.step()
+    # the single-domain path: write the first step's result back, solve again
+    for m, st in enumerate(members):
+        s1 = ens.state(m, dtype=torch.float64)
+        for k in EVP_STATE:
+            getattr(st.variables, k).copy_(s1[k])
+    ens.step()
+    for m, st in enumerate(members):
+        ref = _single(st, N_SUB)
+        got = ens.state(m)
+        for k, r in zip(EVP_STATE, ref):
+            scale = float(r.abs().max()) or 1.0
+            assert float((got[k] - r).abs().max()) <= 1e-5 * scale, (m, k)
+
+
+def test_autotune_picks_a_candidate_and_restores_the_state(tmp_path, monkeypatch):
+    from veris_gb300 import autotune
+    from veris_gb300.ensemble import EVP_STATE, Ensemble
+    monkeypatch.setenv("VERIS_TUNE_CACHE", str(tmp_path / "tune.json"))
+    ens = Ensemble(_members(3), N_SUB)
+    ens.step()
+    before = [ens.state(m) for m in range(len(SIZES))]
+    res = autotune.tune(ens, candidates=((0, 2), (1, 3), (3, 4)), subcycles=3, repeats=2)
+    assert (res["shape"], res["blocks_per_sm"]) in ((0, 2), (1, 3), (3, 4))
+    assert not res["cached"] and len(res["trials"]) == 3
+    for m in range(len(SIZES)):
+        after = ens.state(m)
+        for k in EVP_STATE:
+            assert torch.equal(before[m][k], after[k])
+    again = autotune.tune(ens, candidates=((0, 2), (1, 3), (3, 4)))
+    assert again["cached"] and again["shape"] == res["shape"]

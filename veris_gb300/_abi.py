@@ -149,6 +149,13 @@ SIGNATURES = {
     "veris_growth_adjoint_f64": ([_G, _Pa, _F] + [_P] * 8 + [_P], _I),
     "veris_prep_adjoint_workspace_bytes": ([_G], _S),
     "veris_prep_adjoint_f64": ([_G, _Pa, _F, _F] + [_P] * 6 + [_P, _S, _P], _I),
+    "veris_batch_workspace_bytes": ([ctypes.c_int32, _G], _S),
+    "veris_batch_init": ([ctypes.c_int32, _G, _Pa, _P, _S], _I),
+    "veris_batch_tiles": ([ctypes.c_int32, _G, ctypes.c_int32], _I),
+    "veris_batch_prep_member_f32": ([ctypes.c_int32, _G, _Pa, _P, _S, ctypes.c_int32, _F, _P], _I),
+    "veris_batch_evp_f32": ([ctypes.c_int32, _G, _Pa, _P, _S] + [ctypes.c_int32] * 5 + [_P], _I),
+    "veris_batch_copy_state_f32": ([ctypes.c_int32, _G, _Pa, _P, _S, ctypes.c_int32, ctypes.c_int32]
+                                   + [_P] * 5 + [_P], _I),
     "veris_ocean_stress_uv_f64": ([_G, _Pa, _F, _P, _P, _P], _I),
     "veris_limiter_f64": ([_P, _P, _L, _P], _I),
     "veris_calc_zonal_flux_f64": ([_G, _Pa, _F, _P, _P, _P, _P], _I),

@@ -1,0 +1,86 @@
+"""Launch-shape autotuner of the batched ensemble.
+
+For an ``Ensemble`` it times every candidate (tile shape x CTAs per SM) on a
+few subcycles with CUDA events, keeps the fastest and caches the choice per
+workload signature (member shapes, subcycles, GPU name) in a JSON file
+(``$VERIS_TUNE_CACHE``, default ``~/.cache/veris_gb300/tune.json``).  The
+ensemble's state is saved before the trials and restored after them, so
+tuning does not advance the members.
+"""
+import hashlib
+import json
+import os
+
+import torch
+
+from .ensemble import SHAPES
+
+DEFAULT_CANDIDATES = tuple((s, b) for s in SHAPES for b in (1, 2, 3, 4))
+
+
+def _cache_path():
+    return os.environ.get("VERIS_TUNE_CACHE",
+                          os.path.join(os.path.expanduser("~"), ".cache", "veris_gb300", "tune.json"))
+
+
+def signature(ens):
+    dev = torch.cuda.get_device_name(ens.device)
+    key = json.dumps({"shapes": ens.shapes, "n_sub": ens.n_sub, "device": dev})
+    return hashlib.sha1(key.encode()).hexdigest()
+
+
+def _load():
+    try:
+        with open(_cache_path()) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def _store(cache):
+    path = _cache_path()
+    try:
+        os.makedirs(os.path.dirname(path), exist_ok=True)
+        with open(path, "w") as f:
+            json.dump(cache, f, indent=1)
+    except OSError:
+        pass
+
+
+def tune(ens, candidates=DEFAULT_CANDIDATES, subcycles=10, repeats=3, use_cache=True):
+    """Pick (shape, blocks_per_sm) for ``ens``; sets it and returns
+    {"shape", "blocks_per_sm", "ms_per_subcycle", "trials": [...], "cached"}."""
+    sig = signature(ens)
+    cache = _load() if use_cache else {}
+    if sig in cache:
+        best = cache[sig]
+        ens.set_launch(best["shape"], best["blocks_per_sm"])
+        return dict(best, cached=True)
+    snap = ens.ws.clone()
+    buf0 = ens.buf
+    trials = []
+    for shape, bps in candidates:
+        ens.set_launch(shape, bps)
+        ens._enqueue(False, ens.buf, n_sub=2)    # configures the kernel, warms up
+        times = []
+        for _ in range(repeats):
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record()
+            ens._enqueue(False, ens.buf, n_sub=subcycles)
+            b.record()
+            b.synchronize()
+            times.append(a.elapsed_time(b) / subcycles)
+        trials.append({"shape": shape, "tile": SHAPES[shape], "blocks_per_sm": bps,
+                       "ms_per_subcycle": sorted(times)[len(times) // 2]})
+    ens.ws.copy_(snap)
+    ens.buf = buf0
+    del snap
+    best = min(trials, key=lambda t: t["ms_per_subcycle"])
+    ens.set_launch(best["shape"], best["blocks_per_sm"])
+    choice = {"shape": best["shape"], "blocks_per_sm": best["blocks_per_sm"],
+              "ms_per_subcycle": best["ms_per_subcycle"]}
+    if use_cache:
+        cache[sig] = choice
+        _store(cache)
+    return dict(choice, trials=trials, cached=False)
