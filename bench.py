@@ -62,6 +62,12 @@ def parse():
     ap.add_argument("--adjoint-config", default="c3_1deg")
     ap.add_argument("--adjoint-steps", type=int, default=None)
     ap.add_argument("--snapshots", type=int, default=None, help="step snapshots (default: all)")
+    ap.add_argument("--evp-checkpoint-every", type=int, default=0,
+                    help="EVP subcycle checkpoint interval inside a step's adjoint (0: keep all)")
+    ap.add_argument("--tape", default="auto", choices=("auto", "on", "off"),
+                    help="keep every EVP subcycle state during the forward")
+    ap.add_argument("--adjoint-repeats", type=int, default=2)
+    ap.add_argument("--no-fd", action="store_true", help="skip the centred-difference check of dL/dP*")
     ap.add_argument("--ensemble", action="store_true",
                     help="the batched ensemble (512 members of uneven sizes) against sequential launches")
     ap.add_argument("--members", type=int, default=512)
@@ -436,7 +442,10 @@ def run_adjoint(args):
         sett.nEVPsteps = args.subcycles
     st = VerisState.from_numpy(arrays, sett)
     v = st.variables
-    tr = Trajectory(st, n_steps, snapshots=args.snapshots)
+    tape = {"auto": "auto", "on": True, "off": False}[args.tape]
+    torch.cuda.reset_peak_memory_stats()
+    tr = Trajectory(st, n_steps, snapshots=args.snapshots, evp_checkpoint_every=args.evp_checkpoint_every,
+                    tape=tape)
     x0 = tr._save()
     p0 = float(sett.pStar)
 
@@ -458,7 +467,7 @@ def run_adjoint(args):
     # forward alone: graph replays
     tr._ensure_graph()
     fw = []
-    for _ in range(max(1, args.warmup) + 2):
+    for _ in range(1 + max(1, args.adjoint_repeats)):
         tr._load(x0)
         torch.cuda.synchronize()
         a, b = ev(), ev()
@@ -472,7 +481,7 @@ def run_adjoint(args):
 
     # forward with snapshots, then the adjoint
     res = []
-    for _ in range(2):
+    for _ in range(max(1, args.adjoint_repeats)):
         tr._load(x0)
         torch.cuda.synchronize()
         a, m, b = ev(), ev(), ev()
@@ -486,27 +495,31 @@ def run_adjoint(args):
         res.append((a.elapsed_time(m), m.elapsed_time(b), float(L), float(coeffs["pStar"]), dict(tr.stats)))
     t_f2, t_adj, L0, dLdP, stats = res[-1]
 
+    peak = torch.cuda.max_memory_allocated() / 1e9
     # centred difference in P*
-    hP = 1e-6 * p0
-    Ls = []
-    for pv in (p0 + hP, p0 - hP):
-        tr.set_coefficients(pStar=pv)
-        tr._load(x0)
-        tr.forward()
-        Ls.append(float(tracking_loss_adjoint(st, target)[0]))
-    tr.set_coefficients(pStar=p0)
-    fd = (Ls[0] - Ls[1]) / (2 * hP)
+    fd = None
+    if not args.no_fd:
+        hP = 1e-6 * p0
+        Ls = []
+        for pv in (p0 + hP, p0 - hP):
+            tr.set_coefficients(pStar=pv)
+            tr._load(x0)
+            tr.forward()
+            Ls.append(float(tracking_loss_adjoint(st, target)[0]))
+        tr.set_coefficients(pStar=p0)
+        fd = (Ls[0] - Ls[1]) / (2 * hP)
 
     line = {"metric": "trajectory (forward + adjoint) / forward time", "value": (t_f2 + t_adj) / t_fwd,
             "unit": "x", "higher_is_better": False, "dtype": "f64", "data": "synthetic",
             "config": {"workload": name, "nx": c["nx"], "ny": c["ny"], "steps": n_steps,
                        "subcycles": int(sett.nEVPsteps), "dt_s": c["dt"],
-                       "snapshots": tr.snaps, "evp_checkpoint_every": tr.K,
+                       "snapshots": tr.snaps, "evp_checkpoint_every": tr.K, "evp_tape": tr.tapes is not None,
                        "target": "P* x 1.2 and seed+1 winds", "loss": "interior sum (u-u*)^2+(v-v*)^2+(A-A*)^2"},
             "forward_ms": t_fwd, "forward_with_snapshots_ms": t_f2, "adjoint_ms": t_adj,
             "stats": stats, "loss": L0,
             "dL_dpStar": {"adjoint": dLdP, "centred_difference": fd,
-                          "rel_diff": abs(dLdP - fd) / max(abs(fd), 1e-300)},
+                          "rel_diff": None if fd is None else abs(dLdP - fd) / max(abs(fd), 1e-300)},
+            "peak_hbm_gb": peak, "cost_model_steps": tr.cost[tr.n][tr.snaps],
             "gpu_launches_per_forward_step": tr.eng.launches_per_step}
     print(json.dumps(line))
     return 0

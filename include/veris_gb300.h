@@ -275,6 +275,27 @@ int veris_evp_adjoint_f64(const VerisGrid *g, const VerisParams *p, const VerisF
                           double *l_sigma120, const VerisFieldsF64 *lfields, double *lscalars,
                           void *workspace, size_t workspace_bytes, veris_stream_t s);
 
+/*
+ * Taping forms for gradients of many steps (float64 fast form): the forward
+ * keeps every subcycle's state in a caller buffer of veris_evp_tape_bytes()
+ * (slot k = the five state arrays after k subcycles, internal pitch), and the
+ * adjoint reads the tape instead of recomputing the subcycles.  Same values
+ * as veris_evp_fast_solver_f64 and veris_evp_adjoint_f64.
+ */
+size_t veris_evp_tape_bytes(const VerisGrid *g, int32_t elem_size, int32_t n_subcycles);
+int veris_evp_fast_tape_f64(const VerisGrid *g, const VerisParams *p, const VerisFieldsF64 *vs,
+                            int32_t n_subcycles, double *uIce, double *vIce, double *sigma1,
+                            double *sigma2, double *sigma12, double *tape, size_t tape_bytes,
+                            void *workspace, size_t workspace_bytes, veris_stream_t s);
+size_t veris_evp_adjoint_taped_workspace_bytes(const VerisGrid *g, int32_t n_subcycles);
+int veris_evp_adjoint_taped_f64(const VerisGrid *g, const VerisParams *p, const VerisFieldsF64 *vs,
+                                int32_t n_subcycles, const double *tape, size_t tape_bytes,
+                                const double *l_uIce, const double *l_vIce, const double *l_sigma1,
+                                const double *l_sigma2, const double *l_sigma12, double *l_uIce0,
+                                double *l_vIce0, double *l_sigma10, double *l_sigma20,
+                                double *l_sigma120, const VerisFieldsF64 *lfields, double *lscalars,
+                                void *workspace, size_t workspace_bytes, veris_stream_t s);
+
 /* veris/ocean_stress.py:8-40 OceanStressUV */
 int veris_ocean_stress_uv_f64(const VerisGrid *g, const VerisParams *p,
                               const VerisFieldsF64 *vs, double *OceanStressU,

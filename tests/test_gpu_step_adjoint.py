@@ -282,7 +282,8 @@ def test_trajectory_gradients_match_finite_differences():
 
 
 def test_trajectory_checkpointing_is_exact():
-    """Fewer snapshots recompute steps but give the same gradients."""
+    """Fewer snapshots recompute steps, and the EVP tape skips the subcycle
+    recomputation, but all give the same gradients."""
     from veris_gb300.trajectory import CARRIED, Trajectory
     rng = np.random.default_rng(8)
     st = _trajectory_state()
@@ -290,14 +291,16 @@ def test_trajectory_checkpointing_is_exact():
     x0 = {k: getattr(v, k).clone() for k in CARRIED}
     lam = {k: _rand(rng, v.iceMask) for k in ("uIce", "vIce", "Area", "hIceMean")}
     out = []
-    for snaps in (None, 1, 0):
+    for snaps, tape in ((None, False), (1, False), (0, False), (None, True)):
         for k, t in x0.items():
             getattr(v, k).copy_(t)
-        tr = Trajectory(st, 5, n_subcycles=N_SUB, snapshots=snaps, evp_checkpoint_every=0 if snaps else 4)
+        tr = Trajectory(st, 5, n_subcycles=N_SUB, snapshots=snaps, evp_checkpoint_every=0 if snaps else 4,
+                        tape=tape)
+        assert (tr.tapes is not None) == tape
         tr.forward()
         g, c, _ = tr.backward(lam)
         out.append((g, c, dict(tr.stats)))
-    assert out[0][2]["recomputed_steps"] == 0
+    assert out[0][2]["recomputed_steps"] == 0 and out[3][2]["recomputed_steps"] == 0
     assert out[1][2]["recomputed_steps"] > 0 and out[2][2]["recomputed_steps"] > out[1][2]["recomputed_steps"]
     for g, c, _ in out[1:]:
         for k in CARRIED:

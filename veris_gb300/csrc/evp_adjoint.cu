@@ -583,7 +583,7 @@ struct Plan {
 };
 
 template <class T>
-static size_t plan(const Dims &d, int n, int K, char *base, Plan<T> *pl) {
+static size_t plan(const Dims &d, int n, int K, char *base, Plan<T> *pl, bool taped = false) {
     size_t off = fast_layout<T>(d, base, &pl->c, pl->st2, &pl->status);
     const int64_t lp = internal_pitch(d.NY);
     pl->field = rup256((size_t)d.NX * lp * sizeof(T));
@@ -594,9 +594,9 @@ static size_t plan(const Dims &d, int n, int K, char *base, Plan<T> *pl) {
     double *sc = reinterpret_cast<double *>(take(256));
     pl->a.dragN = sc;
     pl->a.dragS = sc ? sc + 1 : nullptr;
-    const int ncp = (n + K - 1) / K;
+    const int ncp = taped ? 0 : (n + K - 1) / K;
     pl->cp = reinterpret_cast<T *>(take((size_t)ncp * 5 * pl->field));
-    pl->seg = reinterpret_cast<T *>(take((size_t)(K + 1) * 5 * pl->field));
+    pl->seg = reinterpret_cast<T *>(take(taped ? 0 : (size_t)(K + 1) * 5 * pl->field));
     for (int b = 0; b < 2; ++b)
         for (int q = 0; q < 5; ++q) pl->lam[b][q] = reinterpret_cast<T *>(take(pl->field));
     pl->total = off;
@@ -615,19 +615,24 @@ static int copy_state(T *const dst[5], T *const src[5], size_t bytes, cudaStream
     return VERIS_OK;
 }
 
+// tape != nullptr: the forward's subcycle states (slot k = after k
+// subcycles, 5 arrays per slot, plan field bytes each) replace the
+// checkpoints and the recomputation
 template <class T>
 static int evp_adjoint(const VerisGrid *g, const VerisParams *p, const VerisFieldsF64 *vs, int n, int K,
                        const T *const lout[5], T *const lin[5], const VerisFieldsF64 *lf, double *lscal, void *ws,
-                       size_t wsb, veris_stream_t s) {
+                       size_t wsb, veris_stream_t s, const T *tape = nullptr, size_t tape_bytes = 0) {
     Dims d;
     VERIS_CHECK_GRID(g, d);
     VERIS_REQUIRE(p && vs && lf && lscal && n >= 1, VERIS_ERR_ARG);
     for (int q = 0; q < 5; ++q) VERIS_REQUIRE(lout[q] && lin[q], VERIS_ERR_ARG);
     if (fast_support(*p)) return VERIS_ERR_UNSUPPORTED;
-    if (K <= 0 || K > n) K = n;
+    if (K <= 0 || K > n || tape) K = n;
+    const bool taped = tape != nullptr;
     Plan<T> pl;
-    VERIS_REQUIRE(ws && wsb >= plan<T>(d, n, K, nullptr, &pl), VERIS_ERR_WORKSPACE);
-    plan<T>(d, n, K, static_cast<char *>(ws), &pl);
+    VERIS_REQUIRE(ws && wsb >= plan<T>(d, n, K, nullptr, &pl, taped), VERIS_ERR_WORKSPACE);
+    plan<T>(d, n, K, static_cast<char *>(ws), &pl, taped);
+    if (taped) VERIS_REQUIRE(tape_bytes >= (size_t)(n + 1) * 5 * pl.field, VERIS_ERR_WORKSPACE);
     cudaStream_t st = (cudaStream_t)s;
     const int64_t lp = internal_pitch(d.NY);
     const Fields<double> &f = *reinterpret_cast<const Fields<double> *>(vs);
@@ -644,10 +649,10 @@ static int evp_adjoint(const VerisGrid *g, const VerisParams *p, const VerisFiel
 
     // forward sweep: state 0 from the prep, checkpoints every K subcycles
     T *cp0[5];
-    for (int q = 0; q < 5; ++q) cp0[q] = slot(pl.cp, pl.field, 0, q);
-    if ((stt = fast_prep<T>(d, *p, f, pl.c, cp0, st)) != VERIS_OK) return stt;
-    const int ncp = (n + K - 1) / K;
-    {
+    for (int q = 0; q < 5; ++q) cp0[q] = taped ? pl.st2[0][q] : slot(pl.cp, pl.field, 0, q);
+    if ((stt = fast_prep<T>(d, *p, f, pl.c, cp0, st)) != VERIS_OK) return stt;   // constants (+ state 0)
+    const int ncp = taped ? 1 : (n + K - 1) / K;
+    if (!taped) {
         // states K, 2K, ... (ncp-1)K go to checkpoint slots; the ones between to scratch
         const int last = (ncp - 1) * K;
         const T *cur[5] = {cp0[0], cp0[1], cp0[2], cp0[3], cp0[4]};
@@ -663,12 +668,16 @@ static int evp_adjoint(const VerisGrid *g, const VerisParams *p, const VerisFiel
     int lb = 0;   // the adjoint buffer holding lambda_{s+1} (after the first subcycle)
     for (int m = ncp - 1; m >= 0; --m) {
         const int s0 = m * K, s1 = (s0 + K < n) ? s0 + K : n;
-        T *segs[5];
-        for (int q = 0; q < 5; ++q) segs[q] = slot(pl.seg, pl.field, 0, q);
-        T *cps[5];
-        for (int q = 0; q < 5; ++q) cps[q] = slot(pl.cp, pl.field, m, q);
-        if ((stt = copy_state<T>(segs, cps, pl.field, st)) != VERIS_OK) return stt;
-        for (int ss = s0; ss < s1; ++ss) {
+        // segment states: recomputed from the checkpoint, or the forward's tape
+        T *const segb = taped ? const_cast<T *>(tape) : pl.seg;
+        if (!taped) {
+            T *segs[5];
+            for (int q = 0; q < 5; ++q) segs[q] = slot(pl.seg, pl.field, 0, q);
+            T *cps[5];
+            for (int q = 0; q < 5; ++q) cps[q] = slot(pl.cp, pl.field, m, q);
+            if ((stt = copy_state<T>(segs, cps, pl.field, st)) != VERIS_OK) return stt;
+        }
+        for (int ss = s0; ss < s1 && !taped; ++ss) {
             const T *cur[5];
             T *dst[5];
             for (int q = 0; q < 5; ++q) {
@@ -681,18 +690,18 @@ static int evp_adjoint(const VerisGrid *g, const VerisParams *p, const VerisFiel
         for (int ss = s1 - 1; ss >= s0; --ss) {
             const bool first = ss == n - 1;
             T *out[5];
-            for (int q = 0; q < 5; ++q) {
-                out[q] = pl.lam[first ? 0 : lb ^ 1][q];
-                if (cudaMemsetAsync(out[q], 0, pl.field, st) != cudaSuccess) return VERIS_ERR_LAUNCH;
-            }
+            for (int q = 0; q < 5; ++q) out[q] = pl.lam[first ? 0 : lb ^ 1][q];
+            // the five adjoint arrays of a buffer are contiguous: one memset
+            if (cudaMemsetAsync(out[0], 0, 5 * pl.field, st) != cudaSuccess) return VERIS_ERR_LAUNCH;
+            const int rs = taped ? ss : ss - s0;   // slot of this subcycle's input state
             Io<T> io;
-            io.u = slot(pl.seg, pl.field, ss - s0, 0);
-            io.v = slot(pl.seg, pl.field, ss - s0, 1);
-            io.s1 = slot(pl.seg, pl.field, ss - s0, 2);
-            io.s2 = slot(pl.seg, pl.field, ss - s0, 3);
-            io.s12 = slot(pl.seg, pl.field, ss - s0, 4);
-            io.un = slot(pl.seg, pl.field, ss - s0 + 1, 0);
-            io.vn = slot(pl.seg, pl.field, ss - s0 + 1, 1);
+            io.u = slot(segb, pl.field, rs, 0);
+            io.v = slot(segb, pl.field, rs, 1);
+            io.s1 = slot(segb, pl.field, rs, 2);
+            io.s2 = slot(segb, pl.field, rs, 3);
+            io.s12 = slot(segb, pl.field, rs, 4);
+            io.un = slot(segb, pl.field, rs + 1, 0);
+            io.vn = slot(segb, pl.field, rs + 1, 1);
             io.ldn = lp;
             if (first) {
                 io.lu = lout[0]; io.lv = lout[1]; io.ls1 = lout[2]; io.ls2 = lout[3]; io.ls12 = lout[4];
@@ -755,6 +764,25 @@ size_t veris_evp_adjoint_workspace_bytes(const VerisGrid *g, int32_t elem_size, 
         return adj::plan<float>(d, n, K, nullptr, &pl);
     }
     return 0;
+}
+
+size_t veris_evp_adjoint_taped_workspace_bytes(const VerisGrid *g, int32_t n) {
+    Dims d;
+    if (check_grid(g, &d) != VERIS_OK || n < 1) return 0;
+    adj::Plan<double> pl;
+    return adj::plan<double>(d, n, n, nullptr, &pl, true);
+}
+
+int veris_evp_adjoint_taped_f64(const VerisGrid *g, const VerisParams *p, const VerisFieldsF64 *vs, int32_t n,
+                                const double *tape, size_t tape_bytes, const double *lu, const double *lv,
+                                const double *ls1, const double *ls2, const double *ls12, double *lu0,
+                                double *lv0, double *ls10, double *ls20, double *ls120,
+                                const VerisFieldsF64 *lfields, double *lscalars, void *ws, size_t wsb,
+                                veris_stream_t s) {
+    VERIS_REQUIRE(tape, VERIS_ERR_ARG);
+    const double *lout[5] = {lu, lv, ls1, ls2, ls12};
+    double *lin[5] = {lu0, lv0, ls10, ls20, ls120};
+    return adj::evp_adjoint<double>(g, p, vs, n, n, lout, lin, lfields, lscalars, ws, wsb, s, tape, tape_bytes);
 }
 
 int veris_evp_adjoint_f64(const VerisGrid *g, const VerisParams *p, const VerisFieldsF64 *vs, int32_t n,

@@ -188,8 +188,14 @@ template int fast_subcycle<double>(const Dims &, const HaloFill &, const FastCon
                                    const FastScalars<double> &, const FastIO<double> &, bool, bool, cudaStream_t);
 
 template <class T>
+static size_t tape_field(const Dims &d) { return rup256((size_t)d.NX * internal_pitch(d.NY) * sizeof(T)); }
+
+// tape != nullptr: every subcycle's state is kept, slot k (5 arrays of
+// tape_field bytes each, pitch lp) holding the state after k subcycles
+template <class T>
 static int evp_fast(const VerisGrid *g, const VerisParams *p, const VerisFieldsF64 *vs64, int n, T *uo, T *vo,
-                    T *s1o, T *s2o, T *s12o, void *ws, size_t wsb, int allow_tma, veris_stream_t s) {
+                    T *s1o, T *s2o, T *s12o, void *ws, size_t wsb, int allow_tma, veris_stream_t s,
+                    T *tape = nullptr, size_t tape_bytes = 0) {
     Dims d;
     VERIS_CHECK_GRID(g, d);
     VERIS_REQUIRE(p && vs64 && uo && vo && s1o && s2o && s12o, VERIS_ERR_ARG);
@@ -206,18 +212,33 @@ static int evp_fast(const VerisGrid *g, const VerisParams *p, const VerisFieldsF
     if (cudaMemsetAsync(status, 0, sizeof(int), st) != cudaSuccess) return VERIS_ERR_LAUNCH;
     const Fields<double> &f = *reinterpret_cast<const Fields<double> *>(vs64);
     const bool basal = p->basalDragK2 != 0.0, turn = p->sinWat != 0.0;
+    const size_t tf = tape_field<T>(d);
+    if (tape) VERIS_REQUIRE(tape_bytes >= (size_t)(n + 1) * 5 * tf, VERIS_ERR_WORKSPACE);
+    auto tslot = [&](int sl, int q) { return reinterpret_cast<T *>(reinterpret_cast<char *>(tape) + ((size_t)sl * 5 + q) * tf); };
+    T *s0[5];
+    for (int q = 0; q < 5; ++q) s0[q] = tape ? tslot(0, q) : state[0][q];
     dim3 g2((d.NY + 31) / 32, (d.NX + 7) / 8);
     if (basal)
-        fast_prep_kernel<T, true><<<g2, dim3(32, 8), 0, st>>>(*p, f, d, lp, c, state[0][0], state[0][1],
-                                                              state[0][2], state[0][3], state[0][4]);
+        fast_prep_kernel<T, true><<<g2, dim3(32, 8), 0, st>>>(*p, f, d, lp, c, s0[0], s0[1], s0[2], s0[3], s0[4]);
     else
-        fast_prep_kernel<T, false><<<g2, dim3(32, 8), 0, st>>>(*p, f, d, lp, c, state[0][0], state[0][1],
-                                                               state[0][2], state[0][3], state[0][4]);
+        fast_prep_kernel<T, false><<<g2, dim3(32, 8), 0, st>>>(*p, f, d, lp, c, s0[0], s0[1], s0[2], s0[3], s0[4]);
     int stt = launch_status();
     if (stt != VERIS_OK) return stt;
     const FastScalars<T> k = fast_scalars<T>(*p);
     const HaloFill h = halo_fill_of(*p);
     T *outs[5] = {uo, vo, s1o, s2o, s12o};
+    if (tape) {
+        for (int it = 0; it < n; ++it) {
+            FastIO<T> io{tslot(it, 0), tslot(it, 1), tslot(it, 2), tslot(it, 3), tslot(it, 4),
+                         tslot(it + 1, 0), tslot(it + 1, 1), tslot(it + 1, 2), tslot(it + 1, 3), tslot(it + 1, 4), lp};
+            if ((stt = fast_subcycle<T>(d, h, c, k, io, basal, turn, st)) != VERIS_OK) return stt;
+        }
+        for (int q = 0; q < 5; ++q)
+            if (cudaMemcpy2DAsync(outs[q], d.ld * sizeof(T), tslot(n, q), lp * sizeof(T), d.NY * sizeof(T), d.NX,
+                                  cudaMemcpyDeviceToDevice, st) != cudaSuccess)
+                return VERIS_ERR_LAUNCH;
+        return VERIS_OK;
+    }
     if constexpr (sizeof(T) == 4) {
         if (allow_tma) {
             stt = evp_tma_subcycles(d, h, c, k, state, outs, d.ld, n, status, basal, turn, st);
@@ -293,6 +314,21 @@ int veris_evp_fast_solver_f64(const VerisGrid *g, const VerisParams *p, const Ve
                               double *u, double *v, double *s1, double *s2, double *s12, void *ws, size_t wsb,
                               veris_stream_t s) {
     return evp_fast<double>(g, p, vs, n, u, v, s1, s2, s12, ws, wsb, 0, s);
+}
+
+size_t veris_evp_tape_bytes(const VerisGrid *g, int32_t elem_size, int32_t n) {
+    Dims d;
+    if (check_grid(g, &d) != VERIS_OK || n < 1) return 0;
+    if (elem_size == 8) return (size_t)(n + 1) * 5 * tape_field<double>(d);
+    if (elem_size == 4) return (size_t)(n + 1) * 5 * tape_field<float>(d);
+    return 0;
+}
+
+int veris_evp_fast_tape_f64(const VerisGrid *g, const VerisParams *p, const VerisFieldsF64 *vs, int32_t n,
+                            double *u, double *v, double *s1, double *s2, double *s12, double *tape,
+                            size_t tape_bytes, void *ws, size_t wsb, veris_stream_t s) {
+    VERIS_REQUIRE(tape, VERIS_ERR_ARG);
+    return evp_fast<double>(g, p, vs, n, u, v, s1, s2, s12, ws, wsb, 0, s, tape, tape_bytes);
 }
 
 int veris_evp_fast_status(const void *ws, int32_t *status_host, veris_stream_t s) {

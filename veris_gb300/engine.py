@@ -101,6 +101,9 @@ class SeaIceStep:
         self.forcing = ({n: getattr(v, n).clone() for n in HELD_FORCING} if hold_forcing else None)
         self.graph = None
         self.launches_per_step = None
+        # float64 fast form only: a buffer of veris_evp_tape_bytes() that the
+        # next eager step's EVP fills with its subcycle states
+        self.evp_tape = None
 
     def set_settings(self, **kw):
         """Change scalar settings (e.g. pStar, airIceDrag) between steps;
@@ -157,7 +160,18 @@ class SeaIceStep:
         if evp_events:
             evp_events[0].record()
         ws = (self.ws_evp.data_ptr(), self.ws_evp.numel(), st)
-        if self.precision == "f64":
+        if self.precision == "f64" and self.evp_tape is not None:
+            # keep every subcycle's state (gradients of many steps); eager only
+            tape = self.evp_tape
+            check("evp_tape", lib.veris_evp_fast_tape_f64(*r64, self.n_sub, *[t.data_ptr() for t in self.evp_out],
+                                                           tape.data_ptr(), tape.numel() * tape.element_size(),
+                                                           *ws))
+            n += self.n_sub + 1
+            if evp_events:
+                evp_events[1].record()
+            for name, t in zip(EVP_OUT, self.evp_out):
+                getattr(v, name).copy_(t)
+        elif self.precision == "f64":
             fn = lib.veris_evp_fast_solver_f64 if self.evp_form == "fast" else lib.veris_evp_solver_f64
             check("evp_solver", fn(*r64, self.n_sub, *[t.data_ptr() for t in self.evp_out], *ws))
             n += self.n_sub + (1 if self.evp_form == "fast" else 0)

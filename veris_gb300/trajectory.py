@@ -72,7 +72,13 @@ def interior_mask(shape, olx=2, oly=2, device="cuda"):
 class Trajectory:
     """n float64 steps from the state's current values and their adjoint."""
 
-    def __init__(self, state, n_steps, n_subcycles=None, snapshots=None, evp_checkpoint_every=0):
+    def __init__(self, state, n_steps, n_subcycles=None, snapshots=None, evp_checkpoint_every=0, tape="auto",
+                 tape_memory_fraction=0.6):
+        """``snapshots``: step snapshot slots (None: every step).  ``tape``:
+        keep every EVP subcycle state of every step during the forward, so
+        the adjoint recomputes no subcycle ("auto": when every step is
+        snapshotted and the tapes fit in ``tape_memory_fraction`` of the free
+        device memory)."""
         if state.settings.useRealFreshWaterFlux:
             raise ValueError("the step adjoint covers useRealFreshWaterFlux = False only")
         self.state = state
@@ -86,7 +92,6 @@ class Trajectory:
         self.cost, self.split = binomial_schedule(self.n, self.snaps)
         sh, dev = self.eng.shape, self.eng.device
         e = lambda: torch.empty(sh, dtype=torch.float64, device=dev)
-        v = state.variables
         # recomputed intermediates of one step
         self.uv_next = [e(), e()]
         self.adv = [e() for _ in range(3)]                 # after advection
@@ -122,10 +127,18 @@ class Trajectory:
         mk = lambda nbytes: torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device=dev)
         self.ws_adv = mk(self.lib.veris_advection_adjoint_workspace_bytes(g))
         self.ws_prep = mk(self.lib.veris_prep_adjoint_workspace_bytes(g))
-        self.ws_evp = mk(self.lib.veris_evp_adjoint_workspace_bytes(g, 8, self.eng.n_sub, self.K))
+        tape_bytes = int(self.lib.veris_evp_tape_bytes(g, 8, self.eng.n_sub))
+        if tape == "auto":
+            free = torch.cuda.mem_get_info(dev)[0]
+            tape = self.snaps == self.n - 1 and self.n * tape_bytes <= tape_memory_fraction * free
+        elif tape and self.snaps != self.n - 1:
+            raise ValueError("taping needs every step snapshotted (snapshots=None)")
+        self.tapes = ([torch.empty(tape_bytes // 8, dtype=torch.float64, device=dev) for _ in range(self.n)]
+                      if tape else None)
+        self.ws_evp = mk(self.lib.veris_evp_adjoint_taped_workspace_bytes(g, self.eng.n_sub) if tape else
+                         self.lib.veris_evp_adjoint_workspace_bytes(g, 8, self.eng.n_sub, self.K))
         self.snap = {}
         self.stats = {"forward_steps": 0, "recomputed_steps": 0, "adjoint_steps": 0}
-        self._x0 = None
         self._graph_ok = False
 
     # ------------------------------------------------------------ state
@@ -172,7 +185,12 @@ class Trajectory:
             left -= m
             t -= 1
         for k in range(1, self.n + 1):
-            self.eng.step()
+            if self.tapes is not None:
+                self.eng.evp_tape = self.tapes[k - 1]
+                self.eng.launches_per_step = self.eng._enqueue()
+                self.eng.evp_tape = None
+            else:
+                self.eng.step()
             if k in keep:
                 self.snap[k] = self._save()
         v = self.state.variables
@@ -208,14 +226,14 @@ class Trajectory:
             _, lo, hi, t = task
             if hi - lo == 1:
                 self._load(self.snap[lo])
-                self._step_adjoint()
+                self._step_adjoint(lo)
                 continue
             if t == 0:
                 for k in range(hi - 1, lo - 1, -1):
                     self._load(self.snap[lo])
                     self._advance(k - lo)
                     self.stats["recomputed_steps"] += k - lo
-                    self._step_adjoint()
+                    self._step_adjoint(k)
                 continue
             mid = lo + self.split[hi - lo][t]
             if mid not in self.snap:
@@ -234,7 +252,7 @@ class Trajectory:
     def _refs(self, table):
         return ctypes.byref(self.eng.grid), ctypes.byref(self.eng.params), ctypes.byref(table)
 
-    def _step_adjoint(self):
+    def _step_adjoint(self, step):
         """self.lam (end of step k) -> self.lam (start of step k); the state's
         variables hold step k's start state, uv_next the velocities at its end."""
         lib, eng, v = self.lib, self.eng, self.state.variables
@@ -278,10 +296,17 @@ class Trajectory:
         for t in self.lf.values():
             t.zero_()
         self.t_lf.hIceMean, self.t_lf.Area = new["hIceMean"].data_ptr(), new["Area"].data_ptr()
-        check("evp_adjoint", lib.veris_evp_adjoint_f64(
-            *base, eng.n_sub, self.K, *[lam[k].data_ptr() for k in EVP_STATE],
-            *[new[k].data_ptr() for k in EVP_STATE], ctypes.byref(self.t_lf), self.evp_scal.data_ptr(),
-            self.ws_evp.data_ptr(), self.ws_evp.numel(), st))
+        lo_ptrs = [lam[q].data_ptr() for q in EVP_STATE]
+        li_ptrs = [new[q].data_ptr() for q in EVP_STATE]
+        if self.tapes is not None:
+            tape = self.tapes[step]
+            check("evp_adjoint_taped", lib.veris_evp_adjoint_taped_f64(
+                *base, eng.n_sub, tape.data_ptr(), tape.numel() * 8, *lo_ptrs, *li_ptrs, ctypes.byref(self.t_lf),
+                self.evp_scal.data_ptr(), self.ws_evp.data_ptr(), self.ws_evp.numel(), st))
+        else:
+            check("evp_adjoint", lib.veris_evp_adjoint_f64(
+                *base, eng.n_sub, self.K, *lo_ptrs, *li_ptrs, ctypes.byref(self.t_lf), self.evp_scal.data_ptr(),
+                self.ws_evp.data_ptr(), self.ws_evp.numel(), st))
         self.lscal[3:5] += self.evp_scal
         self.ocean_grad["uOcean"] += self.lf["uOcean"]
         self.ocean_grad["vOcean"] += self.lf["vOcean"]
