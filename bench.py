@@ -57,6 +57,10 @@ def parse():
     ap.add_argument("--subcycles", type=int, default=None, help="override the workload's subcycles")
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--evp", default="auto", choices=("auto", "fast", "plain"))
+    ap.add_argument("--f32-kernel", default="walk", choices=("tma", "walk"),
+                    help="float32 EVP kernel: register-walking warps or TMA-staged tiles")
+    ap.add_argument("--walk-rows", type=int, default=0, help="rows per walk (0: from the grid and the SM count)")
+    ap.add_argument("--walk-variant", type=int, default=0)
     ap.add_argument("--adjoint", action="store_true",
                     help="time a trajectory's forward + adjoint against its forward (float64)")
     ap.add_argument("--adjoint-config", default="c3_1deg")
@@ -68,6 +72,9 @@ def parse():
                     help="keep every EVP subcycle state during the forward")
     ap.add_argument("--adjoint-repeats", type=int, default=2)
     ap.add_argument("--no-fd", action="store_true", help="skip the centred-difference check of dL/dP*")
+    ap.add_argument("--evp-alpha-beta", type=float, default=None,
+                    help="override the mEVP relaxation parameters (evpAlpha = evpBeta)")
+    ap.add_argument("--track-norms", action="store_true", help="record the adjoint norm after every step")
     ap.add_argument("--ensemble", action="store_true",
                     help="the batched ensemble (512 members of uneven sizes) against sequential launches")
     ap.add_argument("--members", type=int, default=512)
@@ -286,11 +293,14 @@ def run_ours(args):
     sett = config_settings(args.config)
     if args.subcycles:
         sett.nEVPsteps = args.subcycles
+    if args.evp_alpha_beta:
+        sett.evpAlpha = sett.evpBeta = float(args.evp_alpha_beta)
     n_sub = sett.nEVPsteps
     cells = c["nx"] * c["ny"]
 
     state = VerisState.from_numpy(arrays, sett, device=dev)
-    eng = SeaIceStep(state, precision=args.precision, evp=args.evp)
+    eng = SeaIceStep(state, precision=args.precision, evp=args.evp, f32_kernel=args.f32_kernel,
+                     walk_rows=args.walk_rows, walk_variant=args.walk_variant)
     eng.capture()
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
     for _ in range(args.warmup):
@@ -334,7 +344,8 @@ def run_ours(args):
     traffic = recorded_traffic(args.precision)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": traffic,
-                "kernel": ("evp_tma_kernel" if eng.evp_form == "fast" and args.precision == "f32" else
+                "kernel": (("evp_walk_kernel" if args.f32_kernel == "walk" else "evp_tma_kernel")
+                           if eng.evp_form == "fast" and args.precision == "f32" else
                            ("evp_fast_kernel" if eng.evp_form == "fast" else "evp_subcycle_kernel")
                            + f"<{'float' if args.precision == 'f32' else 'double'}>"),
                 "algorithmic_bytes_per_launch": algo_bytes, "avg_launch_us": per_launch_s * 1e6,
@@ -345,10 +356,14 @@ def run_ours(args):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": args.precision, "data": "synthetic",
             "config": {"workload": args.config, "nx": c["nx"], "ny": c["ny"], "subcycles": n_sub,
+                       "evpAlpha": float(sett.evpAlpha), "evpBeta": float(sett.evpBeta),
                        "dt_s": c["dt"], "cells": cells, "precision": args.precision,
                        "parallelism": "replicas" if ws > 1 else "single-gpu",
                        "l2": "flushed before every timed step (512 MiB write)",
-                       "graph": "one CUDA graph per step", "evp_form": eng.evp_form},
+                       "graph": "one CUDA graph per step", "evp_form": eng.evp_form,
+                       "f32_kernel": args.f32_kernel if args.precision == "f32" else None,
+                       "walk": {"rows": eng.walk_rows, "variant": eng.walk_variant}
+                       if args.f32_kernel == "walk" else None},
             "roofline": roofline, "gpu_launches": launches, "clocks": clk,
             "wall_s_timed_region": wall, "evp_ms_per_step": evp_ms,
             "phase_ms": {k: round(v, 4) for k, v in phases.items()}}
@@ -377,7 +392,8 @@ def run_ours(args):
         names = ("uIce", "vIce", "hIceMean", "hSnowMean", "Area", "TSurf", "Qnet")
         # both precisions from the same initial state; capture() runs step 1
         st32 = VerisState.from_numpy(arrays, sett, device=dev)
-        e32 = SeaIceStep(st32, precision="f32", evp=args.evp)
+        e32 = SeaIceStep(st32, precision="f32", evp=args.evp, f32_kernel=args.f32_kernel,
+                         walk_rows=args.walk_rows, walk_variant=args.walk_variant)
         e32.capture()
         st64 = VerisState.from_numpy(arrays, sett, device=dev)
         e64 = SeaIceStep(st64, precision="f64", evp=args.evp)
@@ -440,12 +456,15 @@ def run_adjoint(args):
     sett = config_settings(name)
     if args.subcycles:
         sett.nEVPsteps = args.subcycles
+    if args.evp_alpha_beta:
+        sett.evpAlpha = sett.evpBeta = float(args.evp_alpha_beta)
     st = VerisState.from_numpy(arrays, sett)
     v = st.variables
     tape = {"auto": "auto", "on": True, "off": False}[args.tape]
     torch.cuda.reset_peak_memory_stats()
     tr = Trajectory(st, n_steps, snapshots=args.snapshots, evp_checkpoint_every=args.evp_checkpoint_every,
                     tape=tape)
+    tr.track_norms = args.track_norms
     x0 = tr._save()
     p0 = float(sett.pStar)
 
@@ -514,6 +533,7 @@ def run_adjoint(args):
             "config": {"workload": name, "nx": c["nx"], "ny": c["ny"], "steps": n_steps,
                        "subcycles": int(sett.nEVPsteps), "dt_s": c["dt"],
                        "snapshots": tr.snaps, "evp_checkpoint_every": tr.K, "evp_tape": tr.tapes is not None,
+                       "evpAlpha": float(sett.evpAlpha), "evpBeta": float(sett.evpBeta),
                        "target": "P* x 1.2 and seed+1 winds", "loss": "interior sum (u-u*)^2+(v-v*)^2+(A-A*)^2"},
             "forward_ms": t_fwd, "forward_with_snapshots_ms": t_f2, "adjoint_ms": t_adj,
             "stats": stats, "loss": L0,

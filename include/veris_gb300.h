@@ -222,6 +222,17 @@ int veris_evp_fast_solver_f64(const VerisGrid *g, const VerisParams *p, const Ve
                               double *sigma2, double *sigma12, void *workspace,
                               size_t workspace_bytes, veris_stream_t s);
 /* the float32 fast form without TMA staging (the shared-memory kernel only) */
+/*
+ * The same float32 loop with the register-walking kernel: one warp per
+ * 28-column strip walks `rows` output rows (4..4096), rows in registers and
+ * columns across lanes; no shared memory, no barriers.  `variant` (0..3)
+ * picks the compiled form, loop unroll x register budget: 0 = 1 x free,
+ * 1 = 4 x free, 2 = 1 x 4 CTAs/SM, 3 = 4 x 4 CTAs/SM; same values.
+ */
+int veris_evp_walk_solver_f32(const VerisGrid *g, const VerisParams *p, const VerisFieldsF64 *vs,
+                              int32_t n_subcycles, int32_t rows, int32_t variant, float *uIce,
+                              float *vIce, float *sigma1, float *sigma2, float *sigma12,
+                              void *workspace, size_t workspace_bytes, veris_stream_t s);
 int veris_evp_smem_solver_f32(const VerisGrid *g, const VerisParams *p, const VerisFieldsF64 *vs,
                               int32_t n_subcycles, float *uIce, float *vIce, float *sigma1,
                               float *sigma2, float *sigma12, void *workspace,

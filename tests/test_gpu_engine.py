@@ -143,3 +143,48 @@ def test_tma_form_matches_smem_form_and_f64(case):
         if name in ("uIce", "vIce"):
             e = G.rel_err(a, ref[name])
             assert e <= 1e-3, f"{case}.{name}: float32 vs reference {e:.2e}"
+
+
+@pytest.mark.parametrize("case", ("c1", "moving", "noice"))
+@pytest.mark.parametrize("rows,variant", ((4, 0), (7, 1), (16, 2), (64, 3), (16, 1)))
+def test_walk_form_matches_tma_and_smem_forms(case, rows, variant):
+    """The register-walking float32 kernel (any walk length, with ragged last
+    walks) against the TMA-staged and the shared-memory float32 kernels from
+    the reference's input state of the first EVP call."""
+    from veris_gb300.evp_solver import evp_solver_fast
+    from veris_gb300.state import VerisState
+    g = G.load(case)
+    first_evp = [i for i, r, _o in G.sequence(g) if r == "IceVelocities"][0]
+    st0 = G.state_before(g, first_evp)
+    st = VerisState.from_numpy(vars(st0.variables), st0.settings)
+    try:
+        smem = evp_solver_fast(st, "f32", "smem")
+    except Exception as e:   # settings the fast forms do not cover
+        pytest.skip(str(e))
+    walk = evp_solver_fast(st, "f32", "walk", rows=rows, variant=variant)
+    tma = evp_solver_fast(st, "f32", "tma")
+    for k, name in enumerate(("uIce", "vIce", "sigma1", "sigma2", "sigma12")):
+        a = walk[k].double().cpu().numpy()
+        assert G.rel_err(a, smem[k].double().cpu().numpy()) <= 1e-5, f"{case}.{name} rows {rows}: walk vs smem"
+        assert G.rel_err(a, tma[k].double().cpu().numpy()) <= 1e-5, f"{case}.{name} rows {rows}: walk vs tma"
+
+
+def test_walk_form_on_a_larger_synthetic_grid():
+    """Many strips and walks, the cyclic x-halo images and the array edges."""
+    from veris_gb300.evp_solver import evp_solver_fast
+    from veris_gb300.state import VerisState
+    from veris_gb300.synthetic import config_settings, make_state
+    st = VerisState.from_numpy(make_state(300, 150, seed=4, init_velocity=0.05), config_settings("c3_1deg"))
+    from veris_gb300 import model
+    for name in ("SeaIceMass", "AreaWS", "WindForcingXY", "SeaIceStrength"):
+        fn, outs = [(f, o) for n, f, o in model.STEP if n == name][0]
+        vals = fn(st)
+        vals = vals if isinstance(vals, tuple) else (vals,)
+        for o, x in zip(outs, vals):
+            setattr(st.variables, o, x)
+    smem = evp_solver_fast(st, "f32", "smem", n_subcycles=20)
+    for rows, variant in ((16, 0), (33, 1), (8, 3)):
+        walk = evp_solver_fast(st, "f32", "walk", n_subcycles=20, rows=rows, variant=variant)
+        for k in range(5):
+            e = G.rel_err(walk[k].double().cpu().numpy(), smem[k].double().cpu().numpy())
+            assert e <= 1e-5, (rows, k, e)

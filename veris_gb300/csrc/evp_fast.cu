@@ -195,7 +195,7 @@ static size_t tape_field(const Dims &d) { return rup256((size_t)d.NX * internal_
 template <class T>
 static int evp_fast(const VerisGrid *g, const VerisParams *p, const VerisFieldsF64 *vs64, int n, T *uo, T *vo,
                     T *s1o, T *s2o, T *s12o, void *ws, size_t wsb, int allow_tma, veris_stream_t s,
-                    T *tape = nullptr, size_t tape_bytes = 0) {
+                    T *tape = nullptr, size_t tape_bytes = 0, int walk_variant = 0) {
     Dims d;
     VERIS_CHECK_GRID(g, d);
     VERIS_REQUIRE(p && vs64 && uo && vo && s1o && s2o && s12o, VERIS_ERR_ARG);
@@ -240,6 +240,8 @@ static int evp_fast(const VerisGrid *g, const VerisParams *p, const VerisFieldsF
         return VERIS_OK;
     }
     if constexpr (sizeof(T) == 4) {
+        if (allow_tma >= 4)   // the register-walking kernel, allow_tma output rows per walk
+            return evp_walk_subcycles(d, h, c, k, state, outs, d.ld, n, basal, turn, allow_tma, walk_variant, st);
         if (allow_tma) {
             stt = evp_tma_subcycles(d, h, c, k, state, outs, d.ld, n, status, basal, turn, st);
             if (stt != VERIS_ERR_UNSUPPORTED) return stt;
@@ -302,6 +304,13 @@ int veris_evp_fast_solver_f32(const VerisGrid *g, const VerisParams *p, const Ve
                               float *u, float *v, float *s1, float *s2, float *s12, void *ws, size_t wsb,
                               veris_stream_t s) {
     return evp_fast<float>(g, p, vs, n, u, v, s1, s2, s12, ws, wsb, 1, s);
+}
+
+int veris_evp_walk_solver_f32(const VerisGrid *g, const VerisParams *p, const VerisFieldsF64 *vs, int32_t n,
+                              int32_t rows, int32_t variant, float *u, float *v, float *s1, float *s2, float *s12,
+                              void *ws, size_t wsb, veris_stream_t s) {
+    VERIS_REQUIRE(rows >= 4 && rows <= 4096 && variant >= 0 && variant < 4, VERIS_ERR_ARG);
+    return evp_fast<float>(g, p, vs, n, u, v, s1, s2, s12, ws, wsb, rows, s, nullptr, 0, variant);
 }
 
 int veris_evp_smem_solver_f32(const VerisGrid *g, const VerisParams *p, const VerisFieldsF64 *vs, int32_t n,

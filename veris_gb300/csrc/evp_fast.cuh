@@ -138,6 +138,12 @@ int evp_tma_subcycles(const Dims &d, const HaloFill &h, const FastConsts<float> 
                       float *const state[2][5], float *const outs[5], int64_t ldo, int n, int *status, bool basal,
                       bool turn, cudaStream_t st);
 bool evp_tma_available();
+// the same with the register-walking kernel: one warp per 28-column strip
+// walking `rows` output rows, compiled form `variant` (loop unroll x register
+// budget), reading state[0] first
+int evp_walk_subcycles(const Dims &d, const HaloFill &h, const FastConsts<float> &c, const FastScalars<float> &k,
+                       float *const state[2][5], float *const outs[5], int64_t ldo, int n, bool basal, bool turn,
+                       int rows, int variant, cudaStream_t st);
 
 template <class T>
 __device__ __forceinline__ T one_if(uint32_t f, uint32_t bit) { return (f & bit) ? T(1) : T(0); }

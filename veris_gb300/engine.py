@@ -45,14 +45,31 @@ FILLED_AFTER_GROWTH = ("hIceMean", "hSnowMean", "Area", "forc_salt_surface_ice",
 HELD_FORCING = ("Qnet", "Qsw")
 
 
+def auto_walk_rows(shape, device):
+    """Rows per walk of the register-walking EVP kernel: long walks (less
+    ring overhead) while there are still about 16 walking warps per SM."""
+    import torch
+    NX, NY = shape
+    strips = (NY + 27) // 28
+    sms = torch.cuda.get_device_properties(device).multi_processor_count
+    rows = NX * strips // (16 * sms)
+    return int(max(8, min(64, rows)))
+
+
 class SeaIceStep:
-    def __init__(self, state: VerisState, precision="f64", n_subcycles=None, evp="auto", hold_forcing=False):
+    def __init__(self, state: VerisState, precision="f64", n_subcycles=None, evp="auto", hold_forcing=False,
+                 f32_kernel="walk", walk_rows=0, walk_variant=0):
         if precision not in ("f64", "f32"):
             raise ValueError("precision must be 'f64' or 'f32'")
         if evp not in ("auto", "fast", "plain"):
             raise ValueError("evp must be 'auto', 'fast' or 'plain'")
+        if f32_kernel not in ("tma", "walk"):
+            raise ValueError("f32_kernel must be 'tma' or 'walk'")
         self.state = state
         self.precision = precision
+        self.f32_kernel = f32_kernel   # float32 fast form: register-walking warps or TMA-staged tiles
+        self.walk_rows = int(walk_rows) or auto_walk_rows(self.shape, self.device)
+        self.walk_variant = int(walk_variant)
         self.lib = _abi.load()
         v = state.variables
         s = state.settings
@@ -185,7 +202,11 @@ class SeaIceStep:
                 self._to32(getattr(v, name), self.v32[name])
             n += len(conv)
             outs = [t.data_ptr() for t in self.evp_out32]
-            if self.evp_form == "fast":
+            if self.evp_form == "fast" and self.f32_kernel == "walk":
+                check("evp_walk_f32", lib.veris_evp_walk_solver_f32(*r64, self.n_sub, self.walk_rows,
+                                                                         self.walk_variant, *outs, *ws))
+                n += self.n_sub + 1
+            elif self.evp_form == "fast":
                 check("evp_fast_f32", lib.veris_evp_fast_solver_f32(*r64, self.n_sub, *outs, *ws))
                 n += self.n_sub + 1
             else:

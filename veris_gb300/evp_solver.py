@@ -38,11 +38,13 @@ def evp_solver_f32(state32, n_subcycles=None):
     return tuple(out)
 
 
-def evp_solver_fast(state, precision="f32", form="tma", n_subcycles=None, return_status=False):
+def evp_solver_fast(state, precision="f32", form="tma", n_subcycles=None, return_status=False, rows=16,
+                    variant=0):
     """The fast forms of the loop on a float64 state: ``form`` "tma" (float32
-    only: TMA-staged tiles) or "smem" (shared-memory tiles).  Results are in
-    the arithmetic type.  Raises ``VerisError`` (status 7) for settings the
-    fast forms do not cover."""
+    only: TMA-staged tiles), "walk" (float32 only: register-walking warps,
+    ``rows`` output rows per walk) or "smem" (shared-memory tiles).  Results
+    are in the arithmetic type.  Raises ``VerisError`` (status 7) for
+    settings the fast forms do not cover."""
     import ctypes
     s = state.settings
     n = int(s.nEVPsteps if n_subcycles is None else n_subcycles)
@@ -50,11 +52,15 @@ def evp_solver_fast(state, precision="f32", form="tma", n_subcycles=None, return
     dt = torch.float32 if precision == "f32" else torch.float64
     out = [torch.empty(c.shape, dtype=dt, device=c.device) for _ in range(5)]
     ws, wsb = c.workspace(c.lib.veris_evp_fast_workspace_bytes(c.refs()[0], 4 if precision == "f32" else 8))
-    if precision == "f64":
-        fn = c.lib.veris_evp_fast_solver_f64
+    if precision == "f32" and form == "walk":
+        check("evp_solver_walk", c.lib.veris_evp_walk_solver_f32(*c.refs(), n, int(rows), int(variant),
+                                                                  *[t.data_ptr() for t in out], ws, wsb, c.stream))
     else:
-        fn = c.lib.veris_evp_fast_solver_f32 if form == "tma" else c.lib.veris_evp_smem_solver_f32
-    check("evp_solver_fast", fn(*c.refs(), n, *[t.data_ptr() for t in out], ws, wsb, c.stream))
+        if precision == "f64":
+            fn = c.lib.veris_evp_fast_solver_f64
+        else:
+            fn = c.lib.veris_evp_fast_solver_f32 if form == "tma" else c.lib.veris_evp_smem_solver_f32
+        check("evp_solver_fast", fn(*c.refs(), n, *[t.data_ptr() for t in out], ws, wsb, c.stream))
     if return_status:
         st = ctypes.c_int32(-1)
         check("evp_fast_status", c.lib.veris_evp_fast_status(ws, ctypes.byref(st), c.stream))

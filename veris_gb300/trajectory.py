@@ -140,6 +140,7 @@ class Trajectory:
         self.snap = {}
         self.stats = {"forward_steps": 0, "recomputed_steps": 0, "adjoint_steps": 0}
         self._graph_ok = False
+        self.track_norms = False   # record |adjoint| after every step (a host sync per step)
 
     # ------------------------------------------------------------ state
     def _save(self):
@@ -316,6 +317,9 @@ class Trajectory:
                                                                              "uIce", "vIce")],
             self.lscal.data_ptr(), self.ws_prep.data_ptr(), self.ws_prep.numel(), st))
         self.lam, self.lam_new = new, lam
+        if self.track_norms:
+            self.stats.setdefault("lam_norms", []).append(
+                float(torch.sqrt(sum((new[q] * new[q]).sum() for q in CARRIED))))
         # this step's start velocities are the previous step's new ones
         self.uv_next[0].copy_(v.uIce)
         self.uv_next[1].copy_(v.vIce)
