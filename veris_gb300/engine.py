@@ -68,13 +68,13 @@ class SeaIceStep:
         self.state = state
         self.precision = precision
         self.f32_kernel = f32_kernel   # float32 fast form: register-walking warps or TMA-staged tiles
-        self.walk_rows = int(walk_rows) or auto_walk_rows(self.shape, self.device)
         self.walk_variant = int(walk_variant)
         self.lib = _abi.load()
         v = state.variables
         s = state.settings
         self.shape = tuple(v.iceMask.shape)
         self.device = v.iceMask.device
+        self.walk_rows = int(walk_rows) or auto_walk_rows(self.shape, self.device)
         NX, NY = self.shape
         self.n_sub = int(s.nEVPsteps if n_subcycles is None else n_subcycles)
         self.grid = _abi.VerisGrid(NX - 2 * s.olx, NY - 2 * s.oly, s.olx, s.oly, NY)
