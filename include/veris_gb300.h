@@ -224,7 +224,8 @@ int veris_evp_fast_solver_f64(const VerisGrid *g, const VerisParams *p, const Ve
 /* the float32 fast form without TMA staging (the shared-memory kernel only) */
 /*
  * The same float32 loop with the register-walking kernel: one warp per
- * 28-column strip walks `rows` output rows (4..4096), rows in registers and
+ * 28-column strip walks `rows` output rows (4..4096; 0: the longest walk
+ * that keeps all walks in one wave of resident warps), rows in registers and
  * columns across lanes; no shared memory, no barriers.  `variant` (0..3)
  * picks the compiled form, loop unroll x register budget: 0 = 1 x free,
  * 1 = 4 x free, 2 = 1 x 4 CTAs/SM, 3 = 4 x 4 CTAs/SM; same values.

@@ -240,8 +240,9 @@ static int evp_fast(const VerisGrid *g, const VerisParams *p, const VerisFieldsF
         return VERIS_OK;
     }
     if constexpr (sizeof(T) == 4) {
-        if (allow_tma >= 4)   // the register-walking kernel, allow_tma output rows per walk
-            return evp_walk_subcycles(d, h, c, k, state, outs, d.ld, n, basal, turn, allow_tma, walk_variant, st);
+        if (allow_tma >= 4 || allow_tma < 0)   // register-walking kernel, allow_tma rows per walk (< 0: auto)
+            return evp_walk_subcycles(d, h, c, k, state, outs, d.ld, n, basal, turn, allow_tma < 0 ? 0 : allow_tma,
+                                      walk_variant, st);
         if (allow_tma) {
             stt = evp_tma_subcycles(d, h, c, k, state, outs, d.ld, n, status, basal, turn, st);
             if (stt != VERIS_ERR_UNSUPPORTED) return stt;
@@ -309,8 +310,8 @@ int veris_evp_fast_solver_f32(const VerisGrid *g, const VerisParams *p, const Ve
 int veris_evp_walk_solver_f32(const VerisGrid *g, const VerisParams *p, const VerisFieldsF64 *vs, int32_t n,
                               int32_t rows, int32_t variant, float *u, float *v, float *s1, float *s2, float *s12,
                               void *ws, size_t wsb, veris_stream_t s) {
-    VERIS_REQUIRE(rows >= 4 && rows <= 4096 && variant >= 0 && variant < 4, VERIS_ERR_ARG);
-    return evp_fast<float>(g, p, vs, n, u, v, s1, s2, s12, ws, wsb, rows, s, nullptr, 0, variant);
+    VERIS_REQUIRE((rows == 0 || (rows >= 4 && rows <= 4096)) && variant >= 0 && variant < 4, VERIS_ERR_ARG);
+    return evp_fast<float>(g, p, vs, n, u, v, s1, s2, s12, ws, wsb, rows == 0 ? -1 : rows, s, nullptr, 0, variant);
 }
 
 int veris_evp_smem_solver_f32(const VerisGrid *g, const VerisParams *p, const VerisFieldsF64 *vs, int32_t n,

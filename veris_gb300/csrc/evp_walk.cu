@@ -269,9 +269,31 @@ static int launch(const Dims &d, int64_t lp, const HaloFill &h, const FastConsts
     return launch_status();
 }
 
+// walk length: the most rows per walk that still fits all walks in one wave
+// of resident warps (rows >= 8); ring overhead per walk is 4 rows
+template <bool B, bool R, int V>
+static int auto_rows(const Dims &d) {
+    int dev = 0, sms = 0, per_sm = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) !=
+                                                  cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, evp_walk_kernel<B, R, V>, WARPS * 32, 0) !=
+            cudaSuccess || sms <= 0 || per_sm <= 0) {
+        cudaGetLastError();
+        return 16;
+    }
+    const int strips = (d.NY + TW - 1) / TW;
+    const int blocks_per_wave = (sms * per_sm * WARPS) / strips;   // row blocks that fit next to each other
+    if (blocks_per_wave < 1) return 16;
+    int rows = (d.NX + blocks_per_wave - 1) / blocks_per_wave;
+    return rows < 8 ? 8 : (rows > 4096 ? 4096 : rows);
+}
+
 template <int V>
 static int launch_v(bool basal, bool turn, const Dims &d, int64_t lp, const HaloFill &h, const FastConsts<float> &c,
                     const FastScalars<float> &k, const FastIO<float> &io, int H, cudaStream_t st) {
+    if (H <= 0)
+        H = basal ? (turn ? auto_rows<true, true, V>(d) : auto_rows<true, false, V>(d))
+                  : (turn ? auto_rows<false, true, V>(d) : auto_rows<false, false, V>(d));
     if (basal)
         return turn ? launch<true, true, V>(d, lp, h, c, k, io, H, st) : launch<true, false, V>(d, lp, h, c, k, io, H, st);
     return turn ? launch<false, true, V>(d, lp, h, c, k, io, H, st) : launch<false, false, V>(d, lp, h, c, k, io, H, st);
@@ -283,7 +305,7 @@ int evp_walk_subcycles(const Dims &d, const HaloFill &h, const FastConsts<float>
                        float *const state[2][5], float *const outs[5], int64_t ldo, int n, bool basal, bool turn,
                        int rows, int variant, cudaStream_t st) {
     const int64_t lp = internal_pitch(d.NY);
-    if (rows < 4 || rows > 4096 || variant < 0 || variant >= walk::N_VARIANTS) return VERIS_ERR_ARG;
+    if ((rows != 0 && (rows < 4 || rows > 4096)) || variant < 0 || variant >= walk::N_VARIANTS) return VERIS_ERR_ARG;
     for (int it = 0; it < n; ++it) {
         const bool last = it == n - 1;
         const int b = it % 2;

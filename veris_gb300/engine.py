@@ -45,17 +45,6 @@ FILLED_AFTER_GROWTH = ("hIceMean", "hSnowMean", "Area", "forc_salt_surface_ice",
 HELD_FORCING = ("Qnet", "Qsw")
 
 
-def auto_walk_rows(shape, device):
-    """Rows per walk of the register-walking EVP kernel: long walks (less
-    ring overhead) while there are still about 16 walking warps per SM."""
-    import torch
-    NX, NY = shape
-    strips = (NY + 27) // 28
-    sms = torch.cuda.get_device_properties(device).multi_processor_count
-    rows = NX * strips // (16 * sms)
-    return int(max(8, min(64, rows)))
-
-
 class SeaIceStep:
     def __init__(self, state: VerisState, precision="f64", n_subcycles=None, evp="auto", hold_forcing=False,
                  f32_kernel="walk", walk_rows=0, walk_variant=0):
@@ -74,7 +63,7 @@ class SeaIceStep:
         s = state.settings
         self.shape = tuple(v.iceMask.shape)
         self.device = v.iceMask.device
-        self.walk_rows = int(walk_rows) or auto_walk_rows(self.shape, self.device)
+        self.walk_rows = int(walk_rows)   # 0: chosen by the library from the grid and the GPU
         NX, NY = self.shape
         self.n_sub = int(s.nEVPsteps if n_subcycles is None else n_subcycles)
         self.grid = _abi.VerisGrid(NX - 2 * s.olx, NY - 2 * s.oly, s.olx, s.oly, NY)
