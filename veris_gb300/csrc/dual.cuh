@@ -112,6 +112,14 @@ __device__ inline Dual<N> vexp10(const Dual<N> &a) {
     return r;
 }
 template <int N>
+__device__ inline Dual<N> vexp2(const Dual<N> &a) {
+    Dual<N> r;
+    r.v = ::exp2(a.v);
+    const double g = r.v * 0.6931471805599453094;   // d/dx 2^x = 2^x ln 2
+    for (int k = 0; k < N; ++k) r.d[k] = g * a.d[k];
+    return r;
+}
+template <int N>
 __device__ inline Dual<N> vlog(const Dual<N> &a) {
     Dual<N> r;
     r.v = ::log(a.v);
@@ -127,6 +135,7 @@ __device__ inline Dual<N> vfabs(const Dual<N> &a) {
 __device__ inline double vsqrt(double x) { return ::sqrt(x); }
 __device__ inline double vexp(double x) { return ::exp(x); }
 __device__ inline double vexp10(double x) { return ::exp10(x); }
+__device__ inline double vexp2(double x) { return ::exp2(x); }
 __device__ inline double vlog(double x) { return ::log(x); }
 __device__ inline double vfabs(double x) { return ::fabs(x); }
 __device__ inline float vfabs(float x) { return ::fabsf(x); }

@@ -1,6 +1,8 @@
 // Thermodynamics in float64: the surface-temperature Newton solve
 // (veris/solve4temp.py:5-174) and ice growth with the ocean budgets
 // (veris/growth.py:8-397).  Both are pointwise; one thread per padded point.
+#include <type_traits>
+
 #include "stencil.cuh"
 #include "dual.cuh"
 
@@ -86,9 +88,7 @@ __device__ S4TOut solve4temp_point(const VerisParams &p, const S4TIn &x) {
 // veris/solve4temp.py:5-174 for NC thickness categories of one cell at once.
 // The categories differ only in their ice and snow thickness; their Newton
 // iterations are independent, so they advance in lockstep and the float64
-// dependency chains interleave.  Per flux evaluation one exp10 gives both
-// 10^(aa1/T) and the saturation vapour pressure 10^(aa2 - aa1/T) =
-// 10^aa2 / 10^(aa1/T), and one reciprocal of T serves every division by T.
+// dependency chains interleave.
 // S is double, or a dual number when the adjoint needs the derivatives with
 // respect to the ice state (branches follow the values either way).
 template <int NC, class S>
@@ -131,29 +131,59 @@ __device__ void solve4temp_multi(const VerisParams &p, const S4TIn &x, const S &
         T[l] = Tin;
     }
     S Fc[NC], Fia[NC];
+    bool moving[NC];
+#pragma unroll
+    for (int l = 0; l < NC; ++l) moving[l] = ice[l];
+    // One flux evaluation per category; with `newton` also the Newton update.
+    // The residual (Fc - Fia) is evaluated in float64 with two divisions:
+    // 10^(aa1/T) = 2^(aa1 log2(10) / T) and, since svp = cc0 / 10^(aa1/T),
+    // qs = bb1 svp / (Pa - (1-bb1) svp) = bb1 cc0 / (10^(aa1/T) Pa - (1-bb1) cc0).
+    // The Newton derivative only sets the convergence rate, not the root:
+    // in float64 arithmetic it and the step use float32 reciprocals (the
+    // iteration still converges to the float64 root); dual numbers keep the
+    // exact step so that the adjoint differentiates a smooth map.  A
+    // category stops once an update moves T by less than 1e-13 T.
+    const double aa1l2 = aa1 * 3.32192809488736234787;   // aa1 log2(10)
+    const double qnum = bb1 * cc0, qsub = one_m_bb1 * cc0;
     auto fluxes = [&](bool newton) {
 #pragma unroll
         for (int l = 0; l < NC; ++l) {
+            if (newton && !moving[l]) continue;
             const S t1 = T[l];
             const S rt = 1.0 / t1;
             const S t2 = t1 * t1, t3 = t2 * t1, t4 = t2 * t2;
-            const S c3 = vexp10(aa1 * rt);
-            const S svp = cc0 / c3;
-            const S qs = bb1 * svp / (Pa - one_m_bb1 * svp);
-            const S den = cc2 - c3 * Pa;
-            const S dqs = cc1 * c3 / (den * den * t2);
+            const S c3 = vexp2(aa1l2 * rt);
+            const S qs = qnum / (c3 * Pa - qsub);
             Fc[l] = ice[l] ? k[l] * (x.TempFrz - t1) : S(0.0);
             const S Flh = ice[l] ? d1iug * (qs - x.aqh) : S(0.0);
             Fia[l] = ice[l] ? (lwabs[l] + t4 * d3[l] + d1ug * (t1 - Ta) + Flh) : S(0.0);
             if (newton) {
-                const S dF = ice[l] ? 4 * d3[l] * t3 + d1ug + d1iug * dqs : S(0.0);
-                S Tn = ice[l] ? t1 + (Fc[l] - Fia[l]) / (k[l] + dF) : S(0.0);
+                const S den = cc2 - c3 * Pa;
+                S Tn;
+                if constexpr (std::is_same<S, double>::value) {
+                    const float rden = __frcp_rn((float)den);
+                    const double dqs = (double)((float)(cc1 * c3) * rden * rden * (float)(rt * rt));
+                    const double dF = 4 * d3[l] * t3 + d1ug + d1iug * dqs;
+                    Tn = ice[l] ? t1 + (Fc[l] - Fia[l]) * (double)__frcp_rn((float)(k[l] + dF)) : 0.0;
+                } else {
+                    const S dqs = cc1 * c3 * (rt * rt) / (den * den);
+                    const S dF = ice[l] ? 4 * d3[l] * t3 + d1ug + d1iug * dqs : S(0.0);
+                    Tn = ice[l] ? t1 + (Fc[l] - Fia[l]) / (k[l] + dF) : S(0.0);
+                }
                 Tn = smin(Tn, S(Tmelt));
-                T[l] = smax(Tn, S(Tmin));
+                Tn = smax(Tn, S(Tmin));
+                if (vfabs(val(Tn) - val(t1)) <= 1e-13 * val(t1)) moving[l] = false;
+                T[l] = Tn;
             }
         }
     };
-    for (int it = 0; it < 6; ++it) fluxes(true);
+    for (int it = 0; it < 6; ++it) {
+        bool any = false;
+#pragma unroll
+        for (int l = 0; l < NC; ++l) any = any || moving[l];
+        if (!any) break;
+        fluxes(true);
+    }
     fluxes(false);
 #pragma unroll
     for (int l = 0; l < NC; ++l) {
