@@ -142,7 +142,7 @@ __device__ void solve4temp_multi(const VerisParams &p, const S4TIn &x, const S &
     // in float64 arithmetic it and the step use float32 reciprocals (the
     // iteration still converges to the float64 root); dual numbers keep the
     // exact step so that the adjoint differentiates a smooth map.  A
-    // category stops once an update moves T by less than 1e-13 T.
+    // category stops once an update moves T by less than 4e-9 T.
     const double aa1l2 = aa1 * 3.32192809488736234787;   // aa1 log2(10)
     const double qnum = bb1 * cc0, qsub = one_m_bb1 * cc0;
     auto fluxes = [&](bool newton) {
@@ -172,11 +172,42 @@ __device__ void solve4temp_multi(const VerisParams &p, const S4TIn &x, const S &
                 }
                 Tn = smin(Tn, S(Tmelt));
                 Tn = smax(Tn, S(Tmin));
-                if (vfabs(val(Tn) - val(t1)) <= 1e-13 * val(t1)) moving[l] = false;
+                // |update| <= 4e-9 T (about 1e-6 K): the error left is below
+                // 1e-7 of the update (float32 derivative) plus C update^2 with
+                // C = F''/2F' ~ 1e-3 / K, i.e. ~1e-13 K, far inside the float64
+                // parity of the fixed six iterations
+                if (vfabs(val(Tn) - val(t1)) <= 4e-9 * val(t1)) moving[l] = false;
                 T[l] = Tn;
             }
         }
     };
+    if constexpr (std::is_same<S, double>::value) {
+        // float32 Newton iterations bring T to ~1e-4 K of the root first; the
+        // float64 iterations below then converge in one or two updates
+        const float aa1l2f = (float)aa1l2, qnumf = (float)qnum, qsubf = (float)qsub, Paf = (float)Pa;
+        const float cc1f = (float)cc1, cc2f = (float)cc2, TFf = (float)x.TempFrz, aqhf = (float)x.aqh;
+        const float d1ugf = (float)d1ug, d1iugf = (float)d1iug, Taf = (float)Ta;
+        const float Tmeltf = (float)Tmelt, Tminf = (float)Tmin;
+#pragma unroll
+        for (int l = 0; l < NC; ++l) {
+            if (!ice[l]) continue;
+            float t = (float)T[l];
+            const float kf = (float)k[l], lwf = (float)lwabs[l], d3f = (float)d3[l];
+            for (int it = 0; it < 3; ++it) {
+                const float rt = __frcp_rn(t);
+                const float t2 = t * t;
+                const float c3 = exp2f(aa1l2f * rt);
+                const float qs = __fdividef(qnumf, c3 * Paf - qsubf);
+                const float den = __frcp_rn(cc2f - c3 * Paf);
+                const float dqs = (cc1f * c3 * den) * den * (rt * rt);
+                const float Fcf = kf * (TFf - t);
+                const float Fiaf = lwf + t2 * t2 * d3f + d1ugf * (t - Taf) + d1iugf * (qs - aqhf);
+                const float dF = 4.f * d3f * t2 * t + d1ugf + d1iugf * dqs;
+                t = fminf(fmaxf(t + (Fcf - Fiaf) * __frcp_rn(kf + dF), Tminf), Tmeltf);
+            }
+            T[l] = (double)t;
+        }
+    }
     for (int it = 0; it < 6; ++it) {
         bool any = false;
 #pragma unroll
