@@ -179,11 +179,13 @@ def hbm_peak():
         return 6800.0, "fallback"
 
 
-def recorded_traffic(precision):
+def recorded_traffic(kernel, workload):
+    """DRAM bytes per launch of ``kernel`` on ``workload`` from an ncu capture
+    (profiles/roofline_traffic.json), or None."""
     path = os.path.join(ROOT, "profiles", "roofline_traffic.json")
     try:
         with open(path) as f:
-            return json.load(f).get(f"evp_{precision}_c2_bytes_per_launch")
+            return json.load(f).get(f"{kernel}/{workload}")
     except (OSError, ValueError):
         return None
 
@@ -341,13 +343,13 @@ def run_ours(args):
     algo_bytes = BYTES_PER_CELL_SUBCYCLE[args.precision] * cells
     achieved = algo_bytes / per_launch_s / 1e9
     peak, peak_kind = hbm_peak()
-    traffic = recorded_traffic(args.precision)
+    kernel = (("evp_walk_kernel" if args.f32_kernel == "walk" else "evp_tma_kernel")
+              if eng.evp_form == "fast" and args.precision == "f32" else
+              ("evp_fast_kernel" if eng.evp_form == "fast" else "evp_subcycle_kernel")
+              + f"<{'float' if args.precision == 'f32' else 'double'}>")
+    traffic = recorded_traffic(kernel, args.config)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "traffic": traffic,
-                "kernel": (("evp_walk_kernel" if args.f32_kernel == "walk" else "evp_tma_kernel")
-                           if eng.evp_form == "fast" and args.precision == "f32" else
-                           ("evp_fast_kernel" if eng.evp_form == "fast" else "evp_subcycle_kernel")
-                           + f"<{'float' if args.precision == 'f32' else 'double'}>"),
+                "frac": achieved / peak, "traffic": traffic, "kernel": kernel,
                 "algorithmic_bytes_per_launch": algo_bytes, "avg_launch_us": per_launch_s * 1e6,
                 "peak_source": f"{peak_kind} HBM copy bandwidth"}
 
