@@ -37,6 +37,7 @@ def _single(member, n):
 
 @pytest.mark.parametrize("shape", (0, 1, 2, 3))
 def test_batch_equals_single_domain(shape):
+    """Shared-memory tiles: bit for bit the single-domain shared-memory form."""
     from veris_gb300.ensemble import EVP_STATE, Ensemble
     members = _members()
     ens = Ensemble(members, N_SUB, shape=shape, blocks_per_sm=2)
@@ -44,6 +45,23 @@ def test_batch_equals_single_domain(shape):
     torch.cuda.synchronize()
     for m, st in enumerate(members):
         ref = _single(st, N_SUB)
+        got = ens.state(m)
+        for k, r in zip(EVP_STATE, ref):
+            assert torch.equal(got[k], r), (shape, m, k, float((got[k] - r).abs().max()))
+
+
+@pytest.mark.parametrize("shape", (4, 5, 6))
+def test_batch_walks_equal_single_domain_walks(shape):
+    """Register walks: bit for bit the single-domain walking form with the
+    same walk length."""
+    from veris_gb300.ensemble import EVP_STATE, SHAPES, Ensemble
+    from veris_gb300.evp_solver import evp_solver_fast
+    members = _members()
+    ens = Ensemble(members, N_SUB, shape=shape, blocks_per_sm=3)
+    ens.step()
+    torch.cuda.synchronize()
+    for m, st in enumerate(members):
+        ref = evp_solver_fast(st, "f32", "walk", n_subcycles=N_SUB, rows=SHAPES[shape][0], variant=2)
         got = ens.state(m)
         for k, r in zip(EVP_STATE, ref):
             assert torch.equal(got[k], r), (shape, m, k, float((got[k] - r).abs().max()))

@@ -15,7 +15,7 @@ import torch
 
 from .ensemble import SHAPES
 
-DEFAULT_CANDIDATES = tuple((s, b) for s in SHAPES for b in (1, 2, 3, 4))
+DEFAULT_CANDIDATES = tuple((s, b) for s in SHAPES for b in ((1, 2, 3, 4) if s < 4 else (2, 3, 4)))
 
 
 def _cache_path():

@@ -16,11 +16,15 @@
 // where each member holds the fast-form layout (constants + two states) and
 // its float32 wind forcing (for refolding the momentum constant each step).
 #include "evp_tile.cuh"
+#include "evp_walk.cuh"
 
 namespace veris {
 namespace batch {
 
-constexpr int N_SHAPES = 4;
+// shapes 0-3: shared-memory tiles (rows x columns); 4-6: register walks of
+// 8, 16 or 32 rows over 28-column strips (one warp each)
+constexpr int N_SHAPES = 7;
+constexpr int FIRST_WALK = 4;
 template <int S>
 struct ShapeOf;
 template <>
@@ -33,7 +37,7 @@ template <>
 struct ShapeOf<3> { static constexpr int TI = 16, TJ = 16, MINB = 4; };
 
 inline void shape_dims(int s, int *ti, int *tj) {
-    static const int T[N_SHAPES][2] = {{32, 32}, {16, 32}, {32, 16}, {16, 16}};
+    static const int T[N_SHAPES][2] = {{32, 32}, {16, 32}, {32, 16}, {16, 16}, {8, 28}, {16, 28}, {32, 28}};
     *ti = T[s][0];
     *tj = T[s][1];
 }
@@ -135,6 +139,43 @@ evp_batch_kernel(const Member *mem, const int *tile_start, int nmem, int ntiles,
     }
 }
 
+// the same work queue with one register walk per ticket, one ticket per warp
+template <bool BASAL, bool TURN>
+__global__ void __launch_bounds__(128, 4)
+evp_batch_walk_kernel(const Member *mem, const int *walk_start, int nmem, int nwalks, FastScalars<float> k, int buf,
+                      unsigned *queue, unsigned base, int H) {
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        unsigned tk = 0;
+        if (lane == 0) tk = atomicAdd(queue, 1u);
+        const int t = (int)(__shfl_sync(0xffffffffu, tk, 0) - base);
+        if (t >= nwalks) break;
+        int lo = 0, hi = nmem - 1;   // last member whose first walk is <= t
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (__ldg(walk_start + mid) <= t) lo = mid;
+            else hi = mid - 1;
+        }
+        const Member &m = mem[lo];
+        const int lt = t - __ldg(walk_start + lo);
+        const int nstrips = (m.d.NY + walk::TW - 1) / walk::TW;
+        FastIO<float> io;
+        io.u = m.state[buf][0];
+        io.v = m.state[buf][1];
+        io.s1 = m.state[buf][2];
+        io.s2 = m.state[buf][3];
+        io.s12 = m.state[buf][4];
+        io.uo = m.state[buf ^ 1][0];
+        io.vo = m.state[buf ^ 1][1];
+        io.s1o = m.state[buf ^ 1][2];
+        io.s2o = m.state[buf ^ 1][3];
+        io.s12o = m.state[buf ^ 1][4];
+        io.ldo = m.lp;
+        walk::walk_strip<BASAL, TURN, 1>(m.d, m.lp, m.h, m.c, k, io, (lt / nstrips) * H, (lt % nstrips) * walk::TW, H,
+                                         lane);
+    }
+}
+
 // cU = mU/dt u + WindForcingX, cV likewise, from the state in buffer buf
 // (the fold fast_prep does once per step, for the steps after the first)
 __global__ void refold_kernel(const Member *mem, int nmem, float rdt, int buf) {
@@ -177,6 +218,23 @@ static int launch_s(bool basal, bool turn, const Member *mem, const int *ts, int
                     : launch<S, true, false>(mem, ts, nmem, ntiles, k, buf, queue, base, blocks, st);
     return turn ? launch<S, false, true>(mem, ts, nmem, ntiles, k, buf, queue, base, blocks, st)
                 : launch<S, false, false>(mem, ts, nmem, ntiles, k, buf, queue, base, blocks, st);
+}
+
+template <bool B, bool R>
+static int launch_walk(const Member *mem, const int *ts, int nmem, int ntiles, const FastScalars<float> &k, int buf,
+                       unsigned *queue, unsigned base, int blocks, int H, cudaStream_t st) {
+    evp_batch_walk_kernel<B, R><<<blocks, 128, 0, st>>>(mem, ts, nmem, ntiles, k, buf, queue, base, H);
+    return launch_status();
+}
+
+static int launch_walk_s(bool basal, bool turn, const Member *mem, const int *ts, int nmem, int ntiles,
+                         const FastScalars<float> &k, int buf, unsigned *queue, unsigned base, int blocks, int H,
+                         cudaStream_t st) {
+    if (basal)
+        return turn ? launch_walk<true, true>(mem, ts, nmem, ntiles, k, buf, queue, base, blocks, H, st)
+                    : launch_walk<true, false>(mem, ts, nmem, ntiles, k, buf, queue, base, blocks, H, st);
+    return turn ? launch_walk<false, true>(mem, ts, nmem, ntiles, k, buf, queue, base, blocks, H, st)
+                : launch_walk<false, false>(mem, ts, nmem, ntiles, k, buf, queue, base, blocks, H, st);
 }
 
 static int sm_count() {
@@ -300,14 +358,26 @@ int veris_batch_evp_f32(int32_t n, const VerisGrid *grids, const VerisParams *p,
     if (n_subcycles == 0) return VERIS_OK;
     const int nsm = sm_count();
     VERIS_REQUIRE(nsm > 0, VERIS_ERR_LAUNCH);
-    const int bps = blocks_per_sm > 0 ? blocks_per_sm : 2;
-    const int blocks = min(nsm * bps, ntiles);
+    const bool walker = shape >= FIRST_WALK;
+    const int bps = blocks_per_sm > 0 ? blocks_per_sm : (walker ? 4 : 2);
+    // tile kernels draw one ticket per CTA, the walk kernel one per warp;
+    // every drawer ends on one ticket past the last
+    const int blocks = walker ? min(nsm * bps, (ntiles + 3) / 4) : min(nsm * bps, ntiles);
+    const int drawers = walker ? blocks * 4 : blocks;
     if (cudaMemsetAsync(queue, 0, sizeof(unsigned), cs) != cudaSuccess) return VERIS_ERR_LAUNCH;
     const FastScalars<float> k = fast_scalars<float>(*p);
     const bool basal = p->basalDragK2 != 0.0, turn = p->sinWat != 0.0;
     int buf = start_buf;
     for (int it = 0; it < n_subcycles; ++it) {
-        const unsigned b = (unsigned)it * (unsigned)(ntiles + blocks);
+        const unsigned b = (unsigned)it * (unsigned)(ntiles + drawers);
+        if (walker) {
+            int H, tj;
+            shape_dims(shape, &H, &tj);
+            st = launch_walk_s(basal, turn, mem, tstart, n, ntiles, k, buf, queue, b, blocks, H, cs);
+            if (st != VERIS_OK) return st;
+            buf ^= 1;
+            continue;
+        }
         switch (shape) {
         case 0: st = launch_s<0>(basal, turn, mem, tstart, n, ntiles, k, buf, queue, b, blocks, cs); break;
         case 1: st = launch_s<1>(basal, turn, mem, tstart, n, ntiles, k, buf, queue, b, blocks, cs); break;

@@ -1,31 +1,11 @@
-// Register-walking float32 mEVP subcycle (veris/evp_solver.py:21-254, the
-// fast form's arithmetic with the TMA kernel's approximate square root and
-// division).
-//
-// One warp owns a strip of 28 output columns (lanes = columns j0-2 .. j0+29,
-// i.e. the strip plus a 2-cell ring) and walks down H output rows plus a
-// 2-row ring at each end.  At walk step t it has row t's inputs and runs, on
-// the rows the stencil chain has completed,
-//
-//   A  e12 at the Z points of row t            (rows t, t-1)
-//   B  viscosities, sigma1/2, drag, Coriolis    at the C points of row t-1
-//   C  sigma12 at the Z points of row t-1      (rows t-1, t-2)
-//   D  u and v at the U/V points of row t-2     (rows t-1 .. t-3)
-//
-// Neighbours along a row come from warp shuffles, neighbours across rows from
-// the registers of the previous steps: no shared memory and no barrier.  The
-// next row's inputs are loaded one step ahead.  Warps are independent; a CTA
-// is just a group of them.
-//
-// The inputs are read straight from the fast form's planar arrays (a
-// repacked float4/float2 layout was measured slower: its wider loads stalled
-// longer on the memory system at the same bytes).
-#include "evp_fast.cuh"
+// Register-walking float32 mEVP subcycle kernels (the walk is in
+// evp_walk.cuh): one launch per subcycle, one warp per walk, and the host
+// loop with the walk-length choice.
+#include "evp_walk.cuh"
 
 namespace veris {
 namespace walk {
 
-constexpr int TW = 28;      // output columns per strip
 constexpr int WARPS = 4;    // warps per CTA
 // kernel variants: (loop unroll, CTAs per SM the register budget must allow)
 template <int V>
@@ -40,47 +20,6 @@ template <>
 struct Variant<3> { static constexpr int UNROLL = 4, MINB = 4; };
 constexpr int N_VARIANTS = 4;
 
-__device__ __forceinline__ float up(float x) { return __shfl_up_sync(0xffffffffu, x, 1); }     // lane - 1
-__device__ __forceinline__ float dn(float x) { return __shfl_down_sync(0xffffffffu, x, 1); }   // lane + 1
-__device__ __forceinline__ uint32_t upu(uint32_t x) { return __shfl_up_sync(0xffffffffu, x, 1); }
-__device__ __forceinline__ uint32_t dnu(uint32_t x) { return __shfl_down_sync(0xffffffffu, x, 1); }
-
-__device__ __forceinline__ float sqrt_approx(float x) {
-    float y;
-    asm("sqrt.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
-    return y;
-}
-
-// the ring inputs of one staged row (one column per lane)
-struct Row {
-    float u, v, s1, s2, s12, uo, vo, mf, ph, qr, rz, bf;
-    uint32_t f;
-    float rdxV, rdxU, dxU, dxV;   // metrics of the row
-};
-
-template <bool BASAL>
-__device__ __forceinline__ void load_row(Row &r, const FastConsts<float> &c, const FastIO<float> &io, int64_t lp,
-                                         int gi, int gj) {
-    const int64_t o = (int64_t)gi * lp + gj;
-    r.u = __ldg(io.u + o);
-    r.v = __ldg(io.v + o);
-    r.s1 = __ldg(io.s1 + o);
-    r.s2 = __ldg(io.s2 + o);
-    r.s12 = __ldg(io.s12 + o);
-    r.uo = __ldg(c.uOc + o);
-    r.vo = __ldg(c.vOc + o);
-    r.mf = __ldg(c.mfC + o);
-    r.ph = __ldg(c.Ph + o);
-    r.qr = __ldg(c.qrA + o);
-    r.rz = __ldg(c.rAz + o);
-    r.bf = BASAL ? __ldg(c.bfac + o) : 0.f;
-    r.f = __ldg(c.flags + o);
-    r.rdxV = __ldg(c.rdxV_x + gi);
-    r.rdxU = __ldg(c.rdxU_x + gi);
-    r.dxU = __ldg(c.dxU_x + gi);
-    r.dxV = __ldg(c.dxV_x + gi);
-}
-
 template <bool BASAL, bool TURN, int V>
 __global__ void __launch_bounds__(WARPS * 32, Variant<V>::MINB)
 evp_walk_kernel(Dims d, int64_t lp, HaloFill h, FastConsts<float> c, FastScalars<float> k, FastIO<float> io,
@@ -89,174 +28,7 @@ evp_walk_kernel(Dims d, int64_t lp, HaloFill h, FastConsts<float> c, FastScalars
     const int w = blockIdx.x * WARPS + (threadIdx.x >> 5);
     if (w >= nwalks) return;   // whole warps only
     const int strip = w % nstrips, rb = w / nstrips;
-    const int j0 = strip * TW, i0 = rb * H;
-    const int jl = j0 - 2 + lane;   // this lane's column (may lie outside [0, NY): wraps)
-    const int gj = d.wy(jl);
-    const float rdyU = __ldg(c.rdyU_y + gj), rdyV = __ldg(c.rdyV_y + gj);
-    const float dyV = __ldg(c.dyV_y + gj), dyU = __ldg(c.dyU_y + gj);
-    const bool own_j = lane >= 2 && lane < 2 + TW && jl < d.NY;
-    const bool images = (h.x_fill && (i0 < 4 || i0 + H > d.NX - 4)) || (h.y_fill && (j0 < 4 || j0 + TW > d.NY - 4));
-    const int64_t ldo = io.ldo;
-
-    Row Pf, N, A, B, C;   // prefetched (t+1), current (t), and rows t-1, t-2, t-3
-    A.f = B.f = C.f = 0u;
-    A.u = A.v = A.uo = A.vo = B.u = B.v = B.uo = B.vo = C.u = C.uo = 0.f;
-    // per-row results: e12/z2 of row t-1; B- and C-stage outputs of rows t-2 (a) and t-3 (b)
-    float e12a = 0.f, z2a = 0.f, zeta_a = 0.f;
-    float s11_a = 0.f, s11_b = 0.f, s22_a = 0.f;
-    float cd_a = 0.f, cd_b = 0.f, cb_a = 0.f, cb_b = 0.f;
-    float fv_a = 0.f, fv_b = 0.f, fu_a = 0.f, s12_a = 0.f;
-    load_row<BASAL>(Pf, c, io, lp, d.wx(i0 - 2), gj);
-    const int T = H + 4;   // rows i0-2 .. i0+H+1
-    // unrolled by the rotation period (variants 1, 3), so that the row ages
-    // are renamed registers rather than copies
-#pragma unroll Variant<V>::UNROLL
-    for (int t = 0; t < T; ++t) {
-        N = Pf;
-        if (t + 1 < T) load_row<BASAL>(Pf, c, io, lp, d.wx(i0 - 2 + t + 1), gj);
-        // own-point constants of row t-2 (stage D)
-        const int64_t ob = (int64_t)d.wx(i0 + t - 4) * lp + gj;
-        float cU = 0.f, cV = 0.f, AW = 0.f, AS = 0.f, mU = 0.f, mV = 0.f, rrAu = 0.f, rrAv = 0.f;
-        if (t >= 4) {
-            cU = __ldg(c.cU + ob);
-            cV = __ldg(c.cV + ob);
-            AW = __ldg(c.AW + ob);
-            AS = __ldg(c.AS + ob);
-            mU = __ldg(c.mU + ob);
-            mV = __ldg(c.mV + ob);
-            rrAu = __ldg(c.rrAu + ob);
-            rrAv = __ldg(c.rrAv + ob);
-        }
-
-        // ---- A: e12 at Z points of row t
-        const uint32_t fs = upu(N.f), fws = upu(A.f);
-        const float mzh = (N.f & A.f & fs & fws & F_MC) ? 0.5f : 0.f;
-        const float hU = one_if<float>(N.f, F_MU) - one_if<float>(fs, F_MU);
-        const float hV = one_if<float>(N.f, F_MV) - one_if<float>(A.f, F_MV);
-        const float us = up(N.u);
-        const float e12n = rdyU * (mzh * (N.u - us) + hU * (N.u + us)) + N.rdxV * (mzh * (N.v - A.v) + hV * (N.v + A.v));
-        const float z2n = N.rz * (e12n * e12n);
-
-        float zeta_new = 0.f, s11_new = 0.f, s22_new = 0.f, cd_new = 0.f, cb_new = 0.f, fv_new = 0.f, fu_new = 0.f;
-        float s12_new = 0.f;
-        if (t >= 2) {
-            // ---- B: C points of row t-1 (A holds its inputs, N the next row)
-            const float mInC = one_if<float>(A.f, F_INC);
-            const float vn = dn(A.v);
-            const float e11 = (N.u - A.u) * A.rdxU * mInC;
-            const float e22 = (vn - A.v) * rdyV * mInC;
-            const float e12c = A.qr * ((z2a + z2n) + (dn(z2a) + dn(z2n)));
-            const float ep = e11 + e22, em = e11 - e22;
-            const float delta = sqrt_approx(ep * ep + k.rsq * (em * em + 4.f * e12c));
-            const float zeta = __fdividef(A.ph, delta + k.deltaMin);
-            zeta_new = zeta;
-            const float mC = one_if<float>(A.f, F_MC);
-            const float press = k.kp * zeta * delta;
-            const float s1 = (A.s1 * k.alpha_m1 + (2.f * zeta * ep - press)) * k.ralpha * mC;
-            const float s2 = (A.s2 * k.alpha_m1 + 0.5f * zeta * em) * k.ralpha * mC;
-            s11_new = 0.5f * (s1 + s2) * dyV;
-            s22_new = 0.5f * (s1 - s2) * A.dxU;
-            const int oi = i0 + t - 3;
-            if (own_j && t >= 3 && t <= H + 2 && oi < d.NX) {
-                const int64_t wo = (int64_t)oi * ldo + jl;
-                io.s1o[wo] = s1;
-                io.s2o[wo] = s2;
-            }
-            const uint32_t fe = N.f, fn = dnu(A.f);
-            const float du0 = (A.u - A.uo) * one_if<float>(A.f, F_INU);
-            const float du1 = (N.u - N.uo) * one_if<float>(fe, F_INU);
-            const float dv0 = (A.v - A.vo) * one_if<float>(A.f, F_INV);
-            const float dv1 = (vn - dn(A.vo)) * one_if<float>(fn, F_INV);
-            const float tt = 0.25f * ((du0 + du1) * (du0 + du1) + (dv0 + dv1) * (dv0 + dv1));
-            const bool south = A.f & F_SOUTH;
-            const float dc = south ? k.dS : k.dN, dc2 = south ? k.dS2 : k.dN2;
-            cd_new = ((dc2 * tt > k.cmin2) ? dc * sqrt_approx(tt) : k.cmin) * mC;
-            if (BASAL) {
-                const float a = A.u * one_if<float>(A.f, F_INU), b = N.u * one_if<float>(fe, F_INU);
-                const float cc = A.v * one_if<float>(A.f, F_INV), e = vn * one_if<float>(fn, F_INV);
-                const float sq2 = 0.25f * (a * a + b * b + cc * cc + e * e);
-                cb_new = __fdividef(A.bf, sqrt_approx(sq2 + k.U02));
-            }
-            fv_new = A.mf * (A.v + vn);
-            fu_new = A.mf * (A.u + N.u);
-        }
-        if (t >= 3) {
-            // ---- C: sigma12 at Z points of row t-1
-            const uint32_t fa = A.f, fb = B.f, fas = upu(A.f), fbs = upu(B.f);
-            const int n = ((fa & F_MC) ? 1 : 0) + ((fb & F_MC) ? 1 : 0) + ((fas & F_MC) ? 1 : 0) + ((fbs & F_MC) ? 1 : 0);
-            const float norm = n == 0 ? 0.f : (n == 1 ? 1.f : (n == 2 ? 0.5f : (n == 3 ? 1.f / 3.f : 0.25f)));
-            const float zz = norm * ((zeta_new + zeta_a) + (up(zeta_new) + up(zeta_a)));
-            s12_new = (A.s12 * k.alpha_m1 + 0.5f * zz * e12a) * k.ralpha;
-            const int oi = i0 + t - 3;
-            if (own_j && t <= H + 2 && oi < d.NX) io.s12o[(int64_t)oi * ldo + jl] = s12_new;
-        }
-        if (t >= 4) {
-            // ---- D: u, v at the U/V points of row t-2 (B holds its inputs)
-            const int oi = i0 + t - 4;
-            const uint32_t f0 = B.f;
-            float un, vnew;
-            {   // U point
-                const float kU = k.halfCos * AW * (cd_a + cd_b);
-                float fx = cU + kU * B.uo + 0.5f * (fv_a + fv_b);
-                if (TURN) {
-                    const float sg = (f0 & F_SPOS) ? 1.f : ((f0 & F_SNEG) ? -1.f : 0.f);
-                    const float du0 = B.uo - B.u, dun = dn(B.uo - B.u);
-                    const float duw = C.uo - C.u, duwn = dn(C.uo - C.u);
-                    fx -= sg * k.sinW * 0.5f * (cd_a * 0.5f * (du0 + dun) + cd_b * 0.5f * (duw + duwn)) *
-                          one_if<float>(f0, F_LMU) * AW;
-                }
-                const float sdx = rrAu * ((s11_a - s11_b) + B.dxV * (dn(s12_a) - s12_a));
-                float den = mU * k.bU1 + kU;
-                if (BASAL) den += 0.5f * AW * (cb_a + cb_b);
-                den = den == 0.f ? 1.f : den;
-                un = one_if<float>(f0, F_MU) * __fdividef(k.bU * mU * B.u + fx + sdx, den);
-            }
-            {   // V point
-                const float cds = up(cd_a);
-                const float kV = k.halfCos * AS * (cd_a + cds);
-                float fy = cV + kV * B.vo - 0.5f * (fu_a + up(fu_a));
-                if (TURN) {
-                    const float sg = (f0 & F_SPOS) ? 1.f : ((f0 & F_SNEG) ? -1.f : 0.f);
-                    const float dv0 = B.vo - B.v, dve = A.vo - A.v;
-                    const float dvs = up(B.vo - B.v), dvse = up(A.vo - A.v);
-                    fy += sg * k.sinW * 0.5f * (cd_a * 0.5f * (dv0 + dve) + cds * 0.5f * (dvs + dvse)) *
-                          one_if<float>(f0, F_LMV) * AS;
-                }
-                const float sdy = rrAv * ((s22_a - up(s22_a)) + dyU * (s12_new - s12_a));
-                float den = mV * k.bU1 + kV;
-                if (BASAL) den += 0.5f * AS * (cb_a + up(cb_a));
-                den = den == 0.f ? 1.f : den;
-                vnew = one_if<float>(f0, F_MV) * __fdividef(k.bU * mV * B.v + fy + sdy, den);
-            }
-            if (own_j && oi < d.NX) {
-                if (images) {
-                    store_filled_ld(io.uo, ldo, d, h, oi, jl, un);
-                    store_filled_ld(io.vo, ldo, d, h, oi, jl, vnew);
-                } else {
-                    io.uo[(int64_t)oi * ldo + jl] = un;
-                    io.vo[(int64_t)oi * ldo + jl] = vnew;
-                }
-            }
-        }
-        // ---- rotate: rows move one age back
-        C = B;
-        B = A;
-        A = N;
-        e12a = e12n;
-        z2a = z2n;
-        zeta_a = zeta_new;
-        s11_b = s11_a;
-        s11_a = s11_new;
-        s22_a = s22_new;
-        cd_b = cd_a;
-        cd_a = cd_new;
-        cb_b = cb_a;
-        cb_a = cb_new;
-        fv_b = fv_a;
-        fv_a = fv_new;
-        fu_a = fu_new;
-        s12_a = s12_new;
-    }
+    walk_strip<BASAL, TURN, Variant<V>::UNROLL>(d, lp, h, c, k, io, rb * H, strip * TW, H, lane);
 }
 
 template <bool B, bool R, int V>

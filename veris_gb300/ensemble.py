@@ -25,7 +25,8 @@ from ._abi import VerisFields, VerisGrid, check
 from .state import VerisState
 
 EVP_STATE = ("uIce", "vIce", "sigma1", "sigma2", "sigma12")
-SHAPES = {0: (32, 32), 1: (16, 32), 2: (32, 16), 3: (16, 16)}
+# 0-3: shared-memory tiles (rows, columns); 4-6: register walks (rows, 28 columns)
+SHAPES = {0: (32, 32), 1: (16, 32), 2: (32, 16), 3: (16, 16), 4: (8, 28), 5: (16, 28), 6: (32, 28)}
 
 
 def prepare_dynamics(lib, grid, params, fields, v, stream):
