@@ -106,9 +106,16 @@ def max_over_ranks(x, ws):
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def replica_value(cells_per_rank, subcycles, steps, ms_max, ws):
+    """Whole-job Gcell-subcycles/s of ws independent replicas (weak scaling):
+    every rank's cells over the slowest rank's time."""
+    return ws * cells_per_rank * subcycles * steps / (ms_max / 1e3) / 1e9
 
 
 # -------------------------------------------------------------------- clocks
@@ -228,36 +235,56 @@ def cpu_sample(arrays, sett, n_sub_sample, n_sub_full):
     return full, desc
 
 
+def _reference_worker(job):
+    """One bounded sample of the oracle in a worker process (one core)."""
+    import os as _os
+    _os.environ.setdefault("OMP_NUM_THREADS", "1")
+    config, seed, n_sample, n_full = job
+    from veris_gb300.synthetic import CONFIGS, make_state, config_settings
+    c = CONFIGS[config]
+    arrays = make_state(c["nx"], c["ny"], seed=seed)
+    sett = config_settings(config)
+    cpu_sample(arrays, sett, n_sample, n_full)          # warm-up
+    return cpu_sample(arrays, sett, n_sample, n_full)
+
+
 def run_reference(args):
-    ws, rank, _ = int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")), 0
+    """The reference's CPU algorithm (the NumPy oracle) on all host cores:
+    one independent replica of the workload per core (NumPy elementwise code
+    uses one core each), every replica timing a bounded sample of a step;
+    value = all replicas' cells x subcycles over the slowest one's time."""
+    ws, rank = int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
-    from veris_gb300.synthetic import CONFIGS, make_state, config_settings
+    import multiprocessing as mp
+    from veris_gb300.synthetic import CONFIGS
     c = CONFIGS[args.config]
     n_full = args.subcycles or c["n_evp"]
-    arrays = make_state(c["nx"], c["ny"], seed=args.seed)
-    sett = config_settings(args.config)
     cells = c["nx"] * c["ny"]
     n_sample = 2
-    for _ in range(args.warmup):
-        cpu_sample(arrays, sett, n_sample, n_full)
+    cores = max(1, os.cpu_count() or 1)
+    ctx = mp.get_context("spawn")
     times = []
     desc = ""
-    for _ in range(args.steps):
-        t, desc = cpu_sample(arrays, sett, n_sample, n_full)
-        times.append(t)
+    with ctx.Pool(cores) as pool:
+        for k in range(args.warmup + args.steps):
+            res = pool.map(_reference_worker, [(args.config, args.seed + r, n_sample, n_full) for r in range(cores)])
+            if k >= args.warmup:
+                times.append(max(t for t, _d in res))
+                desc = res[0][1]
     sec = float(np.sum(times))
-    value = cells * n_full * args.steps / sec / 1e9
+    value = cores * cells * n_full * args.steps / sec / 1e9
+    sample = f"{cores} processes x ({desc})"
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "Gcell-subcycles/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": sec / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": args.config, "nx": c["nx"], "ny": c["ny"], "subcycles": n_full,
-                   "dt_s": c["dt"], "cells": cells, "parallelism": "replicas",
+                   "dt_s": c["dt"], "cells": cells, "parallelism": f"{cores} CPU replicas",
                    "l2": "n/a (CPU)"},
-        "cpu_baseline": {"value": value, "unit": "Gcell-subcycles/s", "cores": 1, "kind": "port",
-                         "sample": desc, "host_cpus": os.cpu_count()},
+        "cpu_baseline": {"value": value, "unit": "Gcell-subcycles/s", "cores": cores, "kind": "port",
+                         "sample": sample, "host_cpus": os.cpu_count()},
         "e2e": {"value": value, "unit": "Gcell-subcycles/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -328,7 +355,7 @@ def run_ours(args):
     clk = clocks.stop()
     ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
     ms = max_over_ranks(ms, ws)
-    value = ws * cells * n_sub * args.steps / (ms / 1e3) / 1e9
+    value = replica_value(cells, n_sub, args.steps, ms, ws)
     launches = eng.launches_per_step * args.steps
 
     # EVP kernel alone (eager, events around the subcycle loop on the launching stream)
