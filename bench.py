@@ -60,7 +60,7 @@ def parse():
     ap.add_argument("--f32-kernel", default="walk", choices=("tma", "walk"),
                     help="float32 EVP kernel: register-walking warps or TMA-staged tiles")
     ap.add_argument("--walk-rows", type=int, default=0, help="rows per walk (0: from the grid and the SM count)")
-    ap.add_argument("--walk-variant", type=int, default=0)
+    ap.add_argument("--walk-variant", type=int, default=-1, help="-1: tuned on the workload")
     ap.add_argument("--adjoint", action="store_true",
                     help="time a trajectory's forward + adjoint against its forward (float64)")
     ap.add_argument("--adjoint-config", default="c3_1deg")
@@ -329,7 +329,11 @@ def run_ours(args):
 
     state = VerisState.from_numpy(arrays, sett, device=dev)
     eng = SeaIceStep(state, precision=args.precision, evp=args.evp, f32_kernel=args.f32_kernel,
-                     walk_rows=args.walk_rows, walk_variant=args.walk_variant)
+                     walk_rows=args.walk_rows, walk_variant=max(0, args.walk_variant))
+    walk_tuning = None
+    if args.precision == "f32" and args.f32_kernel == "walk" and eng.evp_form == "fast" and args.walk_variant < 0:
+        from veris_gb300.autotune import tune_walk
+        walk_tuning = tune_walk(eng)
     eng.capture()
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
     for _ in range(args.warmup):
@@ -391,7 +395,8 @@ def run_ours(args):
                        "l2": "flushed before every timed step (512 MiB write)",
                        "graph": "one CUDA graph per step", "evp_form": eng.evp_form,
                        "f32_kernel": args.f32_kernel if args.precision == "f32" else None,
-                       "walk": {"rows": eng.walk_rows, "variant": eng.walk_variant}
+                       "walk": {"rows": eng.walk_rows or "auto", "variant": eng.walk_variant,
+                                "tuning": walk_tuning}
                        if args.f32_kernel == "walk" else None},
             "roofline": roofline, "gpu_launches": launches, "clocks": clk,
             "wall_s_timed_region": wall, "evp_ms_per_step": evp_ms,
@@ -422,7 +427,7 @@ def run_ours(args):
         # both precisions from the same initial state; capture() runs step 1
         st32 = VerisState.from_numpy(arrays, sett, device=dev)
         e32 = SeaIceStep(st32, precision="f32", evp=args.evp, f32_kernel=args.f32_kernel,
-                         walk_rows=args.walk_rows, walk_variant=args.walk_variant)
+                         walk_rows=args.walk_rows, walk_variant=eng.walk_variant)
         e32.capture()
         st64 = VerisState.from_numpy(arrays, sett, device=dev)
         e64 = SeaIceStep(st64, precision="f64", evp=args.evp)

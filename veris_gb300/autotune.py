@@ -1,4 +1,7 @@
-"""Launch-shape autotuner of the batched ensemble.
+"""Autotuners: the launch shape of the batched ensemble, and the compiled
+register budget of the single-domain walking EVP kernel.
+
+Ensemble: 
 
 For an ``Ensemble`` it times every candidate (tile shape x CTAs per SM) on a
 few subcycles with CUDA events, keeps the fastest and caches the choice per
@@ -84,3 +87,35 @@ def tune(ens, candidates=DEFAULT_CANDIDATES, subcycles=10, repeats=3, use_cache=
         cache[sig] = choice
         _store(cache)
     return dict(choice, trials=trials, cached=False)
+
+
+def tune_walk(eng, variants=(0, 1, 2, 3), subcycles=10, repeats=3):
+    """Pick the walking kernel's compiled register budget (variant) for a
+    float32 ``SeaIceStep`` by timing each on ``subcycles`` subcycles of the
+    engine's state (outputs go to scratch: the state is not advanced).  More
+    resident warps hide more latency but force shorter walks (all walks stay
+    in one wave), so the best budget depends on the grid."""
+    import ctypes
+    from ._abi import check
+    outs = [torch.empty(eng.shape, dtype=torch.float32, device=eng.device) for _ in range(5)]
+    ptrs = [t.data_ptr() for t in outs]
+    ws = (eng.ws_evp.data_ptr(), eng.ws_evp.numel(), eng.stream)
+    r64 = eng._refs(eng.f64)
+    trials = []
+    for v in variants:
+        run = lambda n: check("evp_walk_f32", eng.lib.veris_evp_walk_solver_f32(*r64, n, eng.walk_rows, v, *ptrs, *ws))
+        run(2)
+        times = []
+        for _ in range(repeats):
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record()
+            run(subcycles)
+            b.record()
+            b.synchronize()
+            times.append(a.elapsed_time(b) / subcycles)
+        trials.append({"variant": v, "ms_per_subcycle": sorted(times)[len(times) // 2]})
+    best = min(trials, key=lambda t: t["ms_per_subcycle"])
+    eng.walk_variant = best["variant"]
+    eng.graph = None
+    return {"variant": best["variant"], "trials": trials}

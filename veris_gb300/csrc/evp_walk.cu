@@ -13,11 +13,11 @@ struct Variant;
 template <>
 struct Variant<0> { static constexpr int UNROLL = 1, MINB = 1; };
 template <>
-struct Variant<1> { static constexpr int UNROLL = 4, MINB = 1; };
+struct Variant<1> { static constexpr int UNROLL = 1, MINB = 5; };
 template <>
 struct Variant<2> { static constexpr int UNROLL = 1, MINB = 4; };
 template <>
-struct Variant<3> { static constexpr int UNROLL = 4, MINB = 4; };
+struct Variant<3> { static constexpr int UNROLL = 1, MINB = 6; };
 constexpr int N_VARIANTS = 4;
 
 template <bool BASAL, bool TURN, int V>
