@@ -106,6 +106,19 @@ __device__ void solve4temp_multi(const VerisParams &p, const S4TIn &x, const S &
     S T[NC], k[NC], lwabs[NC];
     double d3[NC];
     bool ice[NC];
+    // penetrating shortwave factor exp(-1.5 hI): the NC = 5 categories of one
+    // cell have hI[l] = (2l+1) hI[0], so one exp and its odd powers serve all
+    S e1[NC];
+    if constexpr (NC == 5) {
+        const S E = vexp(-1.5 * hI[0]), E2 = E * E;
+        e1[0] = E;
+#pragma unroll
+        for (int l = 1; l < NC; ++l) e1[l] = e1[l - 1] * E2;
+    } else {
+#pragma unroll
+        for (int l = 0; l < NC; ++l) e1[l] = vexp(-1.5 * hI[l]);
+    }
+    const double rhCut = 1.0 / p.hCut;
 #pragma unroll
     for (int l = 0; l < NC; ++l) {
         ice[l] = hI[l] > 0;
@@ -119,10 +132,10 @@ __device__ void solve4temp_multi(const VerisParams &p, const S4TIn &x, const S &
         const bool south = ice[l] && x.fCori < 0;
         if (south) { aI = p.dryIceAlb_south; aS = p.drySnowAlb_south; }
         if (south && Tin >= SurfMeltTemp) { aI = p.wetIceAlb_south; aS = p.wetSnowAlb_south; }
-        S alb = ice[l] ? aI + hS[l] / p.hCut * (aS - aI) : S(0.0);
+        S alb = ice[l] ? aI + hS[l] * rhCut * (aS - aI) : S(0.0);
         if (hS[l] > p.hCut) alb = S(aS);
         if (hS[l] == 0) alb = S(aI);
-        S pen = ice[l] ? p.shortwave * vexp(-1.5 * hI[l]) : S(0.0);
+        S pen = ice[l] ? p.shortwave * e1[l] : S(0.0);
         if (snow) pen = S(0.0);
         oPen[l] = ice[l] ? -(1 - alb) * pen * x.SWdown : S(0.0);
         const S absSW = ice[l] ? (1 - alb) * (1 - pen) * x.SWdown : S(0.0);
