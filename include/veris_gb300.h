@@ -227,8 +227,9 @@ int veris_evp_fast_solver_f64(const VerisGrid *g, const VerisParams *p, const Ve
  * 28-column strip walks `rows` output rows (4..4096; 0: the longest walk
  * that keeps all walks in one wave of resident warps), rows in registers and
  * columns across lanes; no shared memory, no barriers.  `variant` (0..3)
- * picks the compiled register budget: 0 = free, 1 = 5, 2 = 4, 3 = 6
- * resident 4-warp CTAs per SM; same values.
+ * picks the compiled form: register budget free (0), 5 (1) or 4 (2, 3)
+ * resident 4-warp CTAs per SM, and (3) the own-point constants loaded one
+ * walk step early; same values.
  */
 int veris_evp_walk_solver_f32(const VerisGrid *g, const VerisParams *p, const VerisFieldsF64 *vs,
                               int32_t n_subcycles, int32_t rows, int32_t variant, float *uIce,

@@ -7,17 +7,18 @@ namespace veris {
 namespace walk {
 
 constexpr int WARPS = 4;    // warps per CTA
-// kernel variants: (loop unroll, CTAs per SM the register budget must allow)
+// kernel variants: (loop unroll, CTAs per SM the register budget must allow,
+// own-point constants loaded a step early)
 template <int V>
 struct Variant;
 template <>
-struct Variant<0> { static constexpr int UNROLL = 1, MINB = 1; };
+struct Variant<0> { static constexpr int UNROLL = 1, MINB = 1; static constexpr bool PRE = false; };
 template <>
-struct Variant<1> { static constexpr int UNROLL = 1, MINB = 5; };
+struct Variant<1> { static constexpr int UNROLL = 1, MINB = 5; static constexpr bool PRE = false; };
 template <>
-struct Variant<2> { static constexpr int UNROLL = 1, MINB = 4; };
+struct Variant<2> { static constexpr int UNROLL = 1, MINB = 4; static constexpr bool PRE = false; };
 template <>
-struct Variant<3> { static constexpr int UNROLL = 1, MINB = 6; };
+struct Variant<3> { static constexpr int UNROLL = 1, MINB = 4; static constexpr bool PRE = true; };
 constexpr int N_VARIANTS = 4;
 
 template <bool BASAL, bool TURN, int V>
@@ -28,7 +29,7 @@ evp_walk_kernel(Dims d, int64_t lp, HaloFill h, FastConsts<float> c, FastScalars
     const int w = blockIdx.x * WARPS + (threadIdx.x >> 5);
     if (w >= nwalks) return;   // whole warps only
     const int strip = w % nstrips, rb = w / nstrips;
-    walk_strip<BASAL, TURN, Variant<V>::UNROLL>(d, lp, h, c, k, io, rb * H, strip * TW, H, lane);
+    walk_strip<BASAL, TURN, Variant<V>::UNROLL, Variant<V>::PRE>(d, lp, h, c, k, io, rb * H, strip * TW, H, lane);
 }
 
 template <bool B, bool R, int V>

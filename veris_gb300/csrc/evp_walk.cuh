@@ -1,6 +1,6 @@
-// Register-walking float32 mEVP subcycle: the walk itself (veris/evp_solver.py:21-254, the
-// fast form's arithmetic with the TMA kernel's approximate square root and
-// division).
+// Register-walking float32 mEVP subcycle, the walk itself
+// (veris/evp_solver.py:21-254: the fast form's arithmetic with the TMA
+// kernel's approximate square root and division).
 //
 // One warp owns a strip of 28 output columns (lanes = columns j0-2 .. j0+29,
 // i.e. the strip plus a 2-cell ring) and walks down H output rows plus a
@@ -72,7 +72,8 @@ __device__ __forceinline__ void load_row(Row &r, const FastConsts<float> &c, con
 
 // One walk: the strip of output columns j0 .. j0+27 and output rows
 // i0 .. i0+H-1 of one subcycle, by the calling warp (all 32 lanes).
-template <bool BASAL, bool TURN, int UNROLL>
+// PRE: load the own-point constants one walk step before stage D uses them
+template <bool BASAL, bool TURN, int UNROLL, bool PRE = false>
 __device__ __forceinline__ void walk_strip(const Dims &d, int64_t lp, const HaloFill &h, const FastConsts<float> &c,
                                            const FastScalars<float> &k, const FastIO<float> &io, int i0, int j0,
                                            int H, int lane) {
@@ -92,18 +93,32 @@ __device__ __forceinline__ void walk_strip(const Dims &d, int64_t lp, const Halo
     float s11_a = 0.f, s11_b = 0.f, s22_a = 0.f;
     float cd_a = 0.f, cd_b = 0.f, cb_a = 0.f, cb_b = 0.f;
     float fv_a = 0.f, fv_b = 0.f, fu_a = 0.f, s12_a = 0.f;
+    float o_cU = 0.f, o_cV = 0.f, o_AW = 0.f, o_AS = 0.f, o_mU = 0.f, o_mV = 0.f, o_rrAu = 0.f, o_rrAv = 0.f;
     load_row<BASAL>(Pf, c, io, lp, d.wx(i0 - 2), gj);
     const int T = H + 4;   // rows i0-2 .. i0+H+1
-    // unrolled by the rotation period (variants 1, 3), so that the row ages
-    // are renamed registers rather than copies
+    // UNROLL = 4 (the rotation period) would rename the row ages instead of
+    // copying them; measured slower (register pressure), the kernels use 1
 #pragma unroll UNROLL
     for (int t = 0; t < T; ++t) {
         N = Pf;
         if (t + 1 < T) load_row<BASAL>(Pf, c, io, lp, d.wx(i0 - 2 + t + 1), gj);
         // own-point constants of row t-2 (stage D)
-        const int64_t ob = (int64_t)d.wx(i0 + t - 4) * lp + gj;
         float cU = 0.f, cV = 0.f, AW = 0.f, AS = 0.f, mU = 0.f, mV = 0.f, rrAu = 0.f, rrAv = 0.f;
-        if (t >= 4) {
+        if (PRE) {
+            cU = o_cU; cV = o_cV; AW = o_AW; AS = o_AS; mU = o_mU; mV = o_mV; rrAu = o_rrAu; rrAv = o_rrAv;
+            if (t >= 3) {   // row t-1, for the next step
+                const int64_t on = (int64_t)d.wx(i0 + t - 3) * lp + gj;
+                o_cU = __ldg(c.cU + on);
+                o_cV = __ldg(c.cV + on);
+                o_AW = __ldg(c.AW + on);
+                o_AS = __ldg(c.AS + on);
+                o_mU = __ldg(c.mU + on);
+                o_mV = __ldg(c.mV + on);
+                o_rrAu = __ldg(c.rrAu + on);
+                o_rrAv = __ldg(c.rrAv + on);
+            }
+        } else if (t >= 4) {
+            const int64_t ob = (int64_t)d.wx(i0 + t - 4) * lp + gj;
             cU = __ldg(c.cU + ob);
             cV = __ldg(c.cV + ob);
             AW = __ldg(c.AW + ob);
