@@ -65,6 +65,7 @@ def parse():
                     help="time a trajectory's forward + adjoint against its forward (float64)")
     ap.add_argument("--adjoint-config", default="c3_1deg")
     ap.add_argument("--adjoint-steps", type=int, default=None)
+    ap.add_argument("--adjoint-precision", default="f64", choices=("f64", "f32"))
     ap.add_argument("--snapshots", type=int, default=None, help="step snapshots (default: all)")
     ap.add_argument("--evp-checkpoint-every", type=int, default=0,
                     help="EVP subcycle checkpoint interval inside a step's adjoint (0: keep all)")
@@ -497,7 +498,7 @@ def run_adjoint(args):
     tape = {"auto": "auto", "on": True, "off": False}[args.tape]
     torch.cuda.reset_peak_memory_stats()
     tr = Trajectory(st, n_steps, snapshots=args.snapshots, evp_checkpoint_every=args.evp_checkpoint_every,
-                    tape=tape)
+                    tape=tape, precision=args.adjoint_precision)
     tr.track_norms = args.track_norms
     x0 = tr._save()
     p0 = float(sett.pStar)
@@ -549,10 +550,10 @@ def run_adjoint(args):
     t_f2, t_adj, L0, dLdP, stats = res[-1]
 
     peak = torch.cuda.max_memory_allocated() / 1e9
-    # centred difference in P*
+    # centred difference in P* (a wider step for the float32 forward)
     fd = None
     if not args.no_fd:
-        hP = 1e-6 * p0
+        hP = (1e-6 if args.adjoint_precision == "f64" else 1e-3) * p0
         Ls = []
         for pv in (p0 + hP, p0 - hP):
             tr.set_coefficients(pStar=pv)
@@ -563,7 +564,7 @@ def run_adjoint(args):
         fd = (Ls[0] - Ls[1]) / (2 * hP)
 
     line = {"metric": "trajectory (forward + adjoint) / forward time", "value": (t_f2 + t_adj) / t_fwd,
-            "unit": "x", "higher_is_better": False, "dtype": "f64", "data": "synthetic",
+            "unit": "x", "higher_is_better": False, "dtype": args.adjoint_precision, "data": "synthetic",
             "config": {"workload": name, "nx": c["nx"], "ny": c["ny"], "steps": n_steps,
                        "subcycles": int(sett.nEVPsteps), "dt_s": c["dt"],
                        "snapshots": tr.snaps, "evp_checkpoint_every": tr.K, "evp_tape": tr.tapes is not None,

@@ -309,6 +309,31 @@ int veris_evp_adjoint_taped_f64(const VerisGrid *g, const VerisParams *p, const 
                                 double *l_sigma120, const VerisFieldsF64 *lfields, double *lscalars,
                                 void *workspace, size_t workspace_bytes, veris_stream_t s);
 
+/*
+ * Float32 forms of the same: the tape holds float32 states (the
+ * shared-memory float32 kernel writes it, whose exact square root and
+ * division the adjoint kernel linearises); the adjoints of the five states
+ * are float32, those of the constants and the drag coefficients float64.
+ */
+int veris_evp_fast_tape_f32(const VerisGrid *g, const VerisParams *p, const VerisFieldsF64 *vs,
+                            int32_t n_subcycles, float *uIce, float *vIce, float *sigma1,
+                            float *sigma2, float *sigma12, float *tape, size_t tape_bytes,
+                            void *workspace, size_t workspace_bytes, veris_stream_t s);
+int veris_evp_adjoint_f32(const VerisGrid *g, const VerisParams *p, const VerisFieldsF64 *vs,
+                          int32_t n_subcycles, int32_t K, const float *l_uIce, const float *l_vIce,
+                          const float *l_sigma1, const float *l_sigma2, const float *l_sigma12,
+                          float *l_uIce0, float *l_vIce0, float *l_sigma10, float *l_sigma20,
+                          float *l_sigma120, const VerisFieldsF64 *lfields, double *lscalars,
+                          void *workspace, size_t workspace_bytes, veris_stream_t s);
+size_t veris_evp_adjoint_taped_workspace_bytes_f32(const VerisGrid *g, int32_t n_subcycles);
+int veris_evp_adjoint_taped_f32(const VerisGrid *g, const VerisParams *p, const VerisFieldsF64 *vs,
+                                int32_t n_subcycles, const float *tape, size_t tape_bytes,
+                                const float *l_uIce, const float *l_vIce, const float *l_sigma1,
+                                const float *l_sigma2, const float *l_sigma12, float *l_uIce0,
+                                float *l_vIce0, float *l_sigma10, float *l_sigma20, float *l_sigma120,
+                                const VerisFieldsF64 *lfields, double *lscalars, void *workspace,
+                                size_t workspace_bytes, veris_stream_t s);
+
 /* veris/ocean_stress.py:8-40 OceanStressUV */
 int veris_ocean_stress_uv_f64(const VerisGrid *g, const VerisParams *p,
                               const VerisFieldsF64 *vs, double *OceanStressU,

@@ -337,3 +337,51 @@ def test_trajectory_autograd_function():
     g, cg, _ = tr.backward({"uIce": W[0], "vIce": W[1], "Area": W[2]})
     assert G.rel_err(h0.grad.cpu().numpy(), g["hIceMean"].cpu().numpy()) <= 1e-12
     assert G.rel_err(A0.grad.cpu().numpy(), g["Area"].cpu().numpy()) <= 1e-12
+
+
+@pytest.mark.parametrize("tape", (True, False))
+def test_float32_trajectory_gradients(tape):
+    """The float32 trajectory (float32 EVP and advection forward, float32 EVP
+    adjoint): its gradients against the float64 ones (1e-2), and dL/dP*
+    against a centred difference of its own forward with a step large enough
+    for float32 rounding."""
+    from veris_gb300.trajectory import Trajectory, tracking_loss_adjoint
+    rng = np.random.default_rng(10)
+    st = _trajectory_state()
+    v = st.variables
+    names = ("uIce", "vIce", "sigma1", "sigma2", "sigma12", "hIceMean", "hSnowMean", "Area", "TSurf")
+    x0 = {k: getattr(v, k).clone() for k in names}
+    target = {k: (getattr(v, k) + 0.01 * _rand(rng, v.iceMask) * v.iceMask).clone() for k in ("uIce", "vIce", "Area")}
+    grads = {}
+    for prec in ("f64", "f32"):
+        for k, t in x0.items():
+            getattr(v, k).copy_(t)
+        tr = Trajectory(st, N_STEPS, n_subcycles=N_SUB, precision=prec, tape=tape)
+        tr.forward()
+        L, lam = tracking_loss_adjoint(st, target)
+        grads[prec] = tr.backward(lam)
+    g64, c64, _ = grads["f64"]
+    g32, c32, _ = grads["f32"]
+    for name in ("pStar", "airIceDrag", "waterIceDrag"):
+        a, b = float(c32[name]), float(c64[name])
+        assert abs(a - b) <= 1e-2 * max(abs(b), 1e-30), (name, a, b)
+    m = _safe_ice(v)
+    d = _rand(rng, v.iceMask) * m
+    a, b = float((g32["hIceMean"] * d).sum()), float((g64["hIceMean"] * d).sum())
+    assert abs(a - b) <= 1e-2 * max(abs(b), 1e-30), ("hIceMean", a, b)
+    # centred difference of the float32 forward in P*: this small trajectory's
+    # loss moves by ~1e-6 of itself per 1e-3 of P*, where float32 rounding
+    # of the state is ~1e-7, so the step is 1e-2 of P*
+    s = st.settings
+    p0 = s.pStar
+    hP = 1e-2 * p0
+    Ls = []
+    for pv in (p0 + hP, p0 - hP):
+        for k, t in x0.items():
+            getattr(v, k).copy_(t)
+        tr.set_coefficients(pStar=pv)
+        tr.forward()
+        Ls.append(float(tracking_loss_adjoint(st, target)[0]))
+    tr.set_coefficients(pStar=p0)
+    fd = (Ls[0] - Ls[1]) / (2 * hP)
+    assert abs(fd - float(c32["pStar"])) <= 5e-2 * max(abs(fd), 1e-30), (fd, float(c32["pStar"]))

@@ -148,6 +148,10 @@ SIGNATURES = {
     "veris_evp_fast_tape_f64": ([_G, _Pa, _F, ctypes.c_int32] + [_P] * 6 + [_S, _P, _S, _P], _I),
     "veris_evp_adjoint_taped_workspace_bytes": ([_G, ctypes.c_int32], _S),
     "veris_evp_adjoint_taped_f64": ([_G, _Pa, _F, ctypes.c_int32, _P, _S] + [_P] * 10 + [_F, _P, _P, _S, _P], _I),
+    "veris_evp_fast_tape_f32": ([_G, _Pa, _F, ctypes.c_int32] + [_P] * 6 + [_S, _P, _S, _P], _I),
+    "veris_evp_adjoint_f32": ([_G, _Pa, _F, ctypes.c_int32, ctypes.c_int32] + [_P] * 10 + [_F, _P, _P, _S, _P], _I),
+    "veris_evp_adjoint_taped_workspace_bytes_f32": ([_G, ctypes.c_int32], _S),
+    "veris_evp_adjoint_taped_f32": ([_G, _Pa, _F, ctypes.c_int32, _P, _S] + [_P] * 10 + [_F, _P, _P, _S, _P], _I),
     "veris_fill_overlap_adjoint_f64": ([_G, _Pa, _P, _P, _P], _I),
     "veris_advection_adjoint_workspace_bytes": ([_G], _S),
     "veris_advection_adjoint_f64": ([_G, _Pa, _F] + [_P] * 8 + [_P, _S, _P], _I),

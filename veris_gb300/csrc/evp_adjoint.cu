@@ -785,6 +785,33 @@ int veris_evp_adjoint_taped_f64(const VerisGrid *g, const VerisParams *p, const 
     return adj::evp_adjoint<double>(g, p, vs, n, n, lout, lin, lfields, lscalars, ws, wsb, s, tape, tape_bytes);
 }
 
+size_t veris_evp_adjoint_taped_workspace_bytes_f32(const VerisGrid *g, int32_t n) {
+    Dims d;
+    if (check_grid(g, &d) != VERIS_OK || n < 1) return 0;
+    adj::Plan<float> pl;
+    return adj::plan<float>(d, n, n, nullptr, &pl, true);
+}
+
+int veris_evp_adjoint_f32(const VerisGrid *g, const VerisParams *p, const VerisFieldsF64 *vs, int32_t n,
+                          int32_t K, const float *lu, const float *lv, const float *ls1, const float *ls2,
+                          const float *ls12, float *lu0, float *lv0, float *ls10, float *ls20, float *ls120,
+                          const VerisFieldsF64 *lfields, double *lscalars, void *ws, size_t wsb, veris_stream_t s) {
+    const float *lout[5] = {lu, lv, ls1, ls2, ls12};
+    float *lin[5] = {lu0, lv0, ls10, ls20, ls120};
+    return adj::evp_adjoint<float>(g, p, vs, n, K, lout, lin, lfields, lscalars, ws, wsb, s);
+}
+
+int veris_evp_adjoint_taped_f32(const VerisGrid *g, const VerisParams *p, const VerisFieldsF64 *vs, int32_t n,
+                                const float *tape, size_t tape_bytes, const float *lu, const float *lv,
+                                const float *ls1, const float *ls2, const float *ls12, float *lu0, float *lv0,
+                                float *ls10, float *ls20, float *ls120, const VerisFieldsF64 *lfields,
+                                double *lscalars, void *ws, size_t wsb, veris_stream_t s) {
+    VERIS_REQUIRE(tape, VERIS_ERR_ARG);
+    const float *lout[5] = {lu, lv, ls1, ls2, ls12};
+    float *lin[5] = {lu0, lv0, ls10, ls20, ls120};
+    return adj::evp_adjoint<float>(g, p, vs, n, n, lout, lin, lfields, lscalars, ws, wsb, s, tape, tape_bytes);
+}
+
 int veris_evp_adjoint_f64(const VerisGrid *g, const VerisParams *p, const VerisFieldsF64 *vs, int32_t n,
                           int32_t K, const double *lu, const double *lv, const double *ls1, const double *ls2,
                           const double *ls12, double *lu0, double *lv0, double *ls10, double *ls20,

@@ -341,6 +341,13 @@ int veris_evp_fast_tape_f64(const VerisGrid *g, const VerisParams *p, const Veri
     return evp_fast<double>(g, p, vs, n, u, v, s1, s2, s12, ws, wsb, 0, s, tape, tape_bytes);
 }
 
+int veris_evp_fast_tape_f32(const VerisGrid *g, const VerisParams *p, const VerisFieldsF64 *vs, int32_t n,
+                            float *u, float *v, float *s1, float *s2, float *s12, float *tape, size_t tape_bytes,
+                            void *ws, size_t wsb, veris_stream_t s) {
+    VERIS_REQUIRE(tape, VERIS_ERR_ARG);
+    return evp_fast<float>(g, p, vs, n, u, v, s1, s2, s12, ws, wsb, 0, s, tape, tape_bytes);
+}
+
 int veris_evp_fast_status(const void *ws, int32_t *status_host, veris_stream_t s) {
     VERIS_REQUIRE(ws && status_host, VERIS_ERR_ARG);
     cudaStream_t st = (cudaStream_t)s;

@@ -107,8 +107,8 @@ class SeaIceStep:
         self.forcing = ({n: getattr(v, n).clone() for n in HELD_FORCING} if hold_forcing else None)
         self.graph = None
         self.launches_per_step = None
-        # float64 fast form only: a buffer of veris_evp_tape_bytes() that the
-        # next eager step's EVP fills with its subcycle states
+        # fast forms: a buffer of veris_evp_tape_bytes() that the next eager
+        # step's EVP fills with its subcycle states
         self.evp_tape = None
 
     def set_settings(self, **kw):
@@ -191,7 +191,13 @@ class SeaIceStep:
                 self._to32(getattr(v, name), self.v32[name])
             n += len(conv)
             outs = [t.data_ptr() for t in self.evp_out32]
-            if self.evp_form == "fast" and self.f32_kernel == "walk":
+            if self.evp_form == "fast" and self.evp_tape is not None:
+                # float32 states of every subcycle (shared-memory kernel); eager only
+                tape = self.evp_tape
+                check("evp_tape_f32", lib.veris_evp_fast_tape_f32(*r64, self.n_sub, *outs, tape.data_ptr(),
+                                                                   tape.numel() * tape.element_size(), *ws))
+                n += self.n_sub + 1
+            elif self.evp_form == "fast" and self.f32_kernel == "walk":
                 check("evp_walk_f32", lib.veris_evp_walk_solver_f32(*r64, self.n_sub, self.walk_rows,
                                                                          self.walk_variant, *outs, *ws))
                 n += self.n_sub + 1

@@ -1,7 +1,7 @@
 """Gradients through many sea-ice steps on one GPU.
 
-``Trajectory`` runs n float64 steps of the sea-ice step (the engine's fast
-EVP form, surface forcing held fixed: Qnet and Qsw are restored before every
+``Trajectory`` runs n steps of the sea-ice step (the engine's fast EVP
+form in float64, or the engine's float32 step; surface forcing held fixed: Qnet and Qsw are restored before every
 step, since Growth overwrites them with the ocean's budgets) and propagates
 adjoints back through them with the hand-written adjoint kernels of every
 routine of the step:
@@ -73,19 +73,24 @@ class Trajectory:
     """n float64 steps from the state's current values and their adjoint."""
 
     def __init__(self, state, n_steps, n_subcycles=None, snapshots=None, evp_checkpoint_every=0, tape="auto",
-                 tape_memory_fraction=0.6):
+                 tape_memory_fraction=0.6, precision="f64"):
         """``snapshots``: step snapshot slots (None: every step).  ``tape``:
         keep every EVP subcycle state of every step during the forward, so
         the adjoint recomputes no subcycle ("auto": when every step is
         snapshotted and the tapes fit in ``tape_memory_fraction`` of the free
-        device memory)."""
+        device memory).  ``precision`` "f32": the forward is the engine's
+        float32 step (float32 EVP and advection, float64 thermodynamics) and
+        the EVP adjoint runs in float32; the other adjoints stay float64."""
+        if precision not in ("f64", "f32"):
+            raise ValueError("precision must be 'f64' or 'f32'")
+        self.precision = precision
         if state.settings.useRealFreshWaterFlux:
             raise ValueError("the step adjoint covers useRealFreshWaterFlux = False only")
         self.state = state
         self.n = int(n_steps)
         if self.n < 1:
             raise ValueError("n_steps must be >= 1")
-        self.eng = SeaIceStep(state, "f64", n_subcycles, evp="fast", hold_forcing=True)
+        self.eng = SeaIceStep(state, precision, n_subcycles, evp="fast", hold_forcing=True)
         self.lib = self.eng.lib
         self.snaps = self.n - 1 if snapshots is None else max(0, min(int(snapshots), self.n - 1))
         self.K = int(evp_checkpoint_every)
@@ -127,16 +132,25 @@ class Trajectory:
         mk = lambda nbytes: torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device=dev)
         self.ws_adv = mk(self.lib.veris_advection_adjoint_workspace_bytes(g))
         self.ws_prep = mk(self.lib.veris_prep_adjoint_workspace_bytes(g))
-        tape_bytes = int(self.lib.veris_evp_tape_bytes(g, 8, self.eng.n_sub))
+        f32 = precision == "f32"
+        esize = 4 if f32 else 8
+        tape_bytes = int(self.lib.veris_evp_tape_bytes(g, esize, self.eng.n_sub))
         if tape == "auto":
             free = torch.cuda.mem_get_info(dev)[0]
             tape = self.snaps == self.n - 1 and self.n * tape_bytes <= tape_memory_fraction * free
         elif tape and self.snaps != self.n - 1:
             raise ValueError("taping needs every step snapshotted (snapshots=None)")
-        self.tapes = ([torch.empty(tape_bytes // 8, dtype=torch.float64, device=dev) for _ in range(self.n)]
+        tdt = torch.float32 if f32 else torch.float64
+        self.tapes = ([torch.empty(tape_bytes // esize, dtype=tdt, device=dev) for _ in range(self.n)]
                       if tape else None)
-        self.ws_evp = mk(self.lib.veris_evp_adjoint_taped_workspace_bytes(g, self.eng.n_sub) if tape else
-                         self.lib.veris_evp_adjoint_workspace_bytes(g, 8, self.eng.n_sub, self.K))
+        if tape:
+            wsb = (self.lib.veris_evp_adjoint_taped_workspace_bytes_f32(g, self.eng.n_sub) if f32 else
+                   self.lib.veris_evp_adjoint_taped_workspace_bytes(g, self.eng.n_sub))
+        else:
+            wsb = self.lib.veris_evp_adjoint_workspace_bytes(g, esize, self.eng.n_sub, self.K)
+        self.ws_evp = mk(wsb)
+        # float32 EVP adjoint: its state adjoints in float32
+        self.l32 = ([torch.empty(sh, dtype=torch.float32, device=dev) for _ in range(10)] if f32 else None)
         self.snap = {}
         self.stats = {"forward_steps": 0, "recomputed_steps": 0, "adjoint_steps": 0}
         self._graph_ok = False
@@ -297,17 +311,39 @@ class Trajectory:
         for t in self.lf.values():
             t.zero_()
         self.t_lf.hIceMean, self.t_lf.Area = new["hIceMean"].data_ptr(), new["Area"].data_ptr()
-        lo_ptrs = [lam[q].data_ptr() for q in EVP_STATE]
-        li_ptrs = [new[q].data_ptr() for q in EVP_STATE]
-        if self.tapes is not None:
-            tape = self.tapes[step]
-            check("evp_adjoint_taped", lib.veris_evp_adjoint_taped_f64(
-                *base, eng.n_sub, tape.data_ptr(), tape.numel() * 8, *lo_ptrs, *li_ptrs, ctypes.byref(self.t_lf),
-                self.evp_scal.data_ptr(), self.ws_evp.data_ptr(), self.ws_evp.numel(), st))
+        if self.l32 is None:
+            lo_ptrs = [lam[q].data_ptr() for q in EVP_STATE]
+            li_ptrs = [new[q].data_ptr() for q in EVP_STATE]
+            if self.tapes is not None:
+                tape = self.tapes[step]
+                check("evp_adjoint_taped", lib.veris_evp_adjoint_taped_f64(
+                    *base, eng.n_sub, tape.data_ptr(), tape.numel() * 8, *lo_ptrs, *li_ptrs,
+                    ctypes.byref(self.t_lf), self.evp_scal.data_ptr(), self.ws_evp.data_ptr(), self.ws_evp.numel(),
+                    st))
+            else:
+                check("evp_adjoint", lib.veris_evp_adjoint_f64(
+                    *base, eng.n_sub, self.K, *lo_ptrs, *li_ptrs, ctypes.byref(self.t_lf),
+                    self.evp_scal.data_ptr(), self.ws_evp.data_ptr(), self.ws_evp.numel(), st))
         else:
-            check("evp_adjoint", lib.veris_evp_adjoint_f64(
-                *base, eng.n_sub, self.K, *lo_ptrs, *li_ptrs, ctypes.byref(self.t_lf), self.evp_scal.data_ptr(),
-                self.ws_evp.data_ptr(), self.ws_evp.numel(), st))
+            lo32, li32 = self.l32[:5], self.l32[5:]
+            for q, name in enumerate(EVP_STATE):
+                check("convert", lib.veris_convert_f64_to_f32(lam[name].data_ptr(), lo32[q].data_ptr(),
+                                                              lo32[q].numel(), st))
+            lo_ptrs = [t.data_ptr() for t in lo32]
+            li_ptrs = [t.data_ptr() for t in li32]
+            if self.tapes is not None:
+                tape = self.tapes[step]
+                check("evp_adjoint_taped_f32", lib.veris_evp_adjoint_taped_f32(
+                    *base, eng.n_sub, tape.data_ptr(), tape.numel() * 4, *lo_ptrs, *li_ptrs,
+                    ctypes.byref(self.t_lf), self.evp_scal.data_ptr(), self.ws_evp.data_ptr(), self.ws_evp.numel(),
+                    st))
+            else:
+                check("evp_adjoint_f32", lib.veris_evp_adjoint_f32(
+                    *base, eng.n_sub, self.K, *lo_ptrs, *li_ptrs, ctypes.byref(self.t_lf),
+                    self.evp_scal.data_ptr(), self.ws_evp.data_ptr(), self.ws_evp.numel(), st))
+            for q, name in enumerate(EVP_STATE):
+                check("convert", lib.veris_convert_f32_to_f64(li32[q].data_ptr(), new[name].data_ptr(),
+                                                              li32[q].numel(), st))
         self.lscal[3:5] += self.evp_scal
         self.ocean_grad["uOcean"] += self.lf["uOcean"]
         self.ocean_grad["vOcean"] += self.lf["vOcean"]
