@@ -20,8 +20,10 @@ struct Fields {
 static_assert(sizeof(Fields<double>) == sizeof(VerisFieldsF64), "field table layout");
 static_assert(sizeof(Fields<float>) == sizeof(VerisFieldsF32), "field table layout");
 
-// Extent and pitch of the padded 2-D arrays; wrap() maps an index one or a
-// few cells outside [0, n) back inside, which is the reference's roll.
+// Extent and pitch of the padded 2-D arrays.  wx()/wy() map an index at
+// most one period outside [0, n) back inside, which is the reference's roll
+// for stencils reaching a few cells; wxa()/wya() wrap any index, for tiles
+// or walks whose ring reaches past the far edge of a small grid.
 struct Dims {
     int NX, NY;   // padded sizes
     int nx, ny;   // interior sizes
@@ -32,6 +34,19 @@ struct Dims {
     __host__ __device__ __forceinline__ int wy(int j) const {
         return j < 0 ? j + NY : (j >= NY ? j - NY : j);
     }
+    __host__ __device__ __forceinline__ int wxa(int i) const {
+        while (i < 0) i += NX;
+        while (i >= NX) i -= NX;
+        return i;
+    }
+    __host__ __device__ __forceinline__ int wya(int j) const {
+        while (j < 0) j += NY;
+        while (j >= NY) j -= NY;
+        return j;
+    }
+    // for tiles: indices in [-2, n + 33]; one period suffices when n > 33
+    __host__ __device__ __forceinline__ int wxt(int i) const { return NX > 33 ? wx(i) : wxa(i); }
+    __host__ __device__ __forceinline__ int wyt(int j) const { return NY > 33 ? wy(j) : wya(j); }
     __host__ __device__ __forceinline__ int64_t at(int i, int j) const {
         return (int64_t)wx(i) * ld + wy(j);
     }

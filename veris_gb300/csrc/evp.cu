@@ -80,6 +80,7 @@ evp_subcycle_kernel(Ctx<T> c, HaloFill h, EvpIO<T> io) {
     for (int idx = tid; idx < S::NZ; idx += EVP_THREADS) {
         const int li = idx / S::WZ - 1, lj = idx % S::WZ - 1;
         const int gi = i0 + li, gj = j0 + lj;
+        if (gi >= d.NX + 2 || gj >= d.NY + 2) continue;   // feeds no stored point; keeps the wrap within one period
         const T e = strain_z(c, io.u, io.v, gi, gj);
         e12s[idx] = e;
         zqs[idx] = c.ld(f.rAz, gi, gj) * (e * e);
@@ -92,6 +93,7 @@ evp_subcycle_kernel(Ctx<T> c, HaloFill h, EvpIO<T> io) {
     for (int idx = tid; idx < S::NB; idx += EVP_THREADS) {
         const int li = idx / S::WB - 1, lj = idx % S::WB - 1;
         const int gi = i0 + li, gj = j0 + lj;
+        if (gi >= d.NX + 2 || gj >= d.NY + 2) continue;   // feeds no stored point; keeps the wrap within one period
         T e11, e22;
         strain_c(c, io.u, io.v, gi, gj, e11, e22);
         T zt, et, pr, dl;
@@ -135,6 +137,7 @@ evp_subcycle_kernel(Ctx<T> c, HaloFill h, EvpIO<T> io) {
     for (int idx = tid; idx < S::NC; idx += EVP_THREADS) {
         const int li = idx / S::WC, lj = idx % S::WC;
         const int gi = i0 + li, gj = j0 + lj;
+        if (gi >= d.NX + 2 || gj >= d.NY + 2) continue;   // feeds no stored point; keeps the wrap within one period
         const T zz = c2z_norm(c, gi, gj, true) *
                      ((zeta[ZB(li, lj)] + zeta[ZB(li - 1, lj)]) + (zeta[ZB(li, lj - 1)] + zeta[ZB(li - 1, lj - 1)]));
         T aZ = alpha, d2 = rdenom;

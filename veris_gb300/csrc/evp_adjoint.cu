@@ -104,7 +104,7 @@ evp_adjoint_kernel(Dims d, int64_t lp, HaloFill h, FastConsts<T> c, FastScalars<
     // ---- stage inputs, clear accumulators
     for (int idx = tid; idx < RS::n(); idx += THREADS) {
         const int li = idx / RS::W + RS::r0, lj = idx % RS::W + RS::c0;
-        const int64_t o = (int64_t)d.wx(i0 + li) * lp + d.wy(j0 + lj);
+        const int64_t o = (int64_t)d.wxt(i0 + li) * lp + d.wyt(j0 + lj);
         sU[idx] = io.u[o];
         sV[idx] = io.v[o];
         sUo[idx] = c.uOc[o];
@@ -123,7 +123,7 @@ evp_adjoint_kernel(Dims d, int64_t lp, HaloFill h, FastConsts<T> c, FastScalars<
     // ---- forward A: e12 at Z
     for (int idx = tid; idx < RZ::n(); idx += THREADS) {
         const int li = idx / RZ::W + RZ::r0, lj = idx % RZ::W + RZ::c0;
-        const int gi = d.wx(i0 + li), gj = d.wy(j0 + lj);
+        const int gi = d.wxt(i0 + li), gj = d.wyt(j0 + lj);
         const uint32_t f0 = sF[XS(li, lj)], fw = sF[XS(li - 1, lj)], fs = sF[XS(li, lj - 1)],
                        fws = sF[XS(li - 1, lj - 1)];
         const T mzh = (f0 & fw & fs & fws & F_MC) ? T(0.5) : T(0);
@@ -139,7 +139,7 @@ evp_adjoint_kernel(Dims d, int64_t lp, HaloFill h, FastConsts<T> c, FastScalars<
     // ---- forward B: Delta, zeta at C [-1, TI] x [-1, TJ]; drag on [-1, TI) x [-1, TJ)
     for (int idx = tid; idx < RB::n(); idx += THREADS) {
         const int li = idx / RB::W + RB::r0, lj = idx % RB::W + RB::c0;
-        const int gi = d.wx(i0 + li), gj = d.wy(j0 + lj);
+        const int gi = d.wxt(i0 + li), gj = d.wyt(j0 + lj);
         const int64_t o = (int64_t)gi * lp + gj;
         const uint32_t f0 = sF[XS(li, lj)];
         const T mInC = one_if<T>(f0, F_INC);
@@ -148,7 +148,7 @@ evp_adjoint_kernel(Dims d, int64_t lp, HaloFill h, FastConsts<T> c, FastScalars<
         const T e22 = (vn - v0) * c.rdyV_y[gj] * mInC;
         auto zq = [&](int a_, int b_) {
             const T e = sE12[RZ::at(a_, b_)];
-            return c.rAz[(int64_t)d.wx(i0 + a_) * lp + d.wy(j0 + b_)] * (e * e);
+            return c.rAz[(int64_t)d.wxt(i0 + a_) * lp + d.wyt(j0 + b_)] * (e * e);
         };
         const T e12c = c.qrA[o] * ((zq(li, lj) + zq(li + 1, lj)) + (zq(li, lj + 1) + zq(li + 1, lj + 1)));
         const T ep = e11 + e22, em = e11 - e22;
@@ -335,7 +335,7 @@ evp_adjoint_kernel(Dims d, int64_t lp, HaloFill h, FastConsts<T> c, FastScalars<
         const int li = idx / RZ2::W + RZ2::r0, lj = idx % RZ2::W + RZ2::c0;
         const T ls = lS12[idx];
         if (ls == T(0)) continue;
-        const int gi = d.wx(i0 + li), gj = d.wy(j0 + lj);
+        const int gi = d.wxt(i0 + li), gj = d.wyt(j0 + lj);
         atomic_add(&io.os12[(int64_t)gi * lp + gj], k.alpha_m1 * k.ralpha * ls);
         const int n = ((sF[XS(li, lj)] & F_MC) ? 1 : 0) + ((sF[XS(li - 1, lj)] & F_MC) ? 1 : 0) +
                       ((sF[XS(li, lj - 1)] & F_MC) ? 1 : 0) + ((sF[XS(li - 1, lj - 1)] & F_MC) ? 1 : 0);
@@ -356,7 +356,7 @@ evp_adjoint_kernel(Dims d, int64_t lp, HaloFill h, FastConsts<T> c, FastScalars<
     double dragN = 0.0, dragS = 0.0;
     for (int idx = tid; idx < RB::n(); idx += THREADS) {
         const int li = idx / RB::W + RB::r0, lj = idx % RB::W + RB::c0;
-        const int gi = d.wx(i0 + li), gj = d.wy(j0 + lj);
+        const int gi = d.wxt(i0 + li), gj = d.wyt(j0 + lj);
         const int64_t o = (int64_t)gi * lp + gj;
         const uint32_t f0 = sF[XS(li, lj)];
         const T mInC = one_if<T>(f0, F_INC), mC = one_if<T>(f0, F_MC);
@@ -443,7 +443,7 @@ evp_adjoint_kernel(Dims d, int64_t lp, HaloFill h, FastConsts<T> c, FastScalars<
             const T le12c = T(4) * k.rsq * lD * c.qrA[o];
             auto put = [&](int a_, int b_) {
                 const T e = sE12[RZ::at(a_, b_)];
-                const T rz = c.rAz[(int64_t)d.wx(i0 + a_) * lp + d.wy(j0 + b_)];
+                const T rz = c.rAz[(int64_t)d.wxt(i0 + a_) * lp + d.wyt(j0 + b_)];
                 atomic_add(&lE12[RZ::at(a_, b_)], le12c * rz * T(2) * e);
             };
             put(li, lj);
@@ -476,7 +476,7 @@ evp_adjoint_kernel(Dims d, int64_t lp, HaloFill h, FastConsts<T> c, FastScalars<
         const T le = lE12[idx];
         if (le == T(0)) continue;
         const int li = idx / RZ::W + RZ::r0, lj = idx % RZ::W + RZ::c0;
-        const int gi = d.wx(i0 + li), gj = d.wy(j0 + lj);
+        const int gi = d.wxt(i0 + li), gj = d.wyt(j0 + lj);
         const uint32_t f0 = sF[XS(li, lj)], fw = sF[XS(li - 1, lj)], fs = sF[XS(li, lj - 1)],
                        fws = sF[XS(li - 1, lj - 1)];
         const T mzh = (f0 & fw & fs & fws & F_MC) ? T(0.5) : T(0);
@@ -493,7 +493,7 @@ evp_adjoint_kernel(Dims d, int64_t lp, HaloFill h, FastConsts<T> c, FastScalars<
     // ---- flush u, v, ocean-velocity adjoints of the staged region
     for (int idx = tid; idx < RS::n(); idx += THREADS) {
         const int li = idx / RS::W + RS::r0, lj = idx % RS::W + RS::c0;
-        const int64_t o = (int64_t)d.wx(i0 + li) * lp + d.wy(j0 + lj);
+        const int64_t o = (int64_t)d.wxt(i0 + li) * lp + d.wyt(j0 + lj);
         if (lU[idx] != T(0)) atomic_add(&io.ou[o], lU[idx]);
         if (lV[idx] != T(0)) atomic_add(&io.ov[o], lV[idx]);
         if (lUo[idx] != T(0)) atomic_add(&a.uOc[o], lUo[idx]);

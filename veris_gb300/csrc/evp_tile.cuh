@@ -57,7 +57,7 @@ __device__ __forceinline__ void fast_tile(unsigned char *smem_raw, const Dims &d
     // ---- stage inputs (tile + 2-cell ring, periodic wrap over the padded array)
     for (int idx = tid; idx < S::NS; idx += FAST_THREADS) {
         const int li = idx / S::WS - 2, lj = idx % S::WS - 2;
-        const int64_t o = (int64_t)d.wx(i0 + li) * lp + d.wy(j0 + lj);
+        const int64_t o = (int64_t)d.wxt(i0 + li) * lp + d.wyt(j0 + lj);
         sU[idx] = __ldg(io.u + o);
         sV[idx] = __ldg(io.v + o);
         sUo[idx] = __ldg(c.uOc + o);
@@ -69,7 +69,7 @@ __device__ __forceinline__ void fast_tile(unsigned char *smem_raw, const Dims &d
     // ---- A: e12 at Z points [-1, TI+1] x [-1, TJ+1]
     for (int idx = tid; idx < S::NZ; idx += FAST_THREADS) {
         const int li = idx / S::WZ - 1, lj = idx % S::WZ - 1;
-        const int gi = d.wx(i0 + li), gj = d.wy(j0 + lj);
+        const int gi = d.wxt(i0 + li), gj = d.wyt(j0 + lj);
         const uint32_t f0 = sF[IS(li, lj)], fw = sF[IS(li - 1, lj)], fs = sF[IS(li, lj - 1)],
                        fws = sF[IS(li - 1, lj - 1)];
         const T mzh = (f0 & fw & fs & fws & F_MC) ? T(0.5) : T(0);
@@ -87,7 +87,7 @@ __device__ __forceinline__ void fast_tile(unsigned char *smem_raw, const Dims &d
     // ---- B: viscosities at C [-1, TI] x [-1, TJ]; stresses, drag, Coriolis on [-1, TI) x [-1, TJ)
     for (int idx = tid; idx < S::NB; idx += FAST_THREADS) {
         const int li = idx / S::WB - 1, lj = idx % S::WB - 1;
-        const int gi = d.wx(i0 + li), gj = d.wy(j0 + lj);
+        const int gi = d.wxt(i0 + li), gj = d.wyt(j0 + lj);
         const int64_t o = (int64_t)gi * lp + gj;
         const uint32_t f0 = sF[IS(li, lj)];
         const T mInC = one_if<T>(f0, F_INC);
@@ -140,7 +140,7 @@ __device__ __forceinline__ void fast_tile(unsigned char *smem_raw, const Dims &d
     // ---- C: sigma12 at Z [0, TI] x [0, TJ] (sZq is dead: reuse it)
     for (int idx = tid; idx < S::NC; idx += FAST_THREADS) {
         const int li = idx / S::WC, lj = idx % S::WC;
-        const int gi = d.wx(i0 + li), gj = d.wy(j0 + lj);
+        const int gi = d.wxt(i0 + li), gj = d.wyt(j0 + lj);
         const int n = ((sF[IS(li, lj)] & F_MC) ? 1 : 0) + ((sF[IS(li - 1, lj)] & F_MC) ? 1 : 0) +
                       ((sF[IS(li, lj - 1)] & F_MC) ? 1 : 0) + ((sF[IS(li - 1, lj - 1)] & F_MC) ? 1 : 0);
         const T norm = n == 0 ? T(0) : (n == 1 ? T(1) : (n == 2 ? T(0.5) : (n == 3 ? T(1) / T(3) : T(0.25))));

@@ -479,6 +479,9 @@ int evp_tma_subcycles(const Dims &d, const HaloFill &h, const FastConsts<float> 
                       float *const state[2][5], float *const outs[5], int64_t ldo, int n, int *status, bool basal,
                       bool turn, cudaStream_t st) {
     using namespace tma;
+    // the tiles' rings wrap within one period only on grids wider than a tile
+    // plus its ring: smaller grids take the shared-memory form
+    if (d.NX < SR + 2 || d.NY < SR + 2) return VERIS_ERR_UNSUPPORTED;
     const int64_t lp = internal_pitch(d.NY);
     Maps maps;
     bool ok = true;

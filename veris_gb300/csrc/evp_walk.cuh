@@ -78,7 +78,7 @@ __device__ __forceinline__ void walk_strip(const Dims &d, int64_t lp, const Halo
                                            const FastScalars<float> &k, const FastIO<float> &io, int i0, int j0,
                                            int H, int lane) {
     const int jl = j0 - 2 + lane;   // this lane's column (may lie outside [0, NY): wraps)
-    const int gj = d.wy(jl);
+    const int gj = d.wya(jl);
     const float rdyU = __ldg(c.rdyU_y + gj), rdyV = __ldg(c.rdyV_y + gj);
     const float dyV = __ldg(c.dyV_y + gj), dyU = __ldg(c.dyU_y + gj);
     const bool own_j = lane >= 2 && lane < 2 + TW && jl < d.NY;
@@ -94,20 +94,25 @@ __device__ __forceinline__ void walk_strip(const Dims &d, int64_t lp, const Halo
     float cd_a = 0.f, cd_b = 0.f, cb_a = 0.f, cb_b = 0.f;
     float fv_a = 0.f, fv_b = 0.f, fu_a = 0.f, s12_a = 0.f;
     float o_cU = 0.f, o_cV = 0.f, o_AW = 0.f, o_AS = 0.f, o_mU = 0.f, o_mV = 0.f, o_rrAu = 0.f, o_rrAv = 0.f;
-    load_row<BASAL>(Pf, c, io, lp, d.wx(i0 - 2), gj);
+    // row indices advance by one per step: wrapped incrementally (any walk length)
+    int gnext = d.wxa(i0 - 2);   // row of the next prefetch
+    int gown = d.wxa(i0 - 4);    // row of this step's own-point constants (row t-2)
+    load_row<BASAL>(Pf, c, io, lp, gnext, gj);
     const int T = H + 4;   // rows i0-2 .. i0+H+1
     // UNROLL = 4 (the rotation period) would rename the row ages instead of
     // copying them; measured slower (register pressure), the kernels use 1
 #pragma unroll UNROLL
     for (int t = 0; t < T; ++t) {
         N = Pf;
-        if (t + 1 < T) load_row<BASAL>(Pf, c, io, lp, d.wx(i0 - 2 + t + 1), gj);
+        gnext = gnext + 1 == d.NX ? 0 : gnext + 1;
+        if (t + 1 < T) load_row<BASAL>(Pf, c, io, lp, gnext, gj);
         // own-point constants of row t-2 (stage D)
         float cU = 0.f, cV = 0.f, AW = 0.f, AS = 0.f, mU = 0.f, mV = 0.f, rrAu = 0.f, rrAv = 0.f;
         if (PRE) {
             cU = o_cU; cV = o_cV; AW = o_AW; AS = o_AS; mU = o_mU; mV = o_mV; rrAu = o_rrAu; rrAv = o_rrAv;
             if (t >= 3) {   // row t-1, for the next step
-                const int64_t on = (int64_t)d.wx(i0 + t - 3) * lp + gj;
+                const int gn = gown + 1 == d.NX ? 0 : gown + 1;
+                const int64_t on = (int64_t)gn * lp + gj;
                 o_cU = __ldg(c.cU + on);
                 o_cV = __ldg(c.cV + on);
                 o_AW = __ldg(c.AW + on);
@@ -118,7 +123,7 @@ __device__ __forceinline__ void walk_strip(const Dims &d, int64_t lp, const Halo
                 o_rrAv = __ldg(c.rrAv + on);
             }
         } else if (t >= 4) {
-            const int64_t ob = (int64_t)d.wx(i0 + t - 4) * lp + gj;
+            const int64_t ob = (int64_t)gown * lp + gj;
             cU = __ldg(c.cU + ob);
             cV = __ldg(c.cV + ob);
             AW = __ldg(c.AW + ob);
@@ -257,6 +262,7 @@ __device__ __forceinline__ void walk_strip(const Dims &d, int64_t lp, const Halo
         fv_a = fv_new;
         fu_a = fu_new;
         s12_a = s12_new;
+        gown = gown + 1 == d.NX ? 0 : gown + 1;
     }
 }
 
