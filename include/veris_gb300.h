@@ -310,10 +310,11 @@ int veris_evp_adjoint_taped_f64(const VerisGrid *g, const VerisParams *p, const 
                                 void *workspace, size_t workspace_bytes, veris_stream_t s);
 
 /*
- * Float32 forms of the same: the tape holds float32 states (the
- * shared-memory float32 kernel writes it, whose exact square root and
- * division the adjoint kernel linearises); the adjoints of the five states
- * are float32, those of the constants and the drag coefficients float64.
+ * Float32 forms of the same: the tape holds float32 states written by the
+ * register-walking float32 kernel (the engine's float32 forward); the
+ * adjoint kernel linearises the fast form with exact square root and
+ * division at those states.  The adjoints of the five states are float32,
+ * those of the constants and the drag coefficients float64.
  */
 int veris_evp_fast_tape_f32(const VerisGrid *g, const VerisParams *p, const VerisFieldsF64 *vs,
                             int32_t n_subcycles, float *uIce, float *vIce, float *sigma1,

@@ -27,7 +27,7 @@ namespace veris {
 
 namespace adj {
 
-constexpr int TI = 16, TJ = 32, THREADS = 256;
+constexpr int TJ = 32, THREADS = 256;   // tile columns and threads; rows TI per instantiation
 
 template <class T>
 struct Adj {
@@ -52,25 +52,35 @@ struct Region {
     __host__ __device__ static constexpr int n() { return H * W; }
     __device__ static __forceinline__ int at(int li, int lj) { return (li - r0) * W + (lj - c0); }
 };
-using RS = Region<-2, -2, TI + 4, TJ + 4>;   // staged inputs and the u/v adjoint accumulators
-using RZ = Region<-1, -1, TI + 3, TJ + 3>;   // e12 and its adjoint
-using RB = Region<-1, -1, TI + 2, TJ + 2>;   // zeta, Delta and the zeta adjoint
-using RC = Region<-1, -1, TI + 1, TJ + 1>;   // drag coefficients, C-point adjoints
-using RZ2 = Region<0, 0, TI + 1, TJ + 1>;    // sigma12' adjoint
+// a TI x TJ tile's regions
+template <int TI>
+struct Geo {
+    using RS = Region<-2, -2, TI + 4, TJ + 4>;   // staged inputs and the u/v adjoint accumulators
+    using RZ = Region<-1, -1, TI + 3, TJ + 3>;   // e12 and its adjoint
+    using RB = Region<-1, -1, TI + 2, TJ + 2>;   // zeta, Delta and the zeta adjoint
+    using RC = Region<-1, -1, TI + 1, TJ + 1>;   // drag coefficients, C-point adjoints
+    using RZ2 = Region<0, 0, TI + 1, TJ + 1>;    // sigma12' adjoint
+};
 
-template <class T>
+template <class T, int TI>
 struct Smem {
-    static constexpr int NT = 8 * RS::n() + 2 * RZ::n() + 3 * RB::n() + 8 * RC::n() + RZ2::n();
-    static constexpr size_t bytes() { return sizeof(T) * (size_t)NT + sizeof(uint32_t) * RS::n(); }
+    using G = Geo<TI>;
+    static constexpr int NT = 8 * G::RS::n() + 2 * G::RZ::n() + 3 * G::RB::n() + 8 * G::RC::n() + G::RZ2::n();
+    static constexpr size_t bytes() { return sizeof(T) * (size_t)NT + sizeof(uint32_t) * G::RS::n(); }
 };
 
 __device__ __forceinline__ double atomic_add(double *a, double v) { return atomicAdd(a, v); }
 __device__ __forceinline__ float atomic_add(float *a, float v) { return atomicAdd(a, v); }
 
-template <class T, bool BASAL, bool TURN>
+template <class T, bool BASAL, bool TURN, int TI>
 __global__ void __launch_bounds__(THREADS)
 evp_adjoint_kernel(Dims d, int64_t lp, HaloFill h, FastConsts<T> c, FastScalars<T> k, Io<T> io, Adj<T> a,
                    T rhoSea) {
+    using RS = typename Geo<TI>::RS;
+    using RZ = typename Geo<TI>::RZ;
+    using RB = typename Geo<TI>::RB;
+    using RC = typename Geo<TI>::RC;
+    using RZ2 = typename Geo<TI>::RZ2;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T *p = reinterpret_cast<T *>(smem_raw);
     T *sU = p; p += RS::n();
@@ -553,11 +563,11 @@ __global__ void scale_kernel(T *x, int64_t n, T s) {
         x[k] *= s;
 }
 
-template <class T, bool B, bool R>
-static int launch_adj(const Dims &d, int64_t lp, const HaloFill &h, const FastConsts<T> &c, const FastScalars<T> &k,
-                      const Io<T> &io, const Adj<T> &a, T rhoSea, cudaStream_t st) {
-    auto kern = evp_adjoint_kernel<T, B, R>;
-    const size_t sm = Smem<T>::bytes();
+template <class T, bool B, bool R, int TI>
+static int launch_adj_ti(const Dims &d, int64_t lp, const HaloFill &h, const FastConsts<T> &c,
+                         const FastScalars<T> &k, const Io<T> &io, const Adj<T> &a, T rhoSea, cudaStream_t st) {
+    auto kern = evp_adjoint_kernel<T, B, R, TI>;
+    const size_t sm = Smem<T, TI>::bytes();
     static bool configured = false;
     if (!configured) {
         if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess)
@@ -567,6 +577,25 @@ static int launch_adj(const Dims &d, int64_t lp, const HaloFill &h, const FastCo
     dim3 grid((d.NY + TJ - 1) / TJ, (d.NX + TI - 1) / TI);
     kern<<<grid, THREADS, sm, st>>>(d, lp, h, c, k, io, a, rhoSea);
     return launch_status();
+}
+
+// tile rows: 8 while 16-row tiles would leave SMs idle (fewer than two
+// tiles per SM), else 16 (less recomputed ring per cell)
+template <class T, bool B, bool R>
+static int launch_adj(const Dims &d, int64_t lp, const HaloFill &h, const FastConsts<T> &c, const FastScalars<T> &k,
+                      const Io<T> &io, const Adj<T> &a, T rhoSea, cudaStream_t st) {
+    static int sms = 0;
+    if (sms == 0) {
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) !=
+                                                      cudaSuccess) {
+            cudaGetLastError();
+            sms = 152;
+        }
+    }
+    const long tiles16 = (long)((d.NY + TJ - 1) / TJ) * ((d.NX + 15) / 16);
+    if (tiles16 < 2L * sms) return launch_adj_ti<T, B, R, 8>(d, lp, h, c, k, io, a, rhoSea, st);
+    return launch_adj_ti<T, B, R, 16>(d, lp, h, c, k, io, a, rhoSea, st);
 }
 
 // workspace: [fast layout][11 constant adjoints][2 scalars]

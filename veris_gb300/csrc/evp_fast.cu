@@ -229,9 +229,25 @@ static int evp_fast(const VerisGrid *g, const VerisParams *p, const VerisFieldsF
     T *outs[5] = {uo, vo, s1o, s2o, s12o};
     if (tape) {
         for (int it = 0; it < n; ++it) {
-            FastIO<T> io{tslot(it, 0), tslot(it, 1), tslot(it, 2), tslot(it, 3), tslot(it, 4),
-                         tslot(it + 1, 0), tslot(it + 1, 1), tslot(it + 1, 2), tslot(it + 1, 3), tslot(it + 1, 4), lp};
-            if ((stt = fast_subcycle<T>(d, h, c, k, io, basal, turn, st)) != VERIS_OK) return stt;
+            bool done = false;
+            if constexpr (sizeof(T) == 4) {
+                if (allow_tma >= 4 || allow_tma < 0) {   // float32 tape written by the register-walking kernel
+                    float *const from[2][5] = {{tslot(it, 0), tslot(it, 1), tslot(it, 2), tslot(it, 3), tslot(it, 4)},
+                                               {nullptr, nullptr, nullptr, nullptr, nullptr}};
+                    float *const to[5] = {tslot(it + 1, 0), tslot(it + 1, 1), tslot(it + 1, 2), tslot(it + 1, 3),
+                                          tslot(it + 1, 4)};
+                    if ((stt = evp_walk_subcycles(d, h, c, k, from, to, lp, 1, basal, turn,
+                                                  allow_tma < 0 ? 0 : allow_tma, walk_variant, st)) != VERIS_OK)
+                        return stt;
+                    done = true;
+                }
+            }
+            if (!done) {
+                FastIO<T> io{tslot(it, 0), tslot(it, 1), tslot(it, 2), tslot(it, 3), tslot(it, 4),
+                             tslot(it + 1, 0), tslot(it + 1, 1), tslot(it + 1, 2), tslot(it + 1, 3), tslot(it + 1, 4),
+                             lp};
+                if ((stt = fast_subcycle<T>(d, h, c, k, io, basal, turn, st)) != VERIS_OK) return stt;
+            }
         }
         for (int q = 0; q < 5; ++q)
             if (cudaMemcpy2DAsync(outs[q], d.ld * sizeof(T), tslot(n, q), lp * sizeof(T), d.NY * sizeof(T), d.NX,
@@ -345,7 +361,7 @@ int veris_evp_fast_tape_f32(const VerisGrid *g, const VerisParams *p, const Veri
                             float *u, float *v, float *s1, float *s2, float *s12, float *tape, size_t tape_bytes,
                             void *ws, size_t wsb, veris_stream_t s) {
     VERIS_REQUIRE(tape, VERIS_ERR_ARG);
-    return evp_fast<float>(g, p, vs, n, u, v, s1, s2, s12, ws, wsb, 0, s, tape, tape_bytes);
+    return evp_fast<float>(g, p, vs, n, u, v, s1, s2, s12, ws, wsb, -1, s, tape, tape_bytes);   // walking kernel
 }
 
 int veris_evp_fast_status(const void *ws, int32_t *status_host, veris_stream_t s) {

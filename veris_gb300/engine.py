@@ -192,7 +192,7 @@ class SeaIceStep:
             n += len(conv)
             outs = [t.data_ptr() for t in self.evp_out32]
             if self.evp_form == "fast" and self.evp_tape is not None:
-                # float32 states of every subcycle (shared-memory kernel); eager only
+                # float32 states of every subcycle (register-walking kernel); eager only
                 tape = self.evp_tape
                 check("evp_tape_f32", lib.veris_evp_fast_tape_f32(*r64, self.n_sub, *outs, tape.data_ptr(),
                                                                    tape.numel() * tape.element_size(), *ws))
