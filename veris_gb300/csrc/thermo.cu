@@ -155,7 +155,7 @@ __device__ void solve4temp_multi(const VerisParams &p, const S4TIn &x, const S &
     // in float64 arithmetic it and the step use float32 reciprocals (the
     // iteration still converges to the float64 root); dual numbers keep the
     // exact step so that the adjoint differentiates a smooth map.  A
-    // category stops once an update moves T by less than 4e-9 T.
+    // category stops once an update moves T by less than 4e-7 T.
     const double aa1l2 = aa1 * 3.32192809488736234787;   // aa1 log2(10)
     const double qnum = bb1 * cc0, qsub = one_m_bb1 * cc0;
     auto fluxes = [&](bool newton) {
@@ -185,11 +185,12 @@ __device__ void solve4temp_multi(const VerisParams &p, const S4TIn &x, const S &
                 }
                 Tn = smin(Tn, S(Tmelt));
                 Tn = smax(Tn, S(Tmin));
-                // |update| <= 4e-9 T (about 1e-6 K): the error left is below
+                // |update| <= 4e-7 T (about 1e-4 K): the error left is below
                 // 1e-7 of the update (float32 derivative) plus C update^2 with
-                // C = F''/2F' ~ 1e-3 / K, i.e. ~1e-13 K, far inside the float64
-                // parity of the fixed six iterations
-                if (vfabs(val(Tn) - val(t1)) <= 4e-9 * val(t1)) moving[l] = false;
+                // C = F''/2F' ~ 1e-3 / K (at most ~1e-2 / K with the latent
+                // heat term), i.e. ~1e-10 K, 4e-13 of T: far inside the
+                // float64 parity of the fixed six iterations
+                if (vfabs(val(Tn) - val(t1)) <= 4e-7 * val(t1)) moving[l] = false;
                 T[l] = Tn;
             }
         }
