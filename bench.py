@@ -54,6 +54,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true", help="skip the float64 comparison leg")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-routines", action="store_true",
+                    help="skip the free-drift, bulk-formula and residual measurements")
     ap.add_argument("--subcycles", type=int, default=None, help="override the workload's subcycles")
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--evp", default="auto", choices=("auto", "fast", "plain"))
@@ -456,6 +458,9 @@ def run_ours(args):
         line["fp32_error_vs_fp64"] = {"after_1_step": errs1, "steps": n_cmp, "fields": errs,
                                       "definition": "max_rel = max|a-b| / max|b|, rms_rel = rms(a-b) / max|b|"}
 
+    if not args.no_routines:
+        line["routines"] = measure_routines(arrays, sett, dev, flush)
+
     if rank == 0 and not args.no_cpu_baseline:
         sec, desc = cpu_sample(arrays, sett, 2, n_sub)
         line["cpu_baseline"] = {"value": cells * n_sub / sec / 1e9, "unit": "Gcell-subcycles/s",
@@ -465,6 +470,83 @@ def run_ours(args):
         print(json.dumps(line))
     barrier(ws)
     return 0
+
+
+def _event_time(fn, repeats, flush):
+    """Median CUDA-event time of ``repeats`` calls of ``fn`` (ms per call),
+    each call timed alone with L2 flushed (512 MiB write) before it."""
+    import torch
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(repeats)]
+    fn()                                    # warm-up
+    for a, b in ev:
+        flush.zero_()
+        a.record()
+        fn()
+        b.record()
+    torch.cuda.synchronize()
+    return float(np.median([a.elapsed_time(b) for a, b in ev]))
+
+
+def measure_routines(arrays, sett, dev, flush):
+    """The routines beside the step on the workload's grid: free drift and
+    the bulk formula (per launch, against the HBM roofline of their
+    algorithmic bytes) and the cost of the EVP residual diagnostics."""
+    import ctypes
+    import torch
+    from veris_gb300.state import Call, VerisState
+    peak, peak_kind = hbm_peak()
+    out = {}
+    NX, NY = arrays["hIceMean"].shape
+    points = NX * NY
+    for prec, dt, esz in (("f64", torch.float64, 8), ("f32", torch.float32, 4)):
+        st = VerisState.from_numpy(arrays, sett, device=dev, dtype=dt)
+        c = Call(st, dtype=dt)
+        u, v = c.empty(2)
+        fn = c.lib.veris_freedrift_solver_f64 if prec == "f64" else c.lib.veris_freedrift_solver_f32
+        refs = c.refs()
+        ms = _event_time(lambda: fn(*refs, u.data_ptr(), v.data_ptr(), c.stream), 20, flush)
+        algo = 10 * esz * points            # 8 fields read, 2 written
+        out[f"freedrift_{prec}"] = {"ms": ms, "Gpoints_per_s": points / ms / 1e6,
+                                    "achieved_GBs": algo / ms / 1e6, "frac_hbm": algo / ms / 1e6 / peak,
+                                    "algorithmic_bytes": algo, "points": points}
+    rng = np.random.default_rng(1)
+    shape = (NX, NY)
+    bulk_in = [rng.normal(0, 7, shape), rng.normal(0, 7, shape), None, 0.02 * rng.random(shape),
+               271 + 30 * rng.random(shape)]
+    bulk_in[2] = bulk_in[4] + rng.normal(0, 5, shape)
+    from veris_gb300 import _abi
+    p = _abi.params_from_settings(sett)
+    lib = _abi.load()
+    stream = torch.cuda.current_stream(dev).cuda_stream
+    for prec, dt, esz in (("f64", torch.float64, 8), ("f32", torch.float32, 4)):
+        ins = [torch.as_tensor(a, dtype=dt, device=dev) for a in bulk_in]
+        outs = [torch.empty(shape, dtype=dt, device=dev) for _ in range(9)]
+        fn = lib.veris_bulkf_formula_lanl_f64 if prec == "f64" else lib.veris_bulkf_formula_lanl_f32
+        pr = ctypes.byref(p)
+        ptrs = [t.data_ptr() for t in ins] + [None] + [t.data_ptr() for t in outs]
+        ms = _event_time(lambda: fn(pr, points, *ptrs, stream), 20, flush)
+        algo = 14 * esz * points            # 5 inputs read, 9 outputs written
+        out[f"bulkf_formula_lanl_{prec}"] = {"ms": ms, "Gpoints_per_s": points / ms / 1e6,
+                                             "achieved_GBs": algo / ms / 1e6,
+                                             "frac_hbm": algo / ms / 1e6 / peak,
+                                             "algorithmic_bytes": algo, "points": points}
+    # residual diagnostics: the float64 loop with and without them
+    from veris_gb300.evp_solver import evp_solver, evp_solver_residuals
+    st = VerisState.from_numpy(arrays, sett, device=dev)
+    n = 20
+    t_plain = _event_time(lambda: evp_solver(st, n), 3, flush)
+    t_res = _event_time(lambda: evp_solver_residuals(st, n), 3, flush)
+    interior = (NX - 4) * (NY - 4)
+    extra_ms = max(t_res - t_plain, 1e-9) / n
+    algo = 13 * 8 * interior                # both states (10 fields) and 3 masks per interior point
+    out["evp_residual_f64"] = {"subcycles": n, "ms_plain_loop": t_plain, "ms_with_residuals": t_res,
+                               "overhead_frac": t_res / t_plain - 1, "ms_per_residual": extra_ms,
+                               "achieved_GBs": algo / extra_ms / 1e6, "frac_hbm": algo / extra_ms / 1e6 / peak,
+                               "algorithmic_bytes": algo}
+    out["peak_GBs"] = peak
+    out["peak_source"] = f"{peak_kind} HBM copy bandwidth"
+    out["l2"] = "flushed before every timed launch"
+    return out
 
 
 def run_adjoint(args):

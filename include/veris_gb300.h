@@ -79,7 +79,8 @@ typedef struct {
     X(PlasDefCoeff) X(deltaMin) X(pressReplFac) X(pStar) X(cStar)                     \
     X(basalDragU0) X(basalDragK1) X(basalDragK2) X(cBasalStar) X(tensileStrFac)       \
     X(CrMax) X(sideDragCoeff) X(sideDragU0)                                           \
-    X(s4t_cc0) X(s4t_cc1) X(s4t_cc2) X(s4t_d1) X(s4t_d1i)
+    X(s4t_cc0) X(s4t_cc1) X(s4t_cc2) X(s4t_d1) X(s4t_d1i)                              \
+    X(zvir) X(cpdair) X(karman) X(latvap) X(ocean_emissivity) X(gamma_blk) X(grav)
 
 #define VERIS_PARAM_INTS(X)                                                           \
     X(nITC) X(noSlip) X(secondOrderBC) X(useRelativeWind) X(useRealFreshWaterFlux)    \
@@ -197,6 +198,64 @@ int veris_evp_solver_f32(const VerisGrid *g, const VerisParams *p, const VerisFi
                          int32_t n_subcycles, float *uIce, float *vIce, float *sigma1,
                          float *sigma2, float *sigma12, void *workspace,
                          size_t workspace_bytes, veris_stream_t s);
+
+/*
+ * The same loop with the residual diagnostics of veris/evp_solver.py:193-234
+ * (settings.computeEvpResidual), as that branch means them: after subcycle
+ * k, over the interior,
+ *   resSig[k] = sum (d sig11 alphaC iceMask)^2 + (d sig22 alphaC iceMask)^2
+ *               + (d sigma12 alphaZ)^2,  sig11/22 = (sigma1 +- sigma2) / 2
+ *   resU[k]   = sum (iceMaskU d uIce betaU)^2 + (iceMaskV d vIce betaV)^2
+ * (d: the change over the subcycle; alpha, beta: those of that subcycle,
+ * adaptive or constant).  resU, resSig: n_subcycles doubles of device
+ * memory.  The sums are float64 and deterministic (fixed reduction order).
+ */
+size_t veris_evp_residual_workspace_bytes(const VerisGrid *g, int32_t elem_size,
+                                          int32_t n_subcycles);
+int veris_evp_residual_solver_f64(const VerisGrid *g, const VerisParams *p,
+                                  const VerisFieldsF64 *vs, int32_t n_subcycles, double *uIce,
+                                  double *vIce, double *sigma1, double *sigma2, double *sigma12,
+                                  double *resU, double *resSig, void *workspace,
+                                  size_t workspace_bytes, veris_stream_t s);
+int veris_evp_residual_solver_f32(const VerisGrid *g, const VerisParams *p,
+                                  const VerisFieldsF32 *vs, int32_t n_subcycles, float *uIce,
+                                  float *vIce, float *sigma1, float *sigma2, float *sigma12,
+                                  double *resU, double *resSig, void *workspace,
+                                  size_t workspace_bytes, veris_stream_t s);
+
+/*
+ * veris/freedrift_solver.py:5-62 freedrift_solver(state): ice velocities
+ * without internal stress, from WindForcingX/Y, uOcean, vOcean, hIceMean,
+ * fCori, iceMaskU, iceMaskV; every padded point of uIce and vIce is written.
+ * veris/dynsolver.py:93-97 selects it when settings.useFreedrift is set.
+ */
+int veris_freedrift_solver_f64(const VerisGrid *g, const VerisParams *p,
+                               const VerisFieldsF64 *vs, double *uIce, double *vIce,
+                               veris_stream_t s);
+int veris_freedrift_solver_f32(const VerisGrid *g, const VerisParams *p,
+                               const VerisFieldsF32 *vs, float *uIce, float *vIce,
+                               veris_stream_t s);
+
+/*
+ * veris/heat_flux_MITgcm.py:5-123 bulkf_formula_lanl(state, uw, vw, ta, qa,
+ * tsf, ocn_mask): bulk fluxes over open ocean at n points (any layout: the
+ * formula is pointwise).  Constants from p: zvir, cpdair, karman, latvap,
+ * ocean_emissivity, gamma_blk, grav, rhoAir, stefBoltz.  ocn_mask is not
+ * read (the reference takes only its shape) and may be NULL; a NULL output
+ * is not written.
+ */
+int veris_bulkf_formula_lanl_f64(const VerisParams *p, int64_t n, const double *uw,
+                                 const double *vw, const double *ta, const double *qa,
+                                 const double *tsf, const double *ocn_mask, double *flwupa,
+                                 double *flha, double *fsha, double *df0dT, double *ust,
+                                 double *vst, double *evp, double *ssq, double *dEvdT,
+                                 veris_stream_t s);
+int veris_bulkf_formula_lanl_f32(const VerisParams *p, int64_t n, const float *uw,
+                                 const float *vw, const float *ta, const float *qa,
+                                 const float *tsf, const float *ocn_mask, float *flwupa,
+                                 float *flha, float *fsha, float *df0dT, float *ust,
+                                 float *vst, float *evp, float *ssq, float *dEvdT,
+                                 veris_stream_t s);
 
 /*
  * The same loop (veris/evp_solver.py:21-319), fast form: a prep kernel folds

@@ -268,8 +268,8 @@ def evp_subcycle(state, c):
 
     ``c`` holds u, v, uNm1, vNm1, sigma1, sigma2, sigma12, denom1, denom2,
     EVPcFac, alphaC, alphaZ, betaU, betaV; it is updated in place.  The
-    residual branch of the reference (:193-234) is not restated: it reads
-    names the reference never defines.
+    residual branch of the reference (:193-234) reads names the reference
+    never defines; ``evp_residuals`` restates what it is meant to compute.
     """
     v, s = state.variables, state.settings
     u, vv = c["u"], c["v"]
@@ -372,6 +372,124 @@ def evp_solver(state, n=None):
     for _ in range(state.settings.nEVPsteps if n is None else n):
         evp_subcycle(state, c)
     return c["u"], c["v"], c["sigma1"], c["sigma2"], c["sigma12"]
+
+
+def evp_residuals(state, n=None):
+    """The EVP loop with the residual diagnostics of veris/evp_solver.py:193-234
+    as they are meant to work (the reference's branch reads the undefined names
+    sigma11/sigma22 and sig11Pm1..., here: the stress components 0.5(s1 +- s2)
+    before and after the subcycle).  Per subcycle k, over the interior:
+
+        resSig[k] = sum (d sig11 alphaC iceMask)^2 + (d sig22 alphaC iceMask)^2
+                        + (d sigma12 alphaZ)^2
+        resU[k]   = sum (iceMaskU d u betaU)^2 + (iceMaskV d v betaV)^2
+
+    Returns (uIce, vIce, sigma1, sigma2, sigma12, resU, resSig)."""
+    v, s = state.variables, state.settings
+    c = evp_carry(state)
+    n = s.nEVPsteps if n is None else n
+    resU = np.zeros(n)
+    resSig = np.zeros(n)
+    I = (slice(s.olx, -s.olx), slice(s.oly, -s.oly))
+    for k in range(n):
+        u0, v0 = c["u"], c["v"]
+        s110 = 0.5 * (c["sigma1"] + c["sigma2"])
+        s220 = 0.5 * (c["sigma1"] - c["sigma2"])
+        s120 = c["sigma12"]
+        evp_subcycle(state, c)
+        s11 = 0.5 * (c["sigma1"] + c["sigma2"])
+        s22 = 0.5 * (c["sigma1"] - c["sigma2"])
+        d11 = (s11 - s110) * c["alphaC"] * v.iceMask
+        d22 = (s22 - s220) * c["alphaC"] * v.iceMask
+        d12 = (c["sigma12"] - s120) * c["alphaZ"]
+        du = v.iceMaskU * (c["u"] - u0) * c["betaU"]
+        dv = v.iceMaskV * (c["v"] - v0) * c["betaV"]
+        resSig[k] = (d11 ** 2 + d22 ** 2 + d12 ** 2)[I].sum()
+        resU[k] = (du ** 2 + dv ** 2)[I].sum()
+    return c["u"], c["v"], c["sigma1"], c["sigma2"], c["sigma12"], resU, resSig
+
+
+def freedrift_solver(state):
+    """veris/freedrift_solver.py:5-62: ice velocities without internal stress."""
+    v, s = state.variables, state.settings
+    tauXc = 0.5 * (v.WindForcingX + _sx(v.WindForcingX, 1))
+    tauYc = 0.5 * (v.WindForcingY + _sy(v.WindForcingY, 1))
+    mIceCor = s.rhoIce * v.hIceMean * v.fCori
+    uOc = 0.5 * (v.uOcean + _sx(v.uOcean, 1))
+    vOc = 0.5 * (v.vOcean + _sy(v.vOcean, 1))
+    rhsX = -tauXc - mIceCor * vOc
+    rhsY = -tauYc + mIceCor * uOc
+    t1 = rhsX ** 2 + rhsY ** 2
+    w1 = t1 > 0
+    rhsN = np.where(w1, np.sqrt(rhsX ** 2 + rhsY ** 2), 0)
+    rhsA = np.where(w1, np.arctan2(rhsY, rhsX), 0)
+    t1 = 1 / (np.where(v.fCori < 0, s.waterIceDrag_south, s.waterIceDrag) * s.rhoSea)
+    t2 = t1 ** 2 * mIceCor ** 2
+    t3 = t1 ** 2 * rhsN ** 2
+    t4 = t2 ** 2 + 4 * t3
+    with np.errstate(invalid="ignore"):
+        solN = np.where(t3 > 0, np.sqrt(0.5 * (np.sqrt(t4) - t2)), 0)
+    t1 = 1 / t1
+    t2 = t1 * solN ** 2
+    t3 = mIceCor * solN
+    t4 = t2 ** 2 + t3 ** 2
+    solA = np.where(t4 > 0, rhsA - np.arctan2(t3, t2), 0)
+    uC = uOc - solN * np.cos(solA)
+    vC = vOc - solN * np.sin(solA)
+    u = 0.5 * (_sx(uC, -1) + uC) * v.iceMaskU
+    vv = 0.5 * (_sy(vC, -1) + vC) * v.iceMaskV
+    return u, vv
+
+
+def bulkf_formula_lanl(state, uw, vw, ta, qa, tsf, ocn_mask):
+    """veris/heat_flux_MITgcm.py:5-123: bulk fluxes over open ocean ->
+    (flwupa, flha, fsha, df0dT, ust, vst, evp, ssq, dEvdT)."""
+    s = state.settings
+    ht, zref, zice = 2.0, 10.0, 0.0005
+    aln = np.log(ht / zref)
+    czol = zref * s.karman * s.grav
+    lath = np.ones_like(ocn_mask) * s.latvap
+    us = np.sqrt(uw * uw + vw * vw)
+    usm = np.maximum(us, 1.0)
+    t0 = ta * (1.0 + s.zvir * qa)
+    ssq = 3.797915 * np.exp(lath * (7.93252e-6 - 2.166847e-3 / tsf)) / 1013.0
+    deltap = ta - tsf + s.gamma_blk * ht
+    delq = qa - ssq
+    rdn = s.karman / np.log(zref / zice)
+    rhn = ren = rdn
+    ustar = rdn * usm
+    tstar = rhn * deltap
+    qstar = ren * delq
+    for _ in range(5):
+        huol = czol / ustar ** 2 * (tstar / t0 + qstar / (1.0 / s.zvir + qa))
+        huol = np.minimum(np.abs(huol), 10.0) * np.sign(huol)
+        stable = 0.5 + 0.5 * np.sign(huol)
+        xsq = np.maximum(np.sqrt(np.abs(1.0 - 16.0 * huol)), 1.0)
+        x = np.sqrt(xsq)
+        psimh = -5.0 * huol * stable + (1.0 - stable) * (
+            2.0 * np.log(0.5 * (1.0 + x)) + 2.0 * np.log(0.5 * (1.0 + xsq)) - 2.0 * np.arctan(x) + np.pi * 0.5)
+        psixh = -5.0 * huol * stable + (1.0 - stable) * (2.0 * np.log(0.5 * (1.0 + xsq)))
+        rd = rdn / (1.0 + rdn * (aln - psimh) / s.karman)
+        rh = rhn / (1.0 + rhn * (aln - psixh) / s.karman)
+        re = rh
+        ustar = rd * usm
+        qstar = re * delq
+        tstar = rh * deltap
+    csha = s.rhoAir * s.cpdair * us * rh * rd
+    clha = s.rhoAir * lath * us * re * rd
+    fsha = csha * deltap
+    flha = clha * delq
+    evp = -flha / lath
+    flwupa = s.ocean_emissivity * s.stefBoltz * tsf ** 4
+    dflwupdt = 4.0 * s.ocean_emissivity * s.stefBoltz * tsf ** 3
+    devdt = clha * ssq * 2.166847e-3 / (tsf * tsf)
+    dflhdt = -lath * devdt
+    dfshdt = -csha
+    df0dt = -dflwupdt + dfshdt + dflhdt
+    cdn = 2.7e-3 / usm + 0.142e-3 + 0.0764e-3 * usm
+    ust = s.rhoAir * cdn * us * uw
+    vst = s.rhoAir * cdn * us * vw
+    return flwupa, flha, fsha, df0dt, ust, vst, evp, ssq, devdt
 
 
 def IceVelocities(state):

@@ -18,6 +18,8 @@ It writes one ``<case>.npz`` per case next to this script:
   (veris/setup/seaice_global_4deg/seaice_global_4deg.py:878-932), with the
   five-value ``IceVelocities`` result unpacked in full and the stresses stored
   back into the state;
+* ``forcing.npz`` (``--forcing``): free drift and the bulk formula, see
+  ``run_forcing``;
 * ``sub.<routine>.<output>``: single calls of the inner routines
   (strain rates, viscosities, drag coefficients, stress divergence, fluxes,
   limiter, solve4temp, one EVP subcycle) on the state after the dynamics
@@ -83,7 +85,9 @@ def _import_reference(ref):
     import veris.growth as growth
     import veris.solve4temp as s4t
     import veris.fill_overlap as fo
-    return SimpleNamespace(area_mass=area_mass, dynsolver=dynsolver, dyn=dyn,
+    import veris.freedrift_solver as fd
+    import veris.heat_flux_MITgcm as heat_flux
+    return SimpleNamespace(fd=fd, heat_flux=heat_flux, area_mass=area_mass, dynsolver=dynsolver, dyn=dyn,
                            averaging=averaging, evp=evp, ocean_stress=ocean_stress,
                            advection=advection, clean_up=clean_up, growth=growth,
                            s4t=s4t, fo=fo)
@@ -202,13 +206,79 @@ def _thermo_routines(R, state, out):
         R.s4t.solve4temp(state, hI, hS, vs.TSurf.copy(), TempFrz))
 
 
+def run_forcing(R):
+    """``forcing.npz``: the routines beside the step, on inputs that reach
+    their branches.
+
+    * ``fd.<case>.*``: ``freedrift_solver`` (veris/freedrift_solver.py:5-62)
+      on the state after the dynamics preparation of a case, and once with the
+      wind and ocean set to zero on part of the domain (rhsN = 0 there);
+    * ``bulk.*``: ``bulkf_formula_lanl`` (veris/heat_flux_MITgcm.py:5-123) on
+      seeded air/sea values spanning stable and unstable layers, calm and
+      strong winds;
+    * ``res.<case>.*``: nothing from the reference (its residual branch does
+      not run); the tests restate it."""
+    from veris_gb300.synthetic import make_state, config_settings
+    out = {}
+    for name in ("moving", "small_b"):
+        case = CASES[name]
+        arrays = make_state(**case["grid"])
+        sett = config_settings(case["config"], **case["overrides"])
+        state = _state(arrays, sett)
+        vs = state.variables
+        for fn, names in ((R.area_mass.SeaIceMass, ("SeaIceMassC", "SeaIceMassU", "SeaIceMassV")),
+                          (R.area_mass.AreaWS, ("AreaW", "AreaS")),
+                          (R.dynsolver.WindForcingXY, ("WindForcingX", "WindForcingY"))):
+            for n, val in zip(names, fn(state)):
+                setattr(vs, n, np.array(val, dtype=np.float64))
+        if name == "small_b":
+            calm = np.zeros_like(vs.hIceMean, dtype=bool)
+            calm[:, : calm.shape[1] // 3] = True
+            for n in ("WindForcingX", "WindForcingY", "uOcean", "vOcean"):
+                setattr(vs, n, np.where(calm, 0.0, getattr(vs, n)))
+        for n in ("WindForcingX", "WindForcingY", "uOcean", "vOcean", "hIceMean", "fCori",
+                  "iceMaskU", "iceMaskV"):
+            out[f"fd.{name}.in.{n}"] = np.array(getattr(vs, n), dtype=np.float64)
+        out[f"fd.{name}.settings"] = np.array(json.dumps(vars(sett), sort_keys=True))
+        list(_record(out, f"fd.{name}", ("uIce", "vIce"), R.fd.freedrift_solver(state)))
+
+    rng = np.random.default_rng(7)
+    shape = (40, 28)
+    uw = rng.normal(0.0, 8.0, shape)
+    vw = rng.normal(0.0, 8.0, shape)
+    uw[:3] *= 0.05                       # calm rows: |u| below 1 m/s
+    vw[:3] *= 0.05
+    uw[3, :4] = 0.0
+    vw[3, :4] = 0.0                      # no wind at all
+    tsf = 271.0 + 30.0 * rng.random(shape)
+    ta = tsf + rng.normal(0.0, 6.0, shape)          # both signs of air-sea difference
+    qa = 0.02 * rng.random(shape)
+    ocn = (rng.random(shape) > 0.2).astype(np.float64)
+    sett = config_settings("c1_4deg")
+    state = _state(dict(hIceMean=np.zeros(shape)), sett)
+    for n, val in (("uw", uw), ("vw", vw), ("ta", ta), ("qa", qa), ("tsf", tsf), ("ocn_mask", ocn)):
+        out[f"bulk.in.{n}"] = val
+    out["bulk.settings"] = np.array(json.dumps(vars(sett), sort_keys=True))
+    list(_record(out, "bulk", ("flwupa", "flha", "fsha", "df0dT", "ust", "vst", "evp", "ssq",
+                               "dEvdT"),
+                 R.heat_flux.bulkf_formula_lanl(state, uw, vw, ta, qa, tsf, ocn)))
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default=os.environ.get("VERIS_REFERENCE", "/root/reference"))
     ap.add_argument("--cases", nargs="*", default=list(CASES))
+    ap.add_argument("--forcing", action="store_true", help="write forcing.npz only")
     args = ap.parse_args()
     np.seterr(all="ignore")    # the reference's where() evaluates both branches
     R = _import_reference(args.reference)
+    if args.forcing:
+        out = run_forcing(R)
+        path = os.path.join(HERE, "forcing.npz")
+        np.savez_compressed(path, **out)
+        print(f"{path}: {len(out)} arrays, {os.path.getsize(path) / 1e6:.2f} MB")
+        return
     for name in args.cases:
         out = run_case(R, CASES[name])
         path = os.path.join(HERE, f"{name}.npz")

@@ -54,3 +54,29 @@ def rel_err(a, b):
     if scale == 0:
         return float(np.max(np.abs(a)))
     return float(np.max(np.abs(a - b)) / scale)
+
+
+def load_forcing():
+    """forcing.npz: free drift (``fd.<case>.*``) and the bulk formula (``bulk.*``)."""
+    return load("forcing")
+
+
+def freedrift_case(g, case):
+    """(state, {uIce, vIce}) of one free-drift record of forcing.npz."""
+    p = f"fd.{case}.in."
+    variables = {k[len(p):]: v.copy() for k, v in g.items() if k.startswith(p)}
+    settings = json.loads(str(g[f"fd.{case}.settings"]))
+    st = SimpleNamespace(variables=SimpleNamespace(**variables),
+                         settings=SimpleNamespace(**settings))
+    return st, {n: g[f"fd.{case}.{n}"] for n in ("uIce", "vIce")}
+
+
+BULK_IN = ("uw", "vw", "ta", "qa", "tsf", "ocn_mask")
+BULK_OUT = ("flwupa", "flha", "fsha", "df0dT", "ust", "vst", "evp", "ssq", "dEvdT")
+FREEDRIFT_CASES = ("moving", "small_b")
+
+
+def bulk_case(g):
+    """(settings, inputs in BULK_IN order, {output: array})."""
+    settings = SimpleNamespace(**json.loads(str(g["bulk.settings"])))
+    return settings, [g[f"bulk.in.{n}"] for n in BULK_IN], {n: g[f"bulk.{n}"] for n in BULK_OUT}

@@ -104,3 +104,46 @@ def test_fill_overlap_idempotent():
     once = O.fill_overlap(st, a.copy())
     twice = O.fill_overlap(st, once.copy())
     np.testing.assert_array_equal(once, twice)
+
+
+@pytest.mark.parametrize("case", G.FREEDRIFT_CASES)
+def test_freedrift_bit_exact(case):
+    st, ref = G.freedrift_case(G.load_forcing(), case)
+    u, v = O.freedrift_solver(st)
+    np.testing.assert_array_equal(u, ref["uIce"])
+    np.testing.assert_array_equal(v, ref["vIce"])
+
+
+def test_freedrift_fixture_reaches_the_zero_branches():
+    st, ref = G.freedrift_case(G.load_forcing(), "small_b")
+    v = st.variables
+    calm = (v.WindForcingX == 0) & (v.WindForcingY == 0) & (v.uOcean == 0) & (v.vOcean == 0)
+    assert calm.sum() > 50 and np.abs(ref["uIce"]).max() > 0
+
+
+def test_bulk_formula_bit_exact():
+    from types import SimpleNamespace
+    sett, args, ref = G.bulk_case(G.load_forcing())
+    got = O.bulkf_formula_lanl(SimpleNamespace(settings=sett), *args)
+    for n, a in zip(G.BULK_OUT, got):
+        np.testing.assert_array_equal(a, ref[n], err_msg=n)
+
+
+def test_bulk_fixture_spans_stable_and_unstable_layers():
+    _sett, (uw, vw, ta, qa, tsf, _m), _ref = G.bulk_case(G.load_forcing())
+    dT = ta - tsf
+    assert (dT > 1).any() and (dT < -1).any()
+    assert (np.hypot(uw, vw) < 1).any() and (np.hypot(uw, vw) == 0).any()
+
+
+def test_evp_residuals_match_the_plain_loop():
+    """The residual loop leaves the EVP result unchanged and its sums are
+    non-negative; with the state at rest and no forcing they are zero."""
+    g = G.load("moving")
+    first_evp = [i for i, r, _o in G.sequence(g) if r == "IceVelocities"][0]
+    st = G.state_before(g, first_evp)
+    u, v, s1, s2, s12, resU, resSig = O.evp_residuals(st, n=6)
+    ref = O.evp_solver(G.state_before(g, first_evp), n=6)
+    for a, b in zip((u, v, s1, s2, s12), ref):
+        np.testing.assert_array_equal(a, b)
+    assert resU.shape == (6,) and (resU > 0).all() and (resSig > 0).all()

@@ -42,7 +42,8 @@ PARAM_DOUBLES = (
     "airIceDrag_south waterIceDrag waterIceDrag_south cDragMin seaIceLoadFac gravity "
     "PlasDefCoeff deltaMin pressReplFac pStar cStar basalDragU0 basalDragK1 basalDragK2 "
     "cBasalStar tensileStrFac CrMax sideDragCoeff sideDragU0 "
-    "s4t_cc0 s4t_cc1 s4t_cc2 s4t_d1 s4t_d1i"
+    "s4t_cc0 s4t_cc1 s4t_cc2 s4t_d1 s4t_d1i "
+    "zvir cpdair karman latvap ocean_emissivity gamma_blk grav"
 ).split()
 PARAM_INTS = (
     "nITC noSlip secondOrderBC useRelativeWind useRealFreshWaterFlux useAdaptiveEVP "
@@ -64,6 +65,7 @@ class VerisFields(ctypes.Structure):
     _fields_ = [(n, ctypes.c_void_p) for n in ABI_ORDER]
 
 
+BULK_PARAMS = ("zvir", "cpdair", "karman", "latvap", "ocean_emissivity", "gamma_blk", "grav")
 DERIVED_PARAMS = ("EVPcFac", "sinWin", "cosWin", "sinWatOcn", "cosWatOcn",
                   "s4t_cc0", "s4t_cc1", "s4t_cc2", "s4t_d1", "s4t_d1i", "pad_")
 
@@ -76,9 +78,15 @@ def params_from_settings(sett):
     veris/evp_solver.py:264-268, veris/solve4temp.py:14-27), so both sides
     start from identically rounded constants.
     """
+    from .settings import SETTINGS
     p = VerisParams()
     for n in PARAM_DOUBLES:
         if n in DERIVED_PARAMS:
+            continue
+        if n in BULK_PARAMS and not hasattr(sett, n):
+            # host-model constants of the bulk formulae; settings saved before
+            # they were carried here hold the defaults
+            setattr(p, n, float(SETTINGS[n][0]))
             continue
         setattr(p, n, float(getattr(sett, n)))
     for n in PARAM_INTS:
@@ -131,6 +139,13 @@ SIGNATURES = {
     "veris_stressdiv_f64": ([_G, _Pa, _F, _P, _P, _P, _P, _P, _P], _I),
     "veris_evp_workspace_bytes": ([_G, ctypes.c_int32], _S),
     "veris_evp_solver_f64": ([_G, _Pa, _F, ctypes.c_int32, _P, _P, _P, _P, _P, _P, _S, _P], _I),
+    "veris_evp_residual_workspace_bytes": ([_G, ctypes.c_int32, ctypes.c_int32], _S),
+    "veris_evp_residual_solver_f64": ([_G, _Pa, _F, ctypes.c_int32] + [_P] * 8 + [_S, _P], _I),
+    "veris_evp_residual_solver_f32": ([_G, _Pa, _F, ctypes.c_int32] + [_P] * 8 + [_S, _P], _I),
+    "veris_freedrift_solver_f64": ([_G, _Pa, _F, _P, _P, _P], _I),
+    "veris_freedrift_solver_f32": ([_G, _Pa, _F, _P, _P, _P], _I),
+    "veris_bulkf_formula_lanl_f64": ([_Pa, _L] + [_P] * 15 + [_P], _I),
+    "veris_bulkf_formula_lanl_f32": ([_Pa, _L] + [_P] * 15 + [_P], _I),
     "veris_evp_solver_f32": ([_G, _Pa, _F, ctypes.c_int32, _P, _P, _P, _P, _P, _P, _S, _P], _I),
     "veris_evp_fast_workspace_bytes": ([_G, ctypes.c_int32], _S),
     "veris_evp_fast_settings_check": ([_Pa], _I),

@@ -31,6 +31,7 @@ struct EvpIO {
     const T *u, *v, *s1, *s2, *s12;   // state at the start of the subcycle
     T *uo, *vo, *s1o, *s2o, *s12o;    // state at its end
     const T *uNm1, *vNm1;             // velocities of the previous time step
+    T *aCo = nullptr;                 // adaptive EVP: alphaC of the subcycle, when not null
 };
 
 template <class T>
@@ -122,6 +123,7 @@ evp_subcycle_kernel(Ctx<T> c, HaloFill h, EvpIO<T> io) {
                 const int64_t o = d.raw(gi, gj);
                 io.s1o[o] = s1;
                 io.s2o[o] = s2;
+                if (ADAPT && io.aCo) io.aCo[o] = aC;
             }
             cds[k] = ocean_drag_c(c, io.u, io.v, gi, gj);
             if (BASAL) cbs[k] = basal_drag_c(c, io.u, io.v, gi, gj);
@@ -294,11 +296,189 @@ static int evp_solver(const VerisGrid *g, const VerisParams *p, const Fields<T> 
     return VERIS_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Residual diagnostics (veris/evp_solver.py:193-234, computeEvpResidual), as
+// that branch means them (it reads names it never binds): after subcycle k,
+// over the interior points,
+//   resSig[k] = sum (d sig11 alphaC iceMask)^2 + (d sig22 alphaC iceMask)^2 + (d sigma12 alphaZ)^2
+//   resU[k]   = sum (iceMaskU d uIce betaU)^2 + (iceMaskV d vIce betaV)^2
+// with sig11, sig22 = (sigma1 +- sigma2) / 2 and d the change over the
+// subcycle.  The ping-pong keeps the state before the subcycle intact, so the
+// residual kernel reads both states directly.  The sums are in float64 and
+// deterministic: a fixed grid (a function of the interior size only), warp
+// shuffles and one partial pair per block, then one block per subcycle adds
+// the partials in index order.
+
+constexpr int RES_THREADS = 256, RES_MAX_BLOCKS = 1024;
+
+static int res_blocks(const Dims &d) {
+    const int64_t want = ((int64_t)d.nx * d.ny + RES_THREADS - 1) / RES_THREADS;
+    return (int)(want < RES_MAX_BLOCKS ? want : RES_MAX_BLOCKS);
+}
+
+template <class T>
+struct ResIO {
+    const T *u0, *v0, *s10, *s20, *s120;   // before the subcycle
+    const T *u1, *v1, *s11, *s21, *s121;   // after it
+    const T *mC, *mU, *mV;
+    const T *aC;                            // adaptive alphaC, or null: alpha and beta are constants
+    double alpha, beta;
+};
+
+__device__ __forceinline__ double warp_sum(double x) {
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    return x;
+}
+
+template <class T>
+__global__ void __launch_bounds__(RES_THREADS) evp_residual_kernel(Dims d, ResIO<T> r, double *partial) {
+    __shared__ double red[2][RES_THREADS / 32];
+    const int64_t n = (int64_t)d.nx * d.ny;
+    const int ox = (d.NX - d.nx) / 2, oy = (d.NY - d.ny) / 2;
+    double su = 0.0, ss = 0.0;
+    for (int64_t k = blockIdx.x * (int64_t)RES_THREADS + threadIdx.x; k < n; k += (int64_t)gridDim.x * RES_THREADS) {
+        const int i = ox + (int)(k / d.ny), j = oy + (int)(k % d.ny);
+        const int64_t o = d.raw(i, j);
+        double aC = r.alpha, aZ = r.alpha, bU = r.beta, bV = r.beta;
+        if (r.aC) {
+            const double a0 = r.aC[o], aw = r.aC[o - d.ld], as = r.aC[o - 1], asw = r.aC[o - d.ld - 1];
+            aC = a0;
+            aZ = 0.5 * (0.5 * (a0 + as) + 0.5 * (aw + asw));
+            bU = 0.5 * (a0 + aw);
+            bV = 0.5 * (a0 + as);
+        }
+        const double s1a = r.s10[o], s2a = r.s20[o], s1b = r.s11[o], s2b = r.s21[o];
+        const double mC = r.mC[o];
+        const double d11 = (0.5 * (s1b + s2b) - 0.5 * (s1a + s2a)) * aC * mC;
+        const double d22 = (0.5 * (s1b - s2b) - 0.5 * (s1a - s2a)) * aC * mC;
+        const double d12 = ((double)r.s121[o] - (double)r.s120[o]) * aZ;
+        const double du = (double)r.mU[o] * ((double)r.u1[o] - (double)r.u0[o]) * bU;
+        const double dv = (double)r.mV[o] * ((double)r.v1[o] - (double)r.v0[o]) * bV;
+        ss += d11 * d11 + d22 * d22 + d12 * d12;
+        su += du * du + dv * dv;
+    }
+    su = warp_sum(su);
+    ss = warp_sum(ss);
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) {
+        red[0][w] = su;
+        red[1][w] = ss;
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        su = threadIdx.x < RES_THREADS / 32 ? red[0][threadIdx.x] : 0.0;
+        ss = threadIdx.x < RES_THREADS / 32 ? red[1][threadIdx.x] : 0.0;
+        su = warp_sum(su);
+        ss = warp_sum(ss);
+        if (threadIdx.x == 0) {
+            partial[2 * blockIdx.x] = su;
+            partial[2 * blockIdx.x + 1] = ss;
+        }
+    }
+}
+
+// one block per subcycle: the partials of that subcycle in index order
+__global__ void __launch_bounds__(RES_THREADS) evp_residual_finish_kernel(const double *partial, int nblk,
+                                                                          double *resU, double *resSig) {
+    __shared__ double red[2][RES_THREADS / 32];
+    const double *pk = partial + (int64_t)blockIdx.x * 2 * nblk;
+    double su = 0.0, ss = 0.0;
+    for (int b = threadIdx.x; b < nblk; b += RES_THREADS) {
+        su += pk[2 * b];
+        ss += pk[2 * b + 1];
+    }
+    su = warp_sum(su);
+    ss = warp_sum(ss);
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) {
+        red[0][w] = su;
+        red[1][w] = ss;
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        su = threadIdx.x < RES_THREADS / 32 ? red[0][threadIdx.x] : 0.0;
+        ss = threadIdx.x < RES_THREADS / 32 ? red[1][threadIdx.x] : 0.0;
+        su = warp_sum(su);
+        ss = warp_sum(ss);
+        if (threadIdx.x == 0) {
+            resU[blockIdx.x] = su;
+            resSig[blockIdx.x] = ss;
+        }
+    }
+}
+
+static size_t residual_workspace_bytes(const Dims &d, size_t elem, int n) {
+    return 6 * round_up(field_bytes(d, elem), 256) + (size_t)(n > 0 ? n : 0) * 2 * res_blocks(d) * sizeof(double);
+}
+
+template <class T>
+static int evp_residual_solver(const VerisGrid *g, const VerisParams *p, const Fields<T> *vs, int n, T *u, T *v,
+                               T *s1, T *s2, T *s12, double *resU, double *resSig, void *ws, size_t ws_bytes,
+                               veris_stream_t s) {
+    Dims d;
+    VERIS_CHECK_GRID(g, d);
+    VERIS_REQUIRE(p && vs && u && v && s1 && s2 && s12, VERIS_ERR_ARG);
+    VERIS_REQUIRE(n >= 0, VERIS_ERR_ARG);
+    if (n == 0) return evp_solver<T>(g, p, vs, 0, u, v, s1, s2, s12, ws, ws_bytes, s);
+    VERIS_REQUIRE(resU && resSig, VERIS_ERR_ARG);
+    VERIS_REQUIRE(ws && ws_bytes >= residual_workspace_bytes(d, sizeof(T), n), VERIS_ERR_WORKSPACE);
+    cudaStream_t st = (cudaStream_t)s;
+    const size_t fb = round_up(field_bytes(d, sizeof(T)), 256);
+    Ctx<T> c;
+    c.f = *vs;
+    c.d = d;
+    c.p = *p;
+    const HaloFill h = halo_fill_of(*p);
+    const bool adapt = p->useAdaptiveEVP != 0;
+    char *base = static_cast<char *>(ws);
+    T *buf[2][5] = {{u, v, s1, s2, s12}, {nullptr, nullptr, nullptr, nullptr, nullptr}};
+    for (int q = 0; q < 5; ++q) buf[1][q] = reinterpret_cast<T *>(base + q * fb);
+    T *aC = reinterpret_cast<T *>(base + 5 * fb);
+    double *partial = reinterpret_cast<double *>(base + 6 * fb);
+    const int nblk = res_blocks(d);
+    const T *cur[5] = {vs->uIce, vs->vIce, vs->sigma1, vs->sigma2, vs->sigma12};
+    for (int it = 0; it < n; ++it) {
+        T **dst = buf[(n - 1 - it) % 2];
+        EvpIO<T> io{cur[0], cur[1], cur[2], cur[3], cur[4], dst[0], dst[1], dst[2], dst[3], dst[4],
+                    vs->uIce, vs->vIce, adapt ? aC : nullptr};
+        int stt = dispatch_subcycle<T>(c, h, io, st);
+        if (stt != VERIS_OK) return stt;
+        ResIO<T> r{cur[0], cur[1], cur[2], cur[3], cur[4], dst[0], dst[1], dst[2], dst[3], dst[4],
+                   vs->iceMask, vs->iceMaskU, vs->iceMaskV, adapt ? aC : nullptr, p->evpAlpha, p->evpBeta};
+        evp_residual_kernel<T><<<nblk, RES_THREADS, 0, st>>>(d, r, partial + (int64_t)it * 2 * nblk);
+        stt = launch_status();
+        if (stt != VERIS_OK) return stt;
+        for (int q = 0; q < 5; ++q) cur[q] = dst[q];
+    }
+    evp_residual_finish_kernel<<<n, RES_THREADS, 0, st>>>(partial, nblk, resU, resSig);
+    return launch_status();
+}
+
 }  // namespace veris
 
 using namespace veris;
 
 extern "C" {
+
+size_t veris_evp_residual_workspace_bytes(const VerisGrid *g, int32_t elem_size, int32_t n_subcycles) {
+    Dims d;
+    if (check_grid(g, &d) != VERIS_OK || (elem_size != 4 && elem_size != 8) || n_subcycles < 0) return 0;
+    return residual_workspace_bytes(d, (size_t)elem_size, n_subcycles);
+}
+
+int veris_evp_residual_solver_f64(const VerisGrid *g, const VerisParams *p, const VerisFieldsF64 *vs,
+                                  int32_t n, double *u, double *v, double *s1, double *s2, double *s12,
+                                  double *resU, double *resSig, void *ws, size_t ws_bytes, veris_stream_t s) {
+    return evp_residual_solver<double>(g, p, reinterpret_cast<const Fields<double> *>(vs), n, u, v, s1, s2, s12,
+                                       resU, resSig, ws, ws_bytes, s);
+}
+
+int veris_evp_residual_solver_f32(const VerisGrid *g, const VerisParams *p, const VerisFieldsF32 *vs,
+                                  int32_t n, float *u, float *v, float *s1, float *s2, float *s12,
+                                  double *resU, double *resSig, void *ws, size_t ws_bytes, veris_stream_t s) {
+    return evp_residual_solver<float>(g, p, reinterpret_cast<const Fields<float> *>(vs), n, u, v, s1, s2, s12,
+                                      resU, resSig, ws, ws_bytes, s);
+}
 
 size_t veris_evp_workspace_bytes(const VerisGrid *g, int32_t elem_size) {
     Dims d;

@@ -2,6 +2,7 @@
 from ._abi import check
 from .state import Call
 from .evp_solver import evp_solver
+from .freedrift_solver import freedrift_solver
 
 
 def tauXY(state):
@@ -24,9 +25,16 @@ def WindForcingXY(state):
 def IceVelocities(state):
     """veris/dynsolver.py:87-102 -> (uIce, vIce, sigma1, sigma2, sigma12).
 
-    The free-drift branch of the reference is not selectable: it reads an
-    undefined name (veris/dynsolver.py:95) and is not part of the step.
+    ``useFreedrift``: the free-drift velocities with the stresses as they
+    are (the reference's branch means this but reads an unbound name,
+    veris/dynsolver.py:95-97); ``useEVP`` (checked second, so it wins when
+    both are set, as in the reference): the EVP loop.
     """
-    if state.settings.useFreedrift and not state.settings.useEVP:
-        raise NotImplementedError("free drift is not part of the GPU step")
-    return evp_solver(state)
+    s = state.settings
+    if s.useEVP:
+        return evp_solver(state)
+    if s.useFreedrift:
+        u, v = freedrift_solver(state)
+        vs = state.variables
+        return u, v, vs.sigma1.clone(), vs.sigma2.clone(), vs.sigma12.clone()
+    raise ValueError("IceVelocities: neither useEVP nor useFreedrift is set")

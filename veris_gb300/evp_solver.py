@@ -5,18 +5,31 @@ from ._abi import check
 from .state import Call
 
 
+# veris/evp_solver.py:18: print the residuals of every subcycle when they are computed
+printEvpResidual = False
+# (resU, resSig) of the last evp_solver call that computed residuals
+last_residuals = None
+
+
 def evp_solver(state, n_subcycles=None):
     """veris/evp_solver.py:257-319 -> (uIce, vIce, sigma1, sigma2, sigma12).
 
     Runs ``settings.nEVPsteps`` subcycles (or ``n_subcycles``) from the
     state's velocities and stresses in float64, one tiled kernel per
-    subcycle.  The residual diagnostics of the reference
-    (``computeEvpResidual``) read undefined names there
-    (veris/evp_solver.py:54-55) and are not part of this entry point.
+    subcycle.  With ``settings.computeEvpResidual`` the residuals of every
+    subcycle are computed as well (``evp_solver_residuals``), kept in the
+    module's ``last_residuals`` and printed when its ``printEvpResidual`` is
+    set, as in the reference (:227-234).
     """
+    global last_residuals
     s = state.settings
     if s.computeEvpResidual:
-        raise NotImplementedError("computeEvpResidual: use veris_gb300.diagnostics.evp_residuals")
+        out = evp_solver_residuals(state, n_subcycles)
+        last_residuals = (out[5], out[6])
+        if printEvpResidual:
+            for k, (ru, rs) in enumerate(zip(out[5].tolist(), out[6].tolist())):
+                print("evp resU, resSigma: %i %e %e" % (k, ru, rs))
+        return tuple(out[:5])
     n = int(s.nEVPsteps if n_subcycles is None else n_subcycles)
     c = Call(state)
     out = c.empty(5)
@@ -24,6 +37,32 @@ def evp_solver(state, n_subcycles=None):
     check("evp_solver", c.lib.veris_evp_solver_f64(*c.refs(), n, *[t.data_ptr() for t in out], ws, wsb,
                                                     c.stream))
     return tuple(out)
+
+
+def evp_solver_residuals(state, n_subcycles=None, precision="f64"):
+    """The loop with the residual diagnostics of veris/evp_solver.py:193-234
+    -> (uIce, vIce, sigma1, sigma2, sigma12, resU, resSig).
+
+    resU[k], resSig[k] (float64, one per subcycle) are the interior sums
+    that branch means to form after subcycle k: the squared changes of the
+    velocities weighted by the masks and beta, and of the stress components
+    sig11, sig22 = (sigma1 +- sigma2) / 2 and sigma12 weighted by alpha
+    (adaptive or constant).  The reference's branch reads names it never
+    binds (:54-56) and does not run; these are the sums it describes.
+    ``precision`` "f32" runs the loop on a float32 state (sums still in
+    float64)."""
+    s = state.settings
+    n = int(s.nEVPsteps if n_subcycles is None else n_subcycles)
+    dt = torch.float32 if precision == "f32" else torch.float64
+    c = Call(state, dtype=dt)
+    out = c.empty(5)
+    res = torch.zeros((2, max(n, 1)), dtype=torch.float64, device=c.device)
+    ws, wsb = c.workspace(c.lib.veris_evp_residual_workspace_bytes(c.refs()[0], 4 if dt == torch.float32 else 8,
+                                                                   n))
+    fn = c.lib.veris_evp_residual_solver_f32 if dt == torch.float32 else c.lib.veris_evp_residual_solver_f64
+    check("evp_solver_residuals", fn(*c.refs(), n, *[t.data_ptr() for t in out], res[0].data_ptr(),
+                                     res[1].data_ptr(), ws, wsb, c.stream))
+    return tuple(out) + (res[0, :n], res[1, :n])
 
 
 def evp_solver_f32(state32, n_subcycles=None):

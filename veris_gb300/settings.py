@@ -116,6 +116,14 @@ SETTINGS = dict(
     CrMax=(1e6, float, "slope-ratio bound of the flux limiter"),
     sideDragCoeff=(0.001, float, "side drag coefficient"),
     sideDragU0=(0.01, float, "side drag velocity [m/s]"),
+    # bulk formulae over open ocean (veris/settings.py:156-173, veris/heat_flux_MITgcm.py)
+    zvir=(0.608, float, "dry-air / water-vapour molecular mass ratio term"),
+    cpdair=(1.00464e3, float, "specific heat of dry air [J/K/kg]"),
+    karman=(0.4, float, "von Karman constant"),
+    latvap=(2.501e6, float, "latent heat of evaporation [J/kg]"),
+    ocean_emissivity=(0.985, float, "ocean surface emissivity"),
+    gamma_blk=(0.010, float, "adiabatic lapse rate [K/m]"),
+    grav=(9.81, float, "gravitational acceleration of the host model (bulk formulae)"),
 )
 
 
