@@ -56,6 +56,8 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-routines", action="store_true",
                     help="skip the free-drift, bulk-formula and residual measurements")
+    ap.add_argument("--routines-only", action="store_true",
+                    help="measure only the free-drift, bulk-formula and residual routines")
     ap.add_argument("--subcycles", type=int, default=None, help="override the workload's subcycles")
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--evp", default="auto", choices=("auto", "fast", "plain"))
@@ -549,6 +551,29 @@ def measure_routines(arrays, sett, dev, flush):
     return out
 
 
+def run_routines(args):
+    """Only the routines beside the step (free drift, bulk formula, EVP
+    residuals) on the workload's grid: one JSON line."""
+    import torch
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    from __graft_entry__ import build
+    build()
+    from veris_gb300.synthetic import CONFIGS, make_state, config_settings
+    c = CONFIGS[args.config]
+    arrays = make_state(c["nx"], c["ny"], seed=args.seed)
+    sett = config_settings(args.config)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    clocks = ClockSampler(0)
+    clocks.start()
+    out = measure_routines(arrays, sett, dev, flush)
+    line = {"metric": "routines beside the EVP step", "config": {"workload": args.config, "nx": c["nx"],
+                                                                  "ny": c["ny"]},
+            "data": "synthetic", "routines": out, "clocks": clocks.stop()}
+    print(json.dumps(line))
+    return 0
+
+
 def run_adjoint(args):
     """Gradient of a tracking loss through a float64 trajectory.
 
@@ -748,6 +773,8 @@ def main():
         return run_ensemble(args)
     if args.adjoint:
         return run_adjoint(args)
+    if args.routines_only and args.impl != "reference":
+        return run_routines(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

@@ -285,7 +285,7 @@ int veris_evp_fast_solver_f64(const VerisGrid *g, const VerisParams *p, const Ve
  * The same float32 loop with the register-walking kernel: one warp per
  * 28-column strip walks `rows` output rows (4..4096; 0: the longest walk
  * that keeps all walks in one wave of resident warps), rows in registers and
- * columns across lanes; no shared memory, no barriers.  `variant` (0..3)
+ * columns across lanes; no shared memory, no barriers.  `variant` (0..5)
  * picks the compiled form: register budget free (0), 5 (1) or 4 (2, 3)
  * resident 4-warp CTAs per SM, and (3) the own-point constants loaded one
  * walk step early; same values.

@@ -183,8 +183,32 @@ def test_walk_form_on_a_larger_synthetic_grid():
         for o, x in zip(outs, vals):
             setattr(st.variables, o, x)
     smem = evp_solver_fast(st, "f32", "smem", n_subcycles=20)
-    for rows, variant in ((16, 0), (33, 1), (8, 3)):
+    for rows, variant in ((16, 0), (33, 1), (8, 3), (0, 2)):
         walk = evp_solver_fast(st, "f32", "walk", n_subcycles=20, rows=rows, variant=variant)
         for k in range(5):
             e = G.rel_err(walk[k].double().cpu().numpy(), smem[k].double().cpu().numpy())
             assert e <= 1e-5, (rows, k, e)
+
+
+@pytest.mark.parametrize("nx,ny", ((297, 151), (61, 9), (5, 57)))
+def test_walk_on_odd_and_narrow_widths(nx, ny):
+    """Odd padded widths, and grids narrower than one strip (the strip
+    covers the periodic width several times over)."""
+    from veris_gb300.evp_solver import evp_solver_fast
+    from veris_gb300.state import VerisState
+    from veris_gb300.synthetic import config_settings, make_state
+    st = VerisState.from_numpy(make_state(nx, ny, seed=nx, init_velocity=0.05, ice_lat=0.0),
+                               config_settings("c3_1deg"))
+    from veris_gb300 import model
+    for name in ("SeaIceMass", "AreaWS", "WindForcingXY", "SeaIceStrength"):
+        fn, outs = [(f, o) for n, f, o in model.STEP if n == name][0]
+        vals = fn(st)
+        vals = vals if isinstance(vals, tuple) else (vals,)
+        for o, x in zip(outs, vals):
+            setattr(st.variables, o, x)
+    smem = evp_solver_fast(st, "f32", "smem", n_subcycles=12)
+    for rows, variant in ((16, 2), (5, 1), (0, 3), (8, 0)):
+        walk = evp_solver_fast(st, "f32", "walk", n_subcycles=12, rows=rows, variant=variant)
+        for k in range(5):
+            e = G.rel_err(walk[k].double().cpu().numpy(), smem[k].double().cpu().numpy())
+            assert e <= 1e-5, (nx, ny, rows, variant, k, e)

@@ -309,12 +309,10 @@ static int evp_solver(const VerisGrid *g, const VerisParams *p, const Fields<T> 
 // shuffles and one partial pair per block, then one block per subcycle adds
 // the partials in index order.
 
-constexpr int RES_THREADS = 256, RES_MAX_BLOCKS = 1024;
+constexpr int RES_THREADS = 256, RES_MAX_BLOCKS = 2048;
 
-static int res_blocks(const Dims &d) {
-    const int64_t want = ((int64_t)d.nx * d.ny + RES_THREADS - 1) / RES_THREADS;
-    return (int)(want < RES_MAX_BLOCKS ? want : RES_MAX_BLOCKS);
-}
+// one block per interior row (rows beyond RES_MAX_BLOCKS go round again)
+static int res_blocks(const Dims &d) { return d.nx < RES_MAX_BLOCKS ? d.nx : RES_MAX_BLOCKS; }
 
 template <class T>
 struct ResIO {
@@ -333,29 +331,33 @@ __device__ __forceinline__ double warp_sum(double x) {
 template <class T>
 __global__ void __launch_bounds__(RES_THREADS) evp_residual_kernel(Dims d, ResIO<T> r, double *partial) {
     __shared__ double red[2][RES_THREADS / 32];
-    const int64_t n = (int64_t)d.nx * d.ny;
     const int ox = (d.NX - d.nx) / 2, oy = (d.NY - d.ny) / 2;
     double su = 0.0, ss = 0.0;
-    for (int64_t k = blockIdx.x * (int64_t)RES_THREADS + threadIdx.x; k < n; k += (int64_t)gridDim.x * RES_THREADS) {
-        const int i = ox + (int)(k / d.ny), j = oy + (int)(k % d.ny);
-        const int64_t o = d.raw(i, j);
-        double aC = r.alpha, aZ = r.alpha, bU = r.beta, bV = r.beta;
+    for (int row = blockIdx.x; row < d.nx; row += gridDim.x)
+    for (int col = threadIdx.x; col < d.ny; col += RES_THREADS) {
+        const int64_t o = d.raw(ox + row, oy + col);
+        // (d sig11)^2 + (d sig22)^2 = 0.5 ((d sigma1)^2 + (d sigma2)^2); with
+        // constant alpha and beta their squares multiply the block sums instead
+        const double d1 = (double)r.s11[o] - (double)r.s10[o], d2 = (double)r.s21[o] - (double)r.s20[o];
+        const double d12 = (double)r.s121[o] - (double)r.s120[o];
+        const double du = (double)r.mU[o] * ((double)r.u1[o] - (double)r.u0[o]);
+        const double dv = (double)r.mV[o] * ((double)r.v1[o] - (double)r.v0[o]);
+        const double mC = r.mC[o];
+        const double c2 = fma(d1, d1, d2 * d2) * (0.5 * (mC * mC));
         if (r.aC) {
             const double a0 = r.aC[o], aw = r.aC[o - d.ld], as = r.aC[o - 1], asw = r.aC[o - d.ld - 1];
-            aC = a0;
-            aZ = 0.5 * (0.5 * (a0 + as) + 0.5 * (aw + asw));
-            bU = 0.5 * (a0 + aw);
-            bV = 0.5 * (a0 + as);
+            const double aZ = 0.5 * (0.5 * (a0 + as) + 0.5 * (aw + asw));
+            const double bU = 0.5 * (a0 + aw), bV = 0.5 * (a0 + as);
+            ss += c2 * (a0 * a0) + (d12 * aZ) * (d12 * aZ);
+            su += (du * bU) * (du * bU) + (dv * bV) * (dv * bV);
+        } else {
+            ss += fma(d12, d12, c2);
+            su += fma(du, du, dv * dv);
         }
-        const double s1a = r.s10[o], s2a = r.s20[o], s1b = r.s11[o], s2b = r.s21[o];
-        const double mC = r.mC[o];
-        const double d11 = (0.5 * (s1b + s2b) - 0.5 * (s1a + s2a)) * aC * mC;
-        const double d22 = (0.5 * (s1b - s2b) - 0.5 * (s1a - s2a)) * aC * mC;
-        const double d12 = ((double)r.s121[o] - (double)r.s120[o]) * aZ;
-        const double du = (double)r.mU[o] * ((double)r.u1[o] - (double)r.u0[o]) * bU;
-        const double dv = (double)r.mV[o] * ((double)r.v1[o] - (double)r.v0[o]) * bV;
-        ss += d11 * d11 + d22 * d22 + d12 * d12;
-        su += du * du + dv * dv;
+    }
+    if (!r.aC) {
+        su *= r.beta * r.beta;
+        ss *= r.alpha * r.alpha;
     }
     su = warp_sum(su);
     ss = warp_sum(ss);

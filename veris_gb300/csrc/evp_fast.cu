@@ -326,7 +326,7 @@ int veris_evp_fast_solver_f32(const VerisGrid *g, const VerisParams *p, const Ve
 int veris_evp_walk_solver_f32(const VerisGrid *g, const VerisParams *p, const VerisFieldsF64 *vs, int32_t n,
                               int32_t rows, int32_t variant, float *u, float *v, float *s1, float *s2, float *s12,
                               void *ws, size_t wsb, veris_stream_t s) {
-    VERIS_REQUIRE((rows == 0 || (rows >= 4 && rows <= 4096)) && variant >= 0 && variant < 4, VERIS_ERR_ARG);
+    VERIS_REQUIRE((rows == 0 || (rows >= 4 && rows <= 4096)) && variant >= 0 && variant < N_WALK_VARIANTS, VERIS_ERR_ARG);
     return evp_fast<float>(g, p, vs, n, u, v, s1, s2, s12, ws, wsb, rows == 0 ? -1 : rows, s, nullptr, 0, variant);
 }
 

@@ -141,6 +141,8 @@ bool evp_tma_available();
 // the same with the register-walking kernel: one warp per 28-column strip
 // walking `rows` output rows, compiled form `variant` (loop unroll x register
 // budget), reading state[0] first
+// compiled forms of the register-walking kernel (evp_walk.cu)
+constexpr int N_WALK_VARIANTS = 4;
 int evp_walk_subcycles(const Dims &d, const HaloFill &h, const FastConsts<float> &c, const FastScalars<float> &k,
                        float *const state[2][5], float *const outs[5], int64_t ldo, int n, bool basal, bool turn,
                        int rows, int variant, cudaStream_t st);

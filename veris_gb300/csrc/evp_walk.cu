@@ -19,7 +19,7 @@ template <>
 struct Variant<2> { static constexpr int UNROLL = 1, MINB = 4; static constexpr bool PRE = false; };
 template <>
 struct Variant<3> { static constexpr int UNROLL = 1, MINB = 4; static constexpr bool PRE = true; };
-constexpr int N_VARIANTS = 4;
+constexpr int N_VARIANTS = N_WALK_VARIANTS;
 
 template <bool BASAL, bool TURN, int V>
 __global__ void __launch_bounds__(WARPS * 32, Variant<V>::MINB)

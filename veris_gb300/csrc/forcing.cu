@@ -5,12 +5,12 @@
 // Free drift.  The reference solves a 2x2 problem at every C point and
 // averages the C-point velocities onto the U and V faces.  Here one warp owns
 // a strip of 31 output columns (lane 0 solves the column to the strip's south
-// for its neighbour) and walks down FD_ROWS rows: the U average needs the row
+// for its neighbour) and walks down a few rows: the U average needs the row
 // above, which the lane still holds from its previous step, and the V average
 // needs the column to the south, one shuffle away; the east and north
 // neighbours of the C-point averages (WindForcingX, uOcean at i+1) are the
 // next row's own loads, carried in registers.  Every C point is solved about
-// 1.1 times.
+// 1.1 times (float64, 16-row walks) or 1.3 times (float32, 4-row walks).
 //
 // The angle of the solution enters the reference only through
 // cos(rhsA - atan2(t3, t2)) and sin(rhsA - atan2(t3, t2)), with rhsA =
@@ -33,7 +33,12 @@
 
 namespace veris {
 
-constexpr int FD_LANES = 31, FD_ROWS = 16, FD_WARPS = 8;
+// rows per walk: float64 is bound by its arithmetic and walks long (fewer
+// C points solved twice); float32 is bound by memory latency and walks short,
+// unrolled, so that all its rows' loads are in flight together
+constexpr int FD_LANES = 31, FD_WARPS = 8;
+template <class T>
+struct FdRows { static constexpr int value = sizeof(T) == 8 ? 16 : 4; };
 
 template <class T>
 struct FdArgs {
@@ -78,9 +83,10 @@ freedrift_kernel(Dims d, FdArgs<T> a, int n_strips) {
     const int lane = threadIdx.x & 31;
     const int w = blockIdx.x * FD_WARPS + (threadIdx.x >> 5);
     const int strip = w % n_strips, band = w / n_strips;
-    const int i_first = band * FD_ROWS;
+    constexpr int ROWS = FdRows<T>::value;
+    const int i_first = band * ROWS;
     if (i_first >= d.NX) return;
-    const int i_end = min(i_first + FD_ROWS, d.NX);
+    const int i_end = min(i_first + ROWS, d.NX);
     const int jc = strip * FD_LANES + lane - 1;            // lane 0: the column to the south
     const bool live = jc < d.NY;                           // columns past the edge feed nothing
     const int j = d.wy(live ? jc : d.NY - 1);
@@ -92,7 +98,10 @@ freedrift_kernel(Dims d, FdArgs<T> a, int n_strips) {
     int64_t o = (int64_t)i * d.ld;
     T wfx = __ldg(a.wfx + o + j), uo = __ldg(a.uo + o + j);
     T uPrev = T(0);
-    for (int r = i_first - 1; r < i_end; ++r) {
+#pragma unroll
+    for (int q = 0; q <= ROWS; ++q) {
+        const int r = i_first - 1 + q;
+        if (r >= i_end) break;
         const int in = d.wx(i + 1);
         const int64_t on = (int64_t)in * d.ld;
         const T wfxN = __ldg(a.wfx + on + j), uoN = __ldg(a.uo + on + j);
@@ -124,6 +133,7 @@ struct BulkArgs {
     T *flwupa, *flha, *fsha, *df0dT, *ust, *vst, *evp, *ssq, *dEvdT;
     int64_t n;
     T zvir, cpdair, karman, latvap, emis, gamma_blk, rhoAir, stefBoltz, czol, aln, rdn;
+    T g, rlatvap;   // rdn / karman, 1 / latvap
 };
 
 template <class T>
@@ -137,14 +147,20 @@ __global__ void __launch_bounds__(256) bulkf_kernel(BulkArgs<T> a) {
         const T us = sqrt(uw * uw + vw * vw);
         const T usm = us > T(1) ? us : T(1);
         const T t0 = ta * (T(1) + a.zvir * qa);
-        const T ssq = T(3.797915) * exp(lath * (T(7.93252e-6) - T(2.166847e-3) / tsf)) / T(1013.0);
+        const T rtsf = T(1) / tsf;
+        const T ssq = T(3.797915) * exp(lath * (T(7.93252e-6) - T(2.166847e-3) * rtsf)) * T(1.0 / 1013.0);
         const T deltap = ta - tsf + a.gamma_blk * ht;
         const T delq = qa - ssq;
         const T qden = T(1) / a.zvir + qa;
-        T ustar = a.rdn * usm, tstar = a.rdn * deltap, qstar = a.rdn * delq;
-        T rd = a.rdn, rh = a.rdn;
+        // With rd = rdn / Dm and rh = re = rdn / Dh (Dm = Dh = 1 before the
+        // first iteration), ustar = rd usm, tstar = rh deltap, qstar = rh delq:
+        //   huol = czol / ustar^2 (tstar / t0 + qstar / qden) = K Dm^2 / Dh,
+        //   K = czol (deltap qden + delq t0) / (t0 qden usm^2 rdn)
+        // one division per iteration instead of seven; rounding differs only.
+        const T K = a.czol * (deltap * qden + delq * t0) / (t0 * qden * (usm * usm) * a.rdn);
+        T Dm = T(1), Dh = T(1);
         for (int it = 0; it < 5; ++it) {
-            T huol = a.czol / (ustar * ustar) * (tstar / t0 + qstar / qden);
+            T huol = it == 0 ? K : K * (Dm * Dm) / Dh;
             const T ah = fabs(huol);
             huol = (ah < T(10) ? ah : T(10)) * bk_sign(huol);
             T psimh, psixh;
@@ -160,21 +176,19 @@ __global__ void __launch_bounds__(256) bulkf_kernel(BulkArgs<T> a) {
                         (T(1) - stable) * (T(2) * log(T(0.5) * (T(1) + x)) + l2 - T(2) * atan(x) + pi * T(0.5));
                 psixh = T(-5) * huol * stable + (T(1) - stable) * l2;
             }
-            rd = a.rdn / (T(1) + a.rdn * (a.aln - psimh) / a.karman);
-            rh = a.rdn / (T(1) + a.rdn * (a.aln - psixh) / a.karman);
-            ustar = rd * usm;
-            qstar = rh * delq;
-            tstar = rh * deltap;
+            Dm = T(1) + a.g * (a.aln - psimh);
+            Dh = T(1) + a.g * (a.aln - psixh);
         }
-        const T csha = a.rhoAir * a.cpdair * us * rh * rd;
-        const T clha = a.rhoAir * lath * us * rh * rd;
+        const T rhrd = a.rdn * a.rdn / (Dm * Dh);   // rh rd (= re rd)
+        const T csha = a.rhoAir * a.cpdair * us * rhrd;
+        const T clha = a.rhoAir * lath * us * rhrd;
         const T flha = clha * delq;
         if (a.fsha) a.fsha[k] = csha * deltap;
         if (a.flha) a.flha[k] = flha;
-        if (a.evp) a.evp[k] = -flha / lath;
+        if (a.evp) a.evp[k] = -flha * a.rlatvap;
         const T t2 = tsf * tsf, t3 = t2 * tsf;
         if (a.flwupa) a.flwupa[k] = a.emis * a.stefBoltz * (t2 * t2);
-        const T devdt = clha * ssq * T(2.166847e-3) / t2;
+        const T devdt = clha * ssq * T(2.166847e-3) * (rtsf * rtsf);
         if (a.df0dT) a.df0dT[k] = -(T(4) * a.emis * a.stefBoltz * t3) + (-csha) + (-lath * devdt);
         if (a.dEvdT) a.dEvdT[k] = devdt;
         if (a.ssq) a.ssq[k] = ssq;
@@ -210,7 +224,7 @@ static int freedrift(const VerisGrid *g, const VerisParams *p, const Fields<T> *
     a.t1n_inv = T(1.0 / t1n);
     a.t1s_inv = T(1.0 / t1s);
     const int n_strips = (d.NY + FD_LANES - 1) / FD_LANES;
-    const int n_bands = (d.NX + FD_ROWS - 1) / FD_ROWS;
+    const int n_bands = (d.NX + FdRows<T>::value - 1) / FdRows<T>::value;
     const int warps = n_strips * n_bands;
     freedrift_kernel<T><<<(warps + FD_WARPS - 1) / FD_WARPS, FD_WARPS * 32, 0, (cudaStream_t)s>>>(d, a, n_strips);
     return launch_status();
@@ -236,6 +250,8 @@ static int bulkf(const VerisParams *p, int64_t n, const T *uw, const T *vw, cons
     a.czol = T(10.0 * p->karman * p->grav);
     a.aln = T(std::log(2.0 / 10.0));
     a.rdn = T(p->karman / std::log(10.0 / 0.0005));
+    a.g = T(p->karman / std::log(10.0 / 0.0005) / p->karman);
+    a.rlatvap = T(1.0 / p->latvap);
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
