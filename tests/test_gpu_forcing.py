@@ -225,3 +225,28 @@ def test_evp_solver_prints_residuals(capsys):
     assert len(out) == 5 and len(lines) == 4
     assert lines[0].startswith("evp resU, resSigma: 0 ")
     assert E.last_residuals[0].shape == (4,)
+
+
+def test_abi_argument_checks():
+    """Status codes of the new entry points for bad arguments (nothing is
+    launched for them)."""
+    import ctypes
+    from veris_gb300 import _abi
+    from veris_gb300.state import Call
+    lib = _abi.load()
+    gst, _st, _ref = _fd_state("moving")
+    c = Call(gst)
+    u = c.empty()
+    assert lib.veris_freedrift_solver_f64(*c.refs(), u.data_ptr(), None, c.stream) == 6   # invalid argument
+    p = _abi.params_from_settings(gst.settings)
+    assert lib.veris_bulkf_formula_lanl_f64(ctypes.byref(p), 0, *([None] * 15), c.stream) == 0   # n = 0: nothing to do
+    assert lib.veris_bulkf_formula_lanl_f64(ctypes.byref(p), -1, *([None] * 15), c.stream) == 6
+    assert lib.veris_bulkf_formula_lanl_f64(ctypes.byref(p), 16, *([None] * 15), c.stream) == 6   # inputs missing
+    need = lib.veris_evp_residual_workspace_bytes(c.refs()[0], 8, 4)
+    assert need > 0
+    res = torch.zeros(8, dtype=torch.float64, device="cuda")
+    ws = torch.empty(need - 8, dtype=torch.uint8, device="cuda")
+    outs = c.empty(5)
+    st = lib.veris_evp_residual_solver_f64(*c.refs(), 4, *[t.data_ptr() for t in outs], res.data_ptr(),
+                                           res[4:].data_ptr(), ws.data_ptr(), ws.numel(), c.stream)
+    assert st == 8   # workspace too small
