@@ -270,6 +270,9 @@ int veris_bulkf_formula_lanl_f32(const VerisParams *p, int64_t n, const float *u
  */
 size_t veris_evp_fast_workspace_bytes(const VerisGrid *g, int32_t elem_size);
 int veris_evp_fast_settings_check(const VerisParams *p);
+/* the same for veris_evp_walk_solver_f32, which also runs the adaptive EVP
+ * (veris/evp_solver.py:65-73, 97-100, 148-150) */
+int veris_evp_walk_settings_check(const VerisParams *p);
 int veris_evp_fast_check(const VerisGrid *g, const VerisParams *p, const VerisFieldsF64 *vs,
                          int32_t *violations_device, veris_stream_t s);
 int veris_evp_fast_solver_f32(const VerisGrid *g, const VerisParams *p, const VerisFieldsF64 *vs,

@@ -212,3 +212,63 @@ def test_walk_on_odd_and_narrow_widths(nx, ny):
         for k in range(5):
             e = G.rel_err(walk[k].double().cpu().numpy(), smem[k].double().cpu().numpy())
             assert e <= 1e-5, (nx, ny, rows, variant, k, e)
+
+
+def _prepared(nx, ny, seed, **overrides):
+    from veris_gb300 import model
+    from veris_gb300.state import VerisState
+    from veris_gb300.synthetic import config_settings, make_state
+    sett = config_settings("c3_1deg", **overrides)
+    st = VerisState.from_numpy(make_state(nx, ny, seed=seed, init_velocity=0.05, init_stress=2000.0, ice_lat=30.0),
+                               sett)
+    for name in ("SeaIceMass", "AreaWS", "WindForcingXY", "SeaIceStrength"):
+        fn, outs = [(f, o) for n, f, o in model.STEP if n == name][0]
+        vals = fn(st)
+        vals = vals if isinstance(vals, tuple) else (vals,)
+        for o, x in zip(outs, vals):
+            setattr(st.variables, o, x)
+    return st
+
+
+@pytest.mark.parametrize("nx,ny,rows,variant", ((120, 90, 0, 2), (61, 33, 7, 0), (200, 150, 16, 3)))
+def test_walk_adaptive_evp(nx, ny, rows, variant):
+    """Adaptive EVP in the register-walking kernel against the plain float64
+    and float32 loops (alphaC from zeta per subcycle, alphaZ and the betas
+    averaged from it)."""
+    from veris_gb300.evp_solver import evp_solver, evp_solver_f32, evp_solver_fast
+    from veris_gb300.state import VerisState
+    st = _prepared(nx, ny, nx, useAdaptiveEVP=True)
+    n = 20
+    walk = evp_solver_fast(st, "f32", "walk", n_subcycles=n, rows=rows, variant=variant)
+    ref = evp_solver(st, n)
+    st32 = VerisState({k: getattr(st.variables, k).float() for k in st.variables.names()}, st.settings)
+    plain32 = evp_solver_f32(st32, n)
+    for k in range(5):
+        w = walk[k].double().cpu().numpy()
+        e64 = G.rel_err(w, ref[k].cpu().numpy())
+        e32 = G.rel_err(w, plain32[k].double().cpu().numpy())
+        assert e64 <= 1e-3, (k, e64)
+        assert e32 <= 1e-3, (k, e32)
+    # and it is not the constant-alpha solve
+    st_c = _prepared(nx, ny, nx)
+    const = evp_solver_fast(st_c, "f32", "walk", n_subcycles=n, rows=rows, variant=variant)
+    assert G.rel_err(walk[0].double().cpu().numpy(), const[0].double().cpu().numpy()) > 1e-3
+
+
+def test_engine_f32_runs_adaptive_evp_in_the_walk():
+    from veris_gb300.engine import SeaIceStep
+    from veris_gb300.state import VerisState
+    from veris_gb300.synthetic import config_settings, make_state
+    sett = config_settings("c3_1deg", useAdaptiveEVP=True, nEVPsteps=30)
+    arrays = make_state(96, 64, seed=9, init_velocity=0.05)
+    s32 = VerisState.from_numpy(arrays, sett)
+    s64 = VerisState.from_numpy(arrays, sett)
+    e32 = SeaIceStep(s32, precision="f32")
+    e64 = SeaIceStep(s64, precision="f64", evp="plain")
+    assert e32.evp_form == "fast"
+    e32.step()
+    e64.step()
+    torch.cuda.synchronize()
+    for k in ("uIce", "vIce", "hIceMean", "Area"):
+        e = G.rel_err(getattr(s32.variables, k).cpu().numpy(), getattr(s64.variables, k).cpu().numpy())
+        assert e <= 1e-3, (k, e)

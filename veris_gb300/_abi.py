@@ -149,6 +149,7 @@ SIGNATURES = {
     "veris_evp_solver_f32": ([_G, _Pa, _F, ctypes.c_int32, _P, _P, _P, _P, _P, _P, _S, _P], _I),
     "veris_evp_fast_workspace_bytes": ([_G, ctypes.c_int32], _S),
     "veris_evp_fast_settings_check": ([_Pa], _I),
+    "veris_evp_walk_settings_check": ([_Pa], _I),
     "veris_evp_fast_check": ([_G, _Pa, _F, _P, _P], _I),
     "veris_evp_fast_solver_f32": ([_G, _Pa, _F, ctypes.c_int32, _P, _P, _P, _P, _P, _P, _S, _P], _I),
     "veris_evp_fast_solver_f64": ([_G, _Pa, _F, ctypes.c_int32, _P, _P, _P, _P, _P, _P, _S, _P], _I),

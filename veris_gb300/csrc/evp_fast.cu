@@ -76,6 +76,8 @@ __global__ void fast_prep_kernel(VerisParams p, Fields<double> f, Dims d, int64_
     c.vOc[q] = (T)f.vOcean[o];
     c.rrAu[q] = (T)f.recip_rAu[o];
     c.rrAv[q] = (T)f.recip_rAv[o];
+    if (p.useAdaptiveEVP)   // veris/evp_solver.py:65-73, the state-only factor of alphaC
+        c.acf[q] = (T)(p.EVPcFac * f.recip_rA[o] / fmax(f.SeaIceMassC[o], 1e-4));
     if (BASAL) {
         const double A = f.Area[o];
         double b = 0.0;
@@ -200,7 +202,9 @@ static int evp_fast(const VerisGrid *g, const VerisParams *p, const VerisFieldsF
     VERIS_CHECK_GRID(g, d);
     VERIS_REQUIRE(p && vs64 && uo && vo && s1o && s2o && s12o, VERIS_ERR_ARG);
     VERIS_REQUIRE(n >= 1, VERIS_ERR_ARG);
-    if (fast_support(*p)) return VERIS_ERR_UNSUPPORTED;
+    const bool walker = sizeof(T) == 4 && (allow_tma >= 4 || allow_tma < 0);
+    if (walker ? walk_support(*p) : fast_support(*p)) return VERIS_ERR_UNSUPPORTED;
+    const bool adapt = p->useAdaptiveEVP != 0;
     FastConsts<T> c;
     T *state[2][5];
     int *status = nullptr;
@@ -236,7 +240,7 @@ static int evp_fast(const VerisGrid *g, const VerisParams *p, const VerisFieldsF
                                                {nullptr, nullptr, nullptr, nullptr, nullptr}};
                     float *const to[5] = {tslot(it + 1, 0), tslot(it + 1, 1), tslot(it + 1, 2), tslot(it + 1, 3),
                                           tslot(it + 1, 4)};
-                    if ((stt = evp_walk_subcycles(d, h, c, k, from, to, lp, 1, basal, turn,
+                    if ((stt = evp_walk_subcycles(adapt, d, h, c, k, from, to, lp, 1, basal, turn,
                                                   allow_tma < 0 ? 0 : allow_tma, walk_variant, st)) != VERIS_OK)
                         return stt;
                     done = true;
@@ -257,7 +261,7 @@ static int evp_fast(const VerisGrid *g, const VerisParams *p, const VerisFieldsF
     }
     if constexpr (sizeof(T) == 4) {
         if (allow_tma >= 4 || allow_tma < 0)   // register-walking kernel, allow_tma rows per walk (< 0: auto)
-            return evp_walk_subcycles(d, h, c, k, state, outs, d.ld, n, basal, turn, allow_tma < 0 ? 0 : allow_tma,
+            return evp_walk_subcycles(adapt, d, h, c, k, state, outs, d.ld, n, basal, turn, allow_tma < 0 ? 0 : allow_tma,
                                       walk_variant, st);
         if (allow_tma) {
             stt = evp_tma_subcycles(d, h, c, k, state, outs, d.ld, n, status, basal, turn, st);
@@ -304,6 +308,8 @@ size_t veris_evp_fast_workspace_bytes(const VerisGrid *g, int32_t elem_size) {
 }
 
 int veris_evp_fast_settings_check(const VerisParams *p) { return p ? fast_support(*p) : V_ADAPT; }
+
+int veris_evp_walk_settings_check(const VerisParams *p) { return p ? walk_support(*p) : V_SLIP; }
 
 int veris_evp_fast_check(const VerisGrid *g, const VerisParams *p, const VerisFieldsF64 *vs, int32_t *viol_device,
                          veris_stream_t s) {

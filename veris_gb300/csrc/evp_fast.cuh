@@ -46,11 +46,12 @@ struct FastConsts {
     T *mU, *cU, *AW, *uOc, *rrAu;   // cU = mU/dt * u^{n-1} + WindForcingX
     // V points
     T *mV, *cV, *AS, *vOc, *rrAv;
+    T *acf;    // adaptive EVP: EVPcFac * recip_rA / max(SeaIceMassC, 1e-4) (alphaC = sqrt(zeta * acf))
     uint32_t *flags;
     T *rdxU_x, *rdxV_x, *dxV_x, *dxU_x;   // grid lengths varying with i
     T *rdyV_y, *rdyU_y, *dyV_y, *dyU_y;   // grid lengths varying with j
 };
-constexpr int N_FAST_2D = 15;
+constexpr int N_FAST_2D = 16;
 
 __host__ __device__ inline int64_t internal_pitch(int NY) { return ((int64_t)NY + 7) / 8 * 8; }
 
@@ -67,7 +68,7 @@ size_t fast_layout(const Dims &d, char *base, FastConsts<T> *c, T *state[2][5], 
     auto take = [&](size_t n) { char *p = base ? base + off : nullptr; off += n; return p; };
     *status = reinterpret_cast<int *>(take(256));
     T **two[N_FAST_2D] = {&c->Ph, &c->mfC, &c->qrA, &c->rAz, &c->bfac, &c->mU, &c->cU, &c->AW,
-                          &c->uOc, &c->rrAu, &c->mV, &c->cV, &c->AS, &c->vOc, &c->rrAv};
+                          &c->uOc, &c->rrAu, &c->mV, &c->cV, &c->AS, &c->vOc, &c->rrAv, &c->acf};
     for (int q = 0; q < N_FAST_2D; ++q) *two[q] = reinterpret_cast<T *>(take(f2));
     c->flags = reinterpret_cast<uint32_t *>(take(fl));
     T **xs[4] = {&c->rdxU_x, &c->rdxV_x, &c->dxV_x, &c->dxU_x};
@@ -86,6 +87,7 @@ struct FastScalars {
     T halfCos, sinW;                         // 0.5 cos(turning angle), sin(turning angle)
     T dN, dS, dN2, dS2, cmin, cmin2;         // ocean drag
     T U02;                                   // basal U0^2
+    T rdt, aMin;                             // 1/dt, aEVPalphaMin (adaptive EVP)
 };
 
 template <class T>
@@ -108,6 +110,8 @@ FastScalars<T> fast_scalars(const VerisParams &p) {
     s.cmin = (T)p.cDragMin;
     s.cmin2 = (T)(p.cDragMin * p.cDragMin);
     s.U02 = (T)(p.basalDragU0 * p.basalDragU0);
+    s.rdt = (T)p.recip_deltatDyn;
+    s.aMin = (T)p.aEVPalphaMin;
     return s;
 }
 
@@ -119,6 +123,8 @@ struct FastIO {
 };
 
 int fast_support(const VerisParams &p);
+// the settings the register-walking kernel does not cover (it runs adaptive EVP)
+inline int walk_support(const VerisParams &p) { return fast_support(p) & ~V_ADAPT; }
 
 // Host helpers of the fast forms (instantiated for float and double):
 // the once-per-step fold of the constants (and of the initial state into
@@ -143,7 +149,8 @@ bool evp_tma_available();
 // budget), reading state[0] first
 // compiled forms of the register-walking kernel (evp_walk.cu)
 constexpr int N_WALK_VARIANTS = 4;
-int evp_walk_subcycles(const Dims &d, const HaloFill &h, const FastConsts<float> &c, const FastScalars<float> &k,
+int evp_walk_subcycles(bool adapt, const Dims &d, const HaloFill &h, const FastConsts<float> &c,
+                       const FastScalars<float> &k,
                        float *const state[2][5], float *const outs[5], int64_t ldo, int n, bool basal, bool turn,
                        int rows, int variant, cudaStream_t st);
 

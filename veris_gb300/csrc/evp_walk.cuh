@@ -42,12 +42,12 @@ __device__ __forceinline__ float sqrt_approx(float x) {
 
 // the ring inputs of one staged row (one column per lane)
 struct Row {
-    float u, v, s1, s2, s12, uo, vo, mf, ph, qr, rz, bf;
+    float u, v, s1, s2, s12, uo, vo, mf, ph, qr, rz, bf, ac;
     uint32_t f;
     float rdxV, rdxU, dxU, dxV;   // metrics of the row
 };
 
-template <bool BASAL>
+template <bool BASAL, bool ADAPT = false>
 __device__ __forceinline__ void load_row(Row &r, const FastConsts<float> &c, const FastIO<float> &io, int64_t lp,
                                          int gi, int gj) {
     const int64_t o = (int64_t)gi * lp + gj;
@@ -63,6 +63,7 @@ __device__ __forceinline__ void load_row(Row &r, const FastConsts<float> &c, con
     r.qr = __ldg(c.qrA + o);
     r.rz = __ldg(c.rAz + o);
     r.bf = BASAL ? __ldg(c.bfac + o) : 0.f;
+    r.ac = ADAPT ? __ldg(c.acf + o) : 0.f;
     r.f = __ldg(c.flags + o);
     r.rdxV = __ldg(c.rdxV_x + gi);
     r.rdxU = __ldg(c.rdxU_x + gi);
@@ -72,8 +73,11 @@ __device__ __forceinline__ void load_row(Row &r, const FastConsts<float> &c, con
 
 // One walk: the strip of output columns j0 .. j0+27 and output rows
 // i0 .. i0+H-1 of one subcycle, by the calling warp (all 32 lanes).
-// PRE: load the own-point constants one walk step before stage D uses them
-template <bool BASAL, bool TURN, int UNROLL, bool PRE = false>
+// PRE: load the own-point constants one walk step before stage D uses them.
+// ADAPT: adaptive EVP (veris/evp_solver.py:65-73, 97-100, 148-150): alphaC
+// from zeta at each C point, alphaZ and the U/V betas averaged from the
+// alphaC of the neighbouring C points, carried across rows like zeta.
+template <bool BASAL, bool TURN, int UNROLL, bool PRE = false, bool ADAPT = false>
 __device__ __forceinline__ void walk_strip(const Dims &d, int64_t lp, const HaloFill &h, const FastConsts<float> &c,
                                            const FastScalars<float> &k, const FastIO<float> &io, int i0, int j0,
                                            int H, int lane) {
@@ -93,11 +97,12 @@ __device__ __forceinline__ void walk_strip(const Dims &d, int64_t lp, const Halo
     float s11_a = 0.f, s11_b = 0.f, s22_a = 0.f;
     float cd_a = 0.f, cd_b = 0.f, cb_a = 0.f, cb_b = 0.f;
     float fv_a = 0.f, fv_b = 0.f, fu_a = 0.f, s12_a = 0.f;
+    float aC_a = 0.f, aC_b = 0.f;   // adaptive alphaC of rows t-2, t-3
     float o_cU = 0.f, o_cV = 0.f, o_AW = 0.f, o_AS = 0.f, o_mU = 0.f, o_mV = 0.f, o_rrAu = 0.f, o_rrAv = 0.f;
     // row indices advance by one per step: wrapped incrementally (any walk length)
     int gnext = d.wxa(i0 - 2);   // row of the next prefetch
     int gown = d.wxa(i0 - 4);    // row of this step's own-point constants (row t-2)
-    load_row<BASAL>(Pf, c, io, lp, gnext, gj);
+    load_row<BASAL, ADAPT>(Pf, c, io, lp, gnext, gj);
     const int T = H + 4;   // rows i0-2 .. i0+H+1
     // UNROLL = 4 (the rotation period) would rename the row ages instead of
     // copying them; measured slower (register pressure), the kernels use 1
@@ -105,7 +110,7 @@ __device__ __forceinline__ void walk_strip(const Dims &d, int64_t lp, const Halo
     for (int t = 0; t < T; ++t) {
         N = Pf;
         gnext = gnext + 1 == d.NX ? 0 : gnext + 1;
-        if (t + 1 < T) load_row<BASAL>(Pf, c, io, lp, gnext, gj);
+        if (t + 1 < T) load_row<BASAL, ADAPT>(Pf, c, io, lp, gnext, gj);
         // own-point constants of row t-2 (stage D)
         float cU = 0.f, cV = 0.f, AW = 0.f, AS = 0.f, mU = 0.f, mV = 0.f, rrAu = 0.f, rrAv = 0.f;
         if (PRE) {
@@ -144,7 +149,7 @@ __device__ __forceinline__ void walk_strip(const Dims &d, int64_t lp, const Halo
         const float z2n = N.rz * (e12n * e12n);
 
         float zeta_new = 0.f, s11_new = 0.f, s22_new = 0.f, cd_new = 0.f, cb_new = 0.f, fv_new = 0.f, fu_new = 0.f;
-        float s12_new = 0.f;
+        float s12_new = 0.f, aC_new = 0.f;
         if (t >= 2) {
             // ---- B: C points of row t-1 (A holds its inputs, N the next row)
             const float mInC = one_if<float>(A.f, F_INC);
@@ -157,9 +162,16 @@ __device__ __forceinline__ void walk_strip(const Dims &d, int64_t lp, const Halo
             const float zeta = __fdividef(A.ph, delta + k.deltaMin);
             zeta_new = zeta;
             const float mC = one_if<float>(A.f, F_MC);
+            float am1 = k.alpha_m1, ral = k.ralpha;
+            if (ADAPT) {
+                const float aC = fmaxf(sqrt_approx(zeta * A.ac) * mC, k.aMin);
+                aC_new = aC;
+                am1 = aC - 1.f;
+                ral = __fdividef(1.f, aC);
+            }
             const float press = k.kp * zeta * delta;
-            const float s1 = (A.s1 * k.alpha_m1 + (2.f * zeta * ep - press)) * k.ralpha * mC;
-            const float s2 = (A.s2 * k.alpha_m1 + 0.5f * zeta * em) * k.ralpha * mC;
+            const float s1 = (A.s1 * am1 + (2.f * zeta * ep - press)) * ral * mC;
+            const float s2 = (A.s2 * am1 + 0.5f * zeta * em) * ral * mC;
             s11_new = 0.5f * (s1 + s2) * dyV;
             s22_new = 0.5f * (s1 - s2) * A.dxU;
             const int oi = i0 + t - 3;
@@ -192,7 +204,13 @@ __device__ __forceinline__ void walk_strip(const Dims &d, int64_t lp, const Halo
             const int n = ((fa & F_MC) ? 1 : 0) + ((fb & F_MC) ? 1 : 0) + ((fas & F_MC) ? 1 : 0) + ((fbs & F_MC) ? 1 : 0);
             const float norm = n == 0 ? 0.f : (n == 1 ? 1.f : (n == 2 ? 0.5f : (n == 3 ? 1.f / 3.f : 0.25f)));
             const float zz = norm * ((zeta_new + zeta_a) + (up(zeta_new) + up(zeta_a)));
-            s12_new = (A.s12 * k.alpha_m1 + 0.5f * zz * e12a) * k.ralpha;
+            float am1 = k.alpha_m1, ral = k.ralpha;
+            if (ADAPT) {
+                const float aZ = 0.5f * (0.5f * (aC_new + up(aC_new)) + 0.5f * (aC_a + up(aC_a)));
+                am1 = aZ - 1.f;
+                ral = __fdividef(1.f, aZ);
+            }
+            s12_new = (A.s12 * am1 + 0.5f * zz * e12a) * ral;
             const int oi = i0 + t - 3;
             if (own_j && t <= H + 2 && oi < d.NX) io.s12o[(int64_t)oi * ldo + jl] = s12_new;
         }
@@ -201,6 +219,14 @@ __device__ __forceinline__ void walk_strip(const Dims &d, int64_t lp, const Halo
             const int oi = i0 + t - 4;
             const uint32_t f0 = B.f;
             float un, vnew;
+            // beta/dt and (beta+1)/dt at the U and V points
+            float bU = k.bU, bU1 = k.bU1, bV = k.bU, bV1 = k.bU1;
+            if (ADAPT) {
+                bU = 0.5f * (aC_a + aC_b) * k.rdt;
+                bU1 = bU + k.rdt;
+                bV = 0.5f * (aC_a + up(aC_a)) * k.rdt;
+                bV1 = bV + k.rdt;
+            }
             {   // U point
                 const float kU = k.halfCos * AW * (cd_a + cd_b);
                 float fx = cU + kU * B.uo + 0.5f * (fv_a + fv_b);
@@ -212,10 +238,10 @@ __device__ __forceinline__ void walk_strip(const Dims &d, int64_t lp, const Halo
                           one_if<float>(f0, F_LMU) * AW;
                 }
                 const float sdx = rrAu * ((s11_a - s11_b) + B.dxV * (dn(s12_a) - s12_a));
-                float den = mU * k.bU1 + kU;
+                float den = mU * bU1 + kU;
                 if (BASAL) den += 0.5f * AW * (cb_a + cb_b);
                 den = den == 0.f ? 1.f : den;
-                un = one_if<float>(f0, F_MU) * __fdividef(k.bU * mU * B.u + fx + sdx, den);
+                un = one_if<float>(f0, F_MU) * __fdividef(bU * mU * B.u + fx + sdx, den);
             }
             {   // V point
                 const float cds = up(cd_a);
@@ -229,10 +255,10 @@ __device__ __forceinline__ void walk_strip(const Dims &d, int64_t lp, const Halo
                           one_if<float>(f0, F_LMV) * AS;
                 }
                 const float sdy = rrAv * ((s22_a - up(s22_a)) + dyU * (s12_new - s12_a));
-                float den = mV * k.bU1 + kV;
+                float den = mV * bV1 + kV;
                 if (BASAL) den += 0.5f * AS * (cb_a + up(cb_a));
                 den = den == 0.f ? 1.f : den;
-                vnew = one_if<float>(f0, F_MV) * __fdividef(k.bU * mV * B.v + fy + sdy, den);
+                vnew = one_if<float>(f0, F_MV) * __fdividef(bV * mV * B.v + fy + sdy, den);
             }
             if (own_j && oi < d.NX) {
                 if (images) {
@@ -262,6 +288,8 @@ __device__ __forceinline__ void walk_strip(const Dims &d, int64_t lp, const Halo
         fv_a = fv_new;
         fu_a = fu_new;
         s12_a = s12_new;
+        aC_b = aC_a;
+        aC_a = aC_new;
         gown = gown + 1 == d.NX ? 0 : gown + 1;
     }
 }

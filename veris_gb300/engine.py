@@ -120,8 +120,12 @@ class SeaIceStep:
         self.graph = None
 
     def _fast_violations(self):
-        """Settings and state properties the fast EVP form does not cover (0: none)."""
-        bits = int(self.lib.veris_evp_fast_settings_check(ctypes.byref(self.params)))
+        """Settings and state properties the fast EVP form does not cover (0: none).
+        The float32 register-walking kernel also runs the adaptive EVP."""
+        walk = self.precision == "f32" and self.f32_kernel == "walk"
+        check_settings = (self.lib.veris_evp_walk_settings_check if walk else
+                          self.lib.veris_evp_fast_settings_check)
+        bits = int(check_settings(ctypes.byref(self.params)))
         flag = torch.zeros(1, dtype=torch.int32, device=self.device)
         check("evp_fast_check", self.lib.veris_evp_fast_check(*self._refs(self.f64), flag.data_ptr(),
                                                               self.stream))
