@@ -54,6 +54,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true", help="skip the float64 comparison leg")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--adaptive", action="store_true", help="adaptive EVP (useAdaptiveEVP)")
     ap.add_argument("--no-routines", action="store_true",
                     help="skip the free-drift, bulk-formula and residual measurements")
     ap.add_argument("--routines-only", action="store_true",
@@ -329,6 +330,8 @@ def run_ours(args):
         sett.nEVPsteps = args.subcycles
     if args.evp_alpha_beta:
         sett.evpAlpha = sett.evpBeta = float(args.evp_alpha_beta)
+    if args.adaptive:
+        sett.useAdaptiveEVP = True
     n_sub = sett.nEVPsteps
     cells = c["nx"] * c["ny"]
 
@@ -395,6 +398,7 @@ def run_ours(args):
             "dtype": args.precision, "data": "synthetic",
             "config": {"workload": args.config, "nx": c["nx"], "ny": c["ny"], "subcycles": n_sub,
                        "evpAlpha": float(sett.evpAlpha), "evpBeta": float(sett.evpBeta),
+                       "adaptive_evp": bool(sett.useAdaptiveEVP),
                        "dt_s": c["dt"], "cells": cells, "precision": args.precision,
                        "parallelism": "replicas" if ws > 1 else "single-gpu",
                        "l2": "flushed before every timed step (512 MiB write)",
