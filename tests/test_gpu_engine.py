@@ -272,3 +272,24 @@ def test_engine_f32_runs_adaptive_evp_in_the_walk():
     for k in ("uIce", "vIce", "hIceMean", "Area"):
         e = G.rel_err(getattr(s32.variables, k).cpu().numpy(), getattr(s64.variables, k).cpu().numpy())
         assert e <= 1e-3, (k, e)
+
+
+def test_engine_free_drift_step():
+    """useFreedrift without useEVP: the engine's step runs free drift, like the
+    drop-in sequence (IceVelocities), and keeps the stresses."""
+    from veris_gb300 import model
+    from veris_gb300.engine import SeaIceStep
+    from veris_gb300.state import VerisState
+    from veris_gb300.synthetic import config_settings, make_state
+    sett = config_settings("c3_1deg", useFreedrift=True, useEVP=False)
+    arrays = make_state(96, 64, seed=5, init_velocity=0.05, init_stress=500.0)
+    ref = VerisState.from_numpy(arrays, sett)
+    model.step(ref)
+    for precision, tol in (("f64", 1e-10), ("f32", 1e-4)):
+        st = VerisState.from_numpy(arrays, sett)
+        SeaIceStep(st, precision=precision).step()
+        torch.cuda.synchronize()
+        for k in ("uIce", "vIce", "hIceMean", "Area", "TSurf"):
+            e = G.rel_err(getattr(st.variables, k).cpu().numpy(), getattr(ref.variables, k).cpu().numpy())
+            assert e <= tol, (precision, k, e)
+        assert torch.equal(st.variables.sigma1, torch.as_tensor(arrays["sigma1"], device="cuda"))

@@ -170,7 +170,23 @@ class SeaIceStep:
         if evp_events:
             evp_events[0].record()
         ws = (self.ws_evp.data_ptr(), self.ws_evp.numel(), st)
-        if self.precision == "f64" and self.evp_tape is not None:
+        sett = self.state.settings
+        if sett.useFreedrift and not sett.useEVP:
+            # veris/dynsolver.py:93-97: free-drift velocities, stresses as they are
+            check("freedrift_solver", lib.veris_freedrift_solver_f64(*r64, self.evp_out[0].data_ptr(),
+                                                                      self.evp_out[1].data_ptr(), st))
+            n += 1
+            if evp_events:
+                evp_events[1].record()
+            v.uIce.copy_(self.evp_out[0])
+            v.vIce.copy_(self.evp_out[1])
+            if self.precision == "f32":
+                for name in ("hIceMean", "hSnowMean", "Area"):
+                    self._to32(getattr(v, name), self.v32[name])
+                self._to32(v.uIce, self.evp_out32[0])
+                self._to32(v.vIce, self.evp_out32[1])
+                n += 5
+        elif self.precision == "f64" and self.evp_tape is not None:
             # keep every subcycle's state (gradients of many steps); eager only
             tape = self.evp_tape
             check("evp_tape", lib.veris_evp_fast_tape_f64(*r64, self.n_sub, *[t.data_ptr() for t in self.evp_out],
