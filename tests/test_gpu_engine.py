@@ -97,6 +97,42 @@ def test_host_coupled_step_roundtrip():
     assert host.h2d_bytes == len(host.inputs) * st.variables.iceMask.numel() * 8
 
 
+@pytest.mark.parametrize("precision", ("f64", "f32"))
+def test_host_coupled_graph_equals_plain_steps(precision):
+    """The captured host exchange (side-stream uploads of the Growth forcing,
+    early downloads of the dynamics outputs) gives the host exactly what an
+    engine step followed by plain copies gives, step after step, with new
+    host inputs every step."""
+    from veris_gb300.engine import SeaIceStep
+    from veris_gb300.host import HostCoupledStep
+    from veris_gb300.state import VerisState
+    from veris_gb300.synthetic import config_settings, make_state
+    arrays = make_state(120, 80, seed=2, init_velocity=0.05)
+    sett = config_settings("c3_1deg", nEVPsteps=40)
+    a = VerisState.from_numpy(arrays, sett)
+    b = VerisState.from_numpy(arrays, sett)
+    host = HostCoupledStep(SeaIceStep(a, precision=precision))
+    eng_b = SeaIceStep(b, precision=precision)
+    h_in, h_out = host.host_buffers()
+    rng = np.random.default_rng(0)
+    for k in range(4):
+        # the host model changes its forcing between steps
+        for n in ("Qnet", "ATemp", "uWind", "theta"):
+            h_in[n].mul_(float(1.0 + 0.01 * rng.standard_normal()))
+        host.step(h_in, h_out)
+        for n in host.inputs:
+            getattr(b.variables, n).copy_(h_in[n].cuda())
+        eng_b.step()
+        torch.cuda.synchronize()
+        for n in host.outputs:
+            assert torch.equal(h_out[n], getattr(b.variables, n).cpu()), (k, n)
+        # the host keeps stepping from what the step returned
+        for n in host.outputs:
+            if n in h_in:
+                h_in[n].copy_(h_out[n])
+    assert len(host.graphs) == 1
+
+
 @pytest.mark.parametrize("case", G.CASES)
 def test_fast_form_support_and_parity(case):
     """The fast EVP form covers the default rheology; in float64 it matches

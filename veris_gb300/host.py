@@ -21,16 +21,69 @@ HOST_OUTPUTS = ("hIceMean", "hSnowMean", "Area", "TSurf", "uIce", "vIce", "sigma
                 "recip_hIceMean", "OceanStressU", "OceanStressV", "os_hIceMean", "os_hSnowMean")
 
 
-class HostCoupledStep:
-    """Runs a ``SeaIceStep`` on host arrays: upload, step, download."""
+# inputs only Growth reads (veris/growth.py, veris/solve4temp.py): their
+# upload overlaps the dynamics
+LATE_INPUTS = ("theta", "ocSalt", "Qnet", "Qsw", "SWdown", "LWdown", "ATemp", "aqh", "precip", "snowfall",
+               "evap", "runoff")
+# outputs final once the ice velocities and the ocean stress are: their
+# download overlaps advection and Growth
+EARLY_OUTPUTS = ("uIce", "vIce", "sigma1", "sigma2", "sigma12", "OceanStressU", "OceanStressV")
 
-    def __init__(self, engine, inputs=HOST_INPUTS, outputs=HOST_OUTPUTS):
+
+class HostCoupledStep:
+    """Runs a ``SeaIceStep`` on host arrays: upload, step, download.
+
+    With pinned host buffers the whole exchange is one CUDA graph per buffer
+    set: the inputs the dynamics read are uploaded first, the forcing only
+    Growth reads is uploaded on a second stream while the dynamics run, and
+    the velocities, stresses and ocean stress are downloaded on a third
+    stream while advection and Growth run; the rest follows Growth.  Other
+    host buffers take the same order eagerly on one stream."""
+
+    def __init__(self, engine, inputs=HOST_INPUTS, outputs=HOST_OUTPUTS, graph=True):
         self.engine = engine
         self.inputs = tuple(inputs)
         self.outputs = tuple(outputs)
         v = engine.state.variables
         self.h2d_bytes = sum(getattr(v, n).numel() * getattr(v, n).element_size() for n in self.inputs)
         self.d2h_bytes = sum(getattr(v, n).numel() * getattr(v, n).element_size() for n in self.outputs)
+        held = set(engine.forcing or ())   # restored on the main stream at the start of the step
+        self.late = tuple(n for n in self.inputs if n in LATE_INPUTS and n not in held)
+        self.early_out = tuple(n for n in self.outputs if n in EARLY_OUTPUTS)
+        self.use_graph = graph
+        self.graphs = {}
+        self._side_in = torch.cuda.Stream(engine.device)
+        self._side_out = torch.cuda.Stream(engine.device)
+
+    def _enqueue(self, h_in, h_out, overlap):
+        v = self.engine.state.variables
+        main = torch.cuda.current_stream(self.engine.device)
+        late = self.late if overlap else ()
+        early_out = self.early_out if overlap else ()
+        for n in self.inputs:
+            if n not in late:
+                getattr(v, n).copy_(h_in[n], non_blocking=True)
+        if late:
+            self._side_in.wait_stream(main)
+            with torch.cuda.stream(self._side_in):
+                for n in late:
+                    getattr(v, n).copy_(h_in[n], non_blocking=True)
+
+        def mark(name):
+            if name == "ocean_stress" and early_out:
+                self._side_out.wait_stream(main)
+                with torch.cuda.stream(self._side_out):
+                    for n in early_out:
+                        h_out[n].copy_(getattr(v, n), non_blocking=True)
+            elif name == "clean_up" and late:   # Growth comes next
+                main.wait_stream(self._side_in)
+
+        self.engine.launches_per_step = self.engine._enqueue(marks=mark)
+        for n in self.outputs:
+            if n not in early_out:
+                h_out[n].copy_(getattr(v, n), non_blocking=True)
+        if early_out:
+            main.wait_stream(self._side_out)
 
     def host_buffers(self):
         """Pinned host copies of the current device state (inputs, outputs)."""
@@ -43,11 +96,27 @@ class HostCoupledStep:
     def step(self, h_in, h_out):
         """One step from host arrays ``h_in`` into host arrays ``h_out``;
         returns after the results are in host memory."""
-        v = self.engine.state.variables
-        for n in self.inputs:
-            getattr(v, n).copy_(h_in[n], non_blocking=True)
-        self.engine.step()
-        for n in self.outputs:
-            h_out[n].copy_(getattr(v, n), non_blocking=True)
-        torch.cuda.current_stream(self.engine.device).synchronize()
+        dev = self.engine.device
+        pinned = all(h_in[n].is_pinned() for n in self.inputs) and all(h_out[n].is_pinned() for n in self.outputs)
+        if not (self.use_graph and pinned):
+            self._enqueue(h_in, h_out, overlap=pinned)
+            torch.cuda.current_stream(dev).synchronize()
+            return h_out
+        key = (tuple(h_in[n].data_ptr() for n in self.inputs), tuple(h_out[n].data_ptr() for n in self.outputs))
+        g = self.graphs.get(key)
+        if g is None:
+            self._enqueue(h_in, h_out, overlap=True)   # the step itself, eagerly, then the capture of the next
+            torch.cuda.synchronize(dev)
+            g = torch.cuda.CUDAGraph()
+            s = torch.cuda.Stream(dev)
+            s.wait_stream(torch.cuda.current_stream(dev))
+            with torch.cuda.stream(s):
+                with torch.cuda.graph(g, stream=s):
+                    self._enqueue(h_in, h_out, overlap=True)
+            torch.cuda.current_stream(dev).wait_stream(s)
+            torch.cuda.synchronize(dev)
+            self.graphs[key] = g
+            return h_out
+        g.replay()
+        torch.cuda.current_stream(dev).synchronize()
         return h_out
