@@ -84,6 +84,8 @@ def parse():
     ap.add_argument("--ensemble", action="store_true",
                     help="the batched ensemble (512 members of uneven sizes) against sequential launches")
     ap.add_argument("--members", type=int, default=512)
+    ap.add_argument("--ens-shape", type=int, default=None, help="ensemble tile/walk shape (skips tuning)")
+    ap.add_argument("--ens-blocks-per-sm", type=int, default=4)
     return ap.parse_args()
 
 
@@ -720,7 +722,11 @@ def run_ensemble(args):
     cells = sum(sp["nx"] * sp["ny"] for sp in specs)
     ens = Ensemble(members, n_sub)
     ens.step()                               # first step: eager, configures the kernels
-    tuned = autotune.tune(ens, use_cache=False)
+    if args.ens_shape is not None:           # a fixed launch (profiling): no tuning
+        ens.set_launch(args.ens_shape, args.ens_blocks_per_sm)
+        tuned = {"shape": args.ens_shape, "blocks_per_sm": args.ens_blocks_per_sm, "trials": [], "fixed": True}
+    else:
+        tuned = autotune.tune(ens, use_cache=False)
     ens.capture()
     for _ in range(max(0, args.warmup - 1)):
         ens.step()
@@ -761,7 +767,7 @@ def run_ensemble(args):
                        "steps": n_steps, "min_member": [min(sp["nx"] for sp in specs), min(sp["ny"] for sp in specs)],
                        "max_member": [max(sp["nx"] for sp in specs), max(sp["ny"] for sp in specs)],
                        "graph": "one CUDA graph per ensemble step", "tiles_per_subcycle": ens.total_tiles},
-            "ms_per_step": ms / n_steps, "tuned": {k: tuned[k] for k in ("shape", "blocks_per_sm", "ms_per_subcycle")},
+            "ms_per_step": ms / n_steps, "tuned": {k: tuned.get(k) for k in ("shape", "blocks_per_sm", "ms_per_subcycle", "fixed")},
             "tuning_trials": tuned.get("trials"),
             "sequential": {"value": seq_value, "ms_per_step": seq_ms,
                            "what": "one veris_evp_fast_solver_f32 call per member, eager, one after another"},
