@@ -156,15 +156,34 @@ __device__ void solve4temp_multi(const VerisParams &p, const S4TIn &x, const S &
     // iteration still converges to the float64 root); dual numbers keep the
     // exact step so that the adjoint differentiates a smooth map.  A
     // category stops once an update moves T by less than 4e-7 T.
+    //
+    // The final evaluation (float64 only) at a converged category's T, at
+    // most 4e-7 T from the last Newton evaluation at t: Fc and the T^4 and
+    // sensible terms are evaluated exactly; qs(T) = qs(t) + qs'(t) (T - t),
+    // whose error qs'' (T - t)^2 / 2 ~ 3e-11 qs (d ln qs / dT = aa1 ln10 / T^2
+    // ~ 0.08 / K) is far inside the parity of the fixed six iterations; this
+    // drops the exp2 and the two divisions of that evaluation.
     const double aa1l2 = aa1 * 3.32192809488736234787;   // aa1 log2(10)
     const double qnum = bb1 * cc0, qsub = one_m_bb1 * cc0;
+    double qsv[NC], dqsv[NC], tv[NC];
+    bool conv[NC];
+#pragma unroll
+    for (int l = 0; l < NC; ++l) conv[l] = false;
     auto fluxes = [&](bool newton) {
 #pragma unroll
         for (int l = 0; l < NC; ++l) {
             if (newton && !moving[l]) continue;
             const S t1 = T[l];
-            const S rt = 1.0 / t1;
             const S t2 = t1 * t1, t3 = t2 * t1, t4 = t2 * t2;
+            if constexpr (std::is_same<S, double>::value) {
+                if (!newton && conv[l]) {
+                    const double qs = qsv[l] + dqsv[l] * (t1 - tv[l]);
+                    Fc[l] = k[l] * (x.TempFrz - t1);
+                    Fia[l] = lwabs[l] + t4 * d3[l] + d1ug * (t1 - Ta) + d1iug * (qs - x.aqh);
+                    continue;
+                }
+            }
+            const S rt = 1.0 / t1;
             const S c3 = vexp2(aa1l2 * rt);
             const S qs = qnum / (c3 * Pa - qsub);
             Fc[l] = ice[l] ? k[l] * (x.TempFrz - t1) : S(0.0);
@@ -178,6 +197,9 @@ __device__ void solve4temp_multi(const VerisParams &p, const S4TIn &x, const S &
                     const double dqs = (double)((float)(cc1 * c3) * rden * rden * (float)(rt * rt));
                     const double dF = 4 * d3[l] * t3 + d1ug + d1iug * dqs;
                     Tn = ice[l] ? t1 + (Fc[l] - Fia[l]) * (double)__frcp_rn((float)(k[l] + dF)) : 0.0;
+                    qsv[l] = qs;   // and d qs / dT = dqs, for the final evaluation
+                    dqsv[l] = dqs;
+                    tv[l] = t1;
                 } else {
                     const S dqs = cc1 * c3 * (rt * rt) / (den * den);
                     const S dF = ice[l] ? 4 * d3[l] * t3 + d1ug + d1iug * dqs : S(0.0);
@@ -190,7 +212,10 @@ __device__ void solve4temp_multi(const VerisParams &p, const S4TIn &x, const S &
                 // C = F''/2F' ~ 1e-3 / K (at most ~1e-2 / K with the latent
                 // heat term), i.e. ~1e-10 K, 4e-13 of T: far inside the
                 // float64 parity of the fixed six iterations
-                if (vfabs(val(Tn) - val(t1)) <= 4e-7 * val(t1)) moving[l] = false;
+                if (vfabs(val(Tn) - val(t1)) <= 4e-7 * val(t1)) {
+                    moving[l] = false;
+                    conv[l] = ice[l];
+                }
                 T[l] = Tn;
             }
         }
