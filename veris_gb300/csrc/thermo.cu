@@ -119,6 +119,12 @@ __device__ void solve4temp_multi(const VerisParams &p, const S4TIn &x, const S &
         for (int l = 0; l < NC; ++l) e1[l] = vexp(-1.5 * hI[l]);
     }
     const double rhCut = 1.0 / p.hCut;
+    // the categories scale ice and snow thickness alike (veris/growth.py:62-71):
+    // with NC = 5, hI[l] = (2l+1) hI[0] and hS[l] = (2l+1) hS[0], so the
+    // effective conductivity is k[0] / (2l+1): one division for the five
+    S k0 = S(0.0);
+    if constexpr (NC == 5)
+        k0 = hI[0] > 0 ? p.iceConduct * p.snowConduct / (p.snowConduct * hI[0] + p.iceConduct * hS[0]) : S(0.0);
 #pragma unroll
     for (int l = 0; l < NC; ++l) {
         ice[l] = hI[l] > 0;
@@ -139,7 +145,12 @@ __device__ void solve4temp_multi(const VerisParams &p, const S4TIn &x, const S &
         if (snow) pen = S(0.0);
         oPen[l] = ice[l] ? -(1 - alb) * pen * x.SWdown : S(0.0);
         const S absSW = ice[l] ? (1 - alb) * (1 - pen) * x.SWdown : S(0.0);
-        k[l] = ice[l] ? p.iceConduct * p.snowConduct / (p.snowConduct * hI[l] + p.iceConduct * hS[l]) : S(0.0);
+        if constexpr (NC == 5) {
+            constexpr double inv_odd[5] = {1.0, 1.0 / 3.0, 1.0 / 5.0, 1.0 / 7.0, 1.0 / 9.0};
+            k[l] = ice[l] ? k0 * inv_odd[l] : S(0.0);
+        } else {
+            k[l] = ice[l] ? p.iceConduct * p.snowConduct / (p.snowConduct * hI[l] + p.iceConduct * hS[l]) : S(0.0);
+        }
         lwabs[l] = -lw - absSW;
         T[l] = Tin;
     }
@@ -269,13 +280,31 @@ struct GrowthOut {
     S h, hs, A, TSurf, EmPmR, forc_salt, Qsw, Qnet, load, pen, rh;
 };
 
+// step constants of Growth, formed once on the host (float64 divisions cost
+// about ten fused multiply-adds each on GB300's float64 pipe)
+struct GrowthK {
+    double qi, qs;        // 1 / (rho lhFusion) of ice and snow
+    double rqi, rqs;      // rho lhFusion of ice and snow
+    double rf2s;          // 1 / rhoFresh2rhoSnow
+};
+
+static GrowthK growth_k(const VerisParams &p) {
+    GrowthK k;
+    k.qi = 1 / (p.rhoIce * p.lhFusion);
+    k.qs = 1 / (p.rhoSnow * p.lhFusion);
+    k.rqi = p.rhoIce * p.lhFusion;
+    k.rqs = p.rhoSnow * p.lhFusion;
+    k.rf2s = 1 / p.rhoFresh2rhoSnow;
+    return k;
+}
+
 // veris/growth.py:8-397 for one point, from the ice state (h, hs, A, TSurf)
 // and the forcing of point o
 template <class S>
-__device__ GrowthOut<S> growth_point(const VerisParams &p, const Fields<double> &f, int64_t o, S hIn, S hsIn,
-                                     S AIn, S TSurfIn) {
-    const double qi = 1 / (p.rhoIce * p.lhFusion);
-    const double qs = 1 / (p.rhoSnow * p.lhFusion);
+__device__ GrowthOut<S> growth_point(const VerisParams &p, const GrowthK &gk, const Fields<double> &f, int64_t o,
+                                     S hIn, S hsIn, S AIn, S TSurfIn) {
+    const double qi = gk.qi;
+    const double qs = gk.qs;
     const bool noIce = hIn == 0 || AIn == 0;
     const double keep = noIce ? 0.0 : 1.0;
     const S h0 = hIn * keep, hs0 = hsIn * keep, A0 = AIn * keep;
@@ -344,7 +373,7 @@ __device__ GrowthOut<S> growth_point(const VerisParams &p, const Fields<double> 
     const S potMelt = potMeltRate * p.deltatTherm;
     const bool allMelt = potMelt >= hs0;
     const S meltRate = allMelt ? hs0 * p.recip_deltatTherm : potMeltRate;
-    const S toSnow = allMelt ? -hs0 * p.recip_deltatTherm / qs : Fia;
+    const S toSnow = allMelt ? -hs0 * p.recip_deltatTherm * gk.rqs : Fia;
     Fia = Fia - toSnow;
     const S gSurf = Fia * qi;
     const S gNet = (gUnder + gSurf) * rregA;
@@ -392,7 +421,7 @@ __device__ GrowthOut<S> growth_point(const VerisParams &p, const Fields<double> 
     g.Qsw = pen * A0 + __ldg(f.Qsw + o) * (1 - A0);
     const S dH = h - h0;
     const S melted = hs0 + snowAccOverIce - hs;
-    const S E_ice = dH / qi;
+    const S E_ice = dH * gk.rqi;
     const S E_out = (A0 * (Fia + Fio + pen) + (1 - A0) * Qnet_in) * p.deltatTherm;
     g.Qnet = (E_out - E_ice) * p.recip_deltatTherm;
     const double sal_fac = (ocSalt > 0 && ocSalt > p.saltIce_ref) ? (1 - p.saltIce_ref / ocSalt) : 1.0;
@@ -400,11 +429,11 @@ __device__ GrowthOut<S> growth_point(const VerisParams &p, const Fields<double> 
     const double salt_ref = dmin(p.saltIce_ref, ocSalt);
     const double osh = __ldg(f.os_hIceMean + o), oshs = __ldg(f.os_hSnowMean + o);
     const S saltflux = (dH + osh) * salt_ref * mask * p.rhoIce * p.recip_deltatTherm;
-    const S fw_snow = melted / p.rhoFresh2rhoSnow;
+    const S fw_snow = melted * gk.rf2s;
     g.EmPmR = mask * ((-__ldg(f.evap + o) - precip) * (1 - A0) - rainToSea * A0 - __ldg(f.runoff + o) -
-                      (fw_ice + fw_snow) / p.deltatTherm) * p.rhoFresh +
+                      (fw_ice + fw_snow) * p.recip_deltatTherm) * p.rhoFresh +
               mask * (osh * p.rhoIce + oshs * p.rhoSnow) * p.recip_deltatTherm;
-    g.forc_salt = g.EmPmR * ocSalt / p.rhoFresh + saltflux;
+    g.forc_salt = g.EmPmR * ocSalt * p.recip_rhoFresh + saltflux;
     g.load = h * p.rhoIce + hs * p.rhoSnow;
     g.pen = pen;
     return g;
@@ -439,11 +468,12 @@ struct GrowthPtrs {
     double *h, *hs, *A, *TSurf, *EmPmR, *forc_salt, *Qsw, *Qnet, *load, *pen, *rh;
 };
 
-__global__ void __launch_bounds__(128) growth_kernel(VerisParams p, Fields<double> f, Dims d, GrowthPtrs out) {
+__global__ void __launch_bounds__(128) growth_kernel(VerisParams p, GrowthK gk, Fields<double> f, Dims d,
+                                                     GrowthPtrs out) {
     const int j = blockIdx.x * 32 + threadIdx.x, i = blockIdx.y * 4 + threadIdx.y;
     if (i >= d.NX || j >= d.NY) return;
     const int64_t o = d.raw(i, j);
-    const GrowthOut<double> g = growth_point<double>(p, f, o, __ldg(f.hIceMean + o), __ldg(f.hSnowMean + o),
+    const GrowthOut<double> g = growth_point<double>(p, gk, f, o, __ldg(f.hIceMean + o), __ldg(f.hSnowMean + o),
                                                      __ldg(f.Area + o), __ldg(f.TSurf + o));
     out.h[o] = g.h;
     out.hs[o] = g.hs;
@@ -459,7 +489,7 @@ __global__ void __launch_bounds__(128) growth_kernel(VerisParams p, Fields<doubl
 }
 
 // adjoint of growth for the ice state: l_in = J^T l_out over (h, hs, A, TSurf)
-__global__ void __launch_bounds__(128) growth_adjoint_kernel(VerisParams p, Fields<double> f, Dims d,
+__global__ void __launch_bounds__(128) growth_adjoint_kernel(VerisParams p, GrowthK gk, Fields<double> f, Dims d,
                                                              const double *lh, const double *lhs, const double *lA,
                                                              const double *lT, double *oh, double *ohs, double *oA,
                                                              double *oT) {
@@ -467,7 +497,7 @@ __global__ void __launch_bounds__(128) growth_adjoint_kernel(VerisParams p, Fiel
     if (i >= d.NX || j >= d.NY) return;
     const int64_t o = d.raw(i, j);
     using D = Dual<4>;
-    const GrowthOut<D> g = growth_point<D>(p, f, o, D::var(f.hIceMean[o], 0), D::var(f.hSnowMean[o], 1),
+    const GrowthOut<D> g = growth_point<D>(p, gk, f, o, D::var(f.hIceMean[o], 0), D::var(f.hSnowMean[o], 1),
                                            D::var(f.Area[o], 2), D::var(f.TSurf[o], 3));
     const double l0 = lh[o], l1 = lhs[o], l2 = lA[o], l3 = lT[o];
     double r[4];
@@ -505,7 +535,7 @@ int veris_growth_adjoint_f64(const VerisGrid *g, const VerisParams *p, const Ver
     VERIS_REQUIRE(p && vs && lh && lhs && lA && lT && oh && ohs && oA && oT, VERIS_ERR_ARG);
     VERIS_REQUIRE(p->nITC >= 1 && p->nITC <= 64, VERIS_ERR_ARG);
     dim3 gr((d.NY + 31) / 32, (d.NX + 3) / 4);
-    growth_adjoint_kernel<<<gr, dim3(32, 4), 0, (cudaStream_t)s>>>(*p, *reinterpret_cast<const Fields<double> *>(vs),
+    growth_adjoint_kernel<<<gr, dim3(32, 4), 0, (cudaStream_t)s>>>(*p, growth_k(*p), *reinterpret_cast<const Fields<double> *>(vs),
                                                                    d, lh, lhs, lA, lT, oh, ohs, oA, oT);
     return launch_status();
 }
@@ -520,7 +550,7 @@ int veris_growth_f64(const VerisGrid *g, const VerisParams *p, const VerisFields
     VERIS_REQUIRE(p->nITC >= 1 && p->nITC <= 64, VERIS_ERR_ARG);
     GrowthPtrs out{h, hs, A, TSurf, EmPmR, forc_salt, Qsw, Qnet, load, pen, rh};
     dim3 gr((d.NY + 31) / 32, (d.NX + 3) / 4);
-    growth_kernel<<<gr, dim3(32, 4), 0, (cudaStream_t)s>>>(*p, *reinterpret_cast<const Fields<double> *>(vs), d,
+    growth_kernel<<<gr, dim3(32, 4), 0, (cudaStream_t)s>>>(*p, growth_k(*p), *reinterpret_cast<const Fields<double> *>(vs), d,
                                                             out);
     return launch_status();
 }
