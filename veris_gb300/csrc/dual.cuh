@@ -97,6 +97,14 @@ __device__ inline Dual<N> vsqrt(const Dual<N> &a) {
     return r;
 }
 template <int N>
+__device__ inline Dual<N> vrsqrt(const Dual<N> &a) {
+    Dual<N> r;
+    r.v = ::rsqrt(a.v);
+    const double g = -0.5 * r.v * r.v * r.v;   // d x^(-1/2) / dx
+    for (int k = 0; k < N; ++k) r.d[k] = g * a.d[k];
+    return r;
+}
+template <int N>
 __device__ inline Dual<N> vexp(const Dual<N> &a) {
     Dual<N> r;
     r.v = ::exp(a.v);
@@ -133,6 +141,7 @@ __device__ inline Dual<N> vfabs(const Dual<N> &a) {
 
 // the same names for plain float64, so templated code calls one spelling
 __device__ inline double vsqrt(double x) { return ::sqrt(x); }
+__device__ inline double vrsqrt(double x) { return ::rsqrt(x); }
 __device__ inline double vexp(double x) { return ::exp(x); }
 __device__ inline double vexp10(double x) { return ::exp10(x); }
 __device__ inline double vexp2(double x) { return ::exp2(x); }

@@ -91,6 +91,17 @@ __device__ S4TOut solve4temp_point(const VerisParams &p, const S4TIn &x) {
 // dependency chains interleave.
 // S is double, or a dual number when the adjoint needs the derivatives with
 // respect to the ice state (branches follow the values either way).
+// 1/x for a float64 x inside the float32 range (a temperature, or the
+// saturation denominator c3 Pa - (1-bb1) cc0 ~ 1e15..1e17 here): the
+// float32 reciprocal refined by two Newton-Raphson steps r <- r + r (1 - x r),
+// relative error ~2^-23 -> ~2^-46 -> float64 rounding
+__device__ __forceinline__ double recip_nr(double x) {
+    double r = (double)__frcp_rn((float)x);
+    r = fma(r, fma(-x, r, 1.0), r);
+    r = fma(r, fma(-x, r, 1.0), r);
+    return r;
+}
+
 template <int NC, class S>
 __device__ void solve4temp_multi(const VerisParams &p, const S4TIn &x, const S &Tin, const S *hI, const S *hS,
                                  S *oT, S *oFio, S *oFia, S *oPen) {
@@ -194,9 +205,16 @@ __device__ void solve4temp_multi(const VerisParams &p, const S4TIn &x, const S &
                     continue;
                 }
             }
-            const S rt = 1.0 / t1;
-            const S c3 = vexp2(aa1l2 * rt);
-            const S qs = qnum / (c3 * Pa - qsub);
+            S rt, qs, c3;
+            if constexpr (std::is_same<S, double>::value) {
+                rt = recip_nr(t1);
+                c3 = vexp2(aa1l2 * rt);
+                qs = qnum * recip_nr(c3 * Pa - qsub);
+            } else {
+                rt = 1.0 / t1;
+                c3 = vexp2(aa1l2 * rt);
+                qs = qnum / (c3 * Pa - qsub);
+            }
             Fc[l] = ice[l] ? k[l] * (x.TempFrz - t1) : S(0.0);
             const S Flh = ice[l] ? d1iug * (qs - x.aqh) : S(0.0);
             Fia[l] = ice[l] ? (lwabs[l] + t4 * d3[l] + d1ug * (t1 - Ta) + Flh) : S(0.0);
@@ -309,10 +327,9 @@ __device__ GrowthOut<S> growth_point(const VerisParams &p, const GrowthK &gk, co
     const double keep = noIce ? 0.0 : 1.0;
     const S h0 = hIn * keep, hs0 = hsIn * keep, A0 = AIn * keep;
     const bool isIce = h0 > 0;
-    const S regA = vsqrt(A0 * A0 + p.Area_reg);
-    const S rregA = 1 / regA;
+    const S rregA = vrsqrt(A0 * A0 + p.Area_reg);
     S hIa = isIce ? h0 * rregA : S(0.0);
-    const S rhIa = A0 / vsqrt(h0 * h0 + p.hIce_reg);
+    const S rhIa = A0 * vrsqrt(h0 * h0 + p.hIce_reg);
     const S hSa = isIce ? hs0 * rregA : S(0.0);
     hIa = smax(hIa, S(0.05));
 
@@ -413,7 +430,7 @@ __device__ GrowthOut<S> growth_point(const VerisParams &p, const GrowthK &gk, co
     const S flood = smax(S(0.0), hsub - h);
     h = h + flood;
     hs = hs - flood * p.rhoIce2rhoSnow;
-    g.rh = 1 / vsqrt(h * h + p.hIce_reg);
+    g.rh = vrsqrt(h * h + p.hIce_reg);
     g.h = h;
     g.hs = hs;
     g.A = A;
