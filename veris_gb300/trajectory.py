@@ -137,12 +137,17 @@ class Trajectory:
         tape_bytes = int(self.lib.veris_evp_tape_bytes(g, esize, self.eng.n_sub))
         if tape == "auto":
             free = torch.cuda.mem_get_info(dev)[0]
-            tape = self.snaps == self.n - 1 and self.n * tape_bytes <= tape_memory_fraction * free
+            tape = self.snaps == self.n - 1 and (self.n + 1) * tape_bytes <= tape_memory_fraction * free
         elif tape and self.snaps != self.n - 1:
             raise ValueError("taping needs every step snapshotted (snapshots=None)")
         tdt = torch.float32 if f32 else torch.float64
         self.tapes = ([torch.empty(tape_bytes // esize, dtype=tdt, device=dev) for _ in range(self.n)]
                       if tape else None)
+        # the taped step is one CUDA graph writing this staging tape, copied
+        # to the step's own tape after each replay (a graph holds fixed
+        # addresses; the copy costs less than launching the step eagerly)
+        self.tape_stage = torch.empty_like(self.tapes[0]) if tape else None
+        self._tape_graph = None
         if tape:
             wsb = (self.lib.veris_evp_adjoint_taped_workspace_bytes_f32(g, self.eng.n_sub) if f32 else
                    self.lib.veris_evp_adjoint_taped_workspace_bytes(g, self.eng.n_sub))
@@ -183,6 +188,20 @@ class Trajectory:
             x = self._save()
             self.eng.capture()          # its eager warm-up step moves the state
             self._load(x)
+            if self.tapes is not None:
+                dev = self.eng.device
+                g = torch.cuda.CUDAGraph()
+                s = torch.cuda.Stream(dev)
+                s.wait_stream(torch.cuda.current_stream(dev))
+                self.eng.evp_tape = self.tape_stage
+                try:
+                    with torch.cuda.stream(s):
+                        with torch.cuda.graph(g, stream=s):
+                            self.eng.launches_per_step = self.eng._enqueue()
+                finally:
+                    self.eng.evp_tape = None
+                torch.cuda.current_stream(dev).wait_stream(s)
+                self._tape_graph = g
             self._graph_ok = True
 
     # ---------------------------------------------------------- forward
@@ -201,9 +220,8 @@ class Trajectory:
             t -= 1
         for k in range(1, self.n + 1):
             if self.tapes is not None:
-                self.eng.evp_tape = self.tapes[k - 1]
-                self.eng.launches_per_step = self.eng._enqueue()
-                self.eng.evp_tape = None
+                self._tape_graph.replay()
+                self.tapes[k - 1].copy_(self.tape_stage)
             else:
                 self.eng.step()
             if k in keep:
