@@ -1,0 +1,108 @@
+"""The path at the workloads' full sizes.
+
+* 1440 x 720 (the quarter-degree workload): one whole step against the
+  oracle (two subcycles keep the NumPy side to seconds), bar 1e-10.
+* 3600 x 1800 (the tenth-degree workload), properties that do not depend on
+  an oracle: the float64 fast EVP form equals the plain float64 kernel to
+  1e-10, the float32 walk equals the shared-memory float32 form to 1e-5, a
+  float32 engine step is bit-reproducible, the halo fill is idempotent and
+  the deterministic global sum repeats bit for bit.
+"""
+import numpy as np
+import pytest
+
+from tests import golden_io as G
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _lib():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from veris_gb300 import _abi
+    return _abi.load()
+
+
+def _prepared(st):
+    from veris_gb300 import model
+    for name in ("SeaIceMass", "AreaWS", "WindForcingXY", "SeaIceStrength"):
+        fn, outs = [(f, o) for n, f, o in model.STEP if n == name][0]
+        vals = fn(st)
+        vals = vals if isinstance(vals, tuple) else (vals,)
+        for o, x in zip(outs, vals):
+            setattr(st.variables, o, x)
+    return st
+
+
+def test_quarter_degree_step_against_the_oracle():
+    from types import SimpleNamespace
+    from oracle import veris_oracle as O
+    from veris_gb300 import model
+    from veris_gb300.state import VerisState
+    from veris_gb300.synthetic import config_settings, config_state
+    arrays = config_state("c2_quarterdeg", seed=3, init_velocity=0.05, init_stress=1000.0)
+    sett = config_settings("c2_quarterdeg", nEVPsteps=2)
+    ref = SimpleNamespace(variables=SimpleNamespace(**{k: v.copy() for k, v in arrays.items()}), settings=sett)
+    O.step(ref)
+    st = VerisState.from_numpy(arrays, sett)
+    model.step(st)
+    torch.cuda.synchronize()
+    for k in ("uIce", "vIce", "sigma1", "sigma2", "sigma12", "hIceMean", "hSnowMean", "Area", "TSurf",
+              "Qnet", "EmPmR", "forc_salt_surface_ice"):
+        e = G.rel_err(getattr(st.variables, k).cpu().numpy(), getattr(ref.variables, k))
+        assert e <= 1e-10, (k, e)
+
+
+@pytest.fixture(scope="module")
+def tenth():
+    from veris_gb300.state import VerisState
+    from veris_gb300.synthetic import config_settings, config_state
+    arrays = config_state("c5_tenthdeg", seed=1, init_velocity=0.05)
+    return arrays, config_settings("c5_tenthdeg")
+
+
+def test_tenth_degree_fast_forms_agree(tenth):
+    from veris_gb300.evp_solver import evp_solver, evp_solver_fast
+    from veris_gb300.state import VerisState
+    arrays, sett = tenth
+    st = _prepared(VerisState.from_numpy(arrays, sett))
+    plain = evp_solver(st, 3)
+    fast = evp_solver_fast(st, "f64", "smem", n_subcycles=3)
+    for k in range(5):
+        e = G.rel_err(fast[k].cpu().numpy(), plain[k].cpu().numpy())
+        assert e <= 1e-10, (k, e)
+    walk = evp_solver_fast(st, "f32", "walk", n_subcycles=10, rows=0, variant=2)
+    smem = evp_solver_fast(st, "f32", "smem", n_subcycles=10)
+    for k in range(5):
+        e = G.rel_err(walk[k].double().cpu().numpy(), smem[k].double().cpu().numpy())
+        assert e <= 1e-5, (k, e)
+
+
+def test_tenth_degree_step_is_reproducible_and_fill_idempotent(tenth):
+    from veris_gb300.engine import SeaIceStep
+    from veris_gb300.fill_overlap import fill_overlap
+    from veris_gb300.global_sum import interior_sum
+    from veris_gb300.state import VerisState
+    arrays, sett = tenth
+    sett = type(sett)(**vars(sett))
+    sett.nEVPsteps = 50
+    outs = []
+    for _ in range(2):
+        st = VerisState.from_numpy(arrays, sett)
+        SeaIceStep(st, precision="f32").step()
+        torch.cuda.synchronize()
+        outs.append({k: getattr(st.variables, k).clone() for k in ("uIce", "vIce", "hIceMean", "Area", "Qnet")})
+    for k in outs[0]:
+        assert torch.equal(outs[0][k], outs[1][k]), k
+    h = outs[0]["hIceMean"]
+    once = fill_overlap(st, h.clone())
+    twice = fill_overlap(st, once.clone())
+    assert torch.equal(once, twice)
+    rA = st.variables.rA
+    s1 = interior_sum(h, rA)
+    s2 = interior_sum(h, rA)
+    assert torch.equal(s1, s2)
+    ref = float((h[2:-2, 2:-2] * rA[2:-2, 2:-2]).sum())
+    assert abs(float(s1) - ref) <= 1e-12 * abs(ref)
