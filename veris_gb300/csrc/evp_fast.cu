@@ -107,6 +107,10 @@ __global__ void fast_prep_kernel(VerisParams p, Fields<double> f, Dims d, int64_
         c.rdxV_x[i] = (T)f.recip_dxV[o];
         c.dxV_x[i] = (T)f.dxV[o];
         c.dxU_x[i] = (T)f.dxU[o];
+        c.xm4[4 * i] = (T)f.recip_dxV[o];
+        c.xm4[4 * i + 1] = (T)f.recip_dxU[o];
+        c.xm4[4 * i + 2] = (T)f.dxU[o];
+        c.xm4[4 * i + 3] = (T)f.dxV[o];
     }
     if (i == 0) {
         c.rdyV_y[j] = (T)f.recip_dyV[o];

@@ -65,10 +65,11 @@ __device__ __forceinline__ void load_row(Row &r, const FastConsts<float> &c, con
     r.bf = BASAL ? __ldg(c.bfac + o) : 0.f;
     r.ac = ADAPT ? __ldg(c.acf + o) : 0.f;
     r.f = __ldg(c.flags + o);
-    r.rdxV = __ldg(c.rdxV_x + gi);
-    r.rdxU = __ldg(c.rdxU_x + gi);
-    r.dxU = __ldg(c.dxU_x + gi);
-    r.dxV = __ldg(c.dxV_x + gi);
+    const float4 m = __ldg(reinterpret_cast<const float4 *>(c.xm4) + gi);
+    r.rdxV = m.x;
+    r.rdxU = m.y;
+    r.dxU = m.z;
+    r.dxV = m.w;
 }
 
 // One walk: the strip of output columns j0 .. j0+27 and output rows
