@@ -76,6 +76,14 @@ __global__ void fast_prep_kernel(VerisParams p, Fields<double> f, Dims d, int64_
     c.vOc[q] = (T)f.vOcean[o];
     c.rrAu[q] = (T)f.recip_rAu[o];
     c.rrAv[q] = (T)f.recip_rAv[o];
+    c.pUV[2 * q] = c.cU[q];
+    c.pUV[2 * q + 1] = c.cV[q];
+    c.pAWS[2 * q] = c.AW[q];
+    c.pAWS[2 * q + 1] = c.AS[q];
+    c.pMUV[2 * q] = c.mU[q];
+    c.pMUV[2 * q + 1] = c.mV[q];
+    c.pRR[2 * q] = c.rrAu[q];
+    c.pRR[2 * q + 1] = c.rrAv[q];
     if (p.useAdaptiveEVP)   // veris/evp_solver.py:65-73, the state-only factor of alphaC
         c.acf[q] = (T)(p.EVPcFac * f.recip_rA[o] / fmax(f.SeaIceMassC[o], 1e-4));
     if (BASAL) {

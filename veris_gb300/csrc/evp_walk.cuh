@@ -119,25 +119,22 @@ __device__ __forceinline__ void walk_strip(const Dims &d, int64_t lp, const Halo
             if (t >= 3) {   // row t-1, for the next step
                 const int gn = gown + 1 == d.NX ? 0 : gown + 1;
                 const int64_t on = (int64_t)gn * lp + gj;
-                o_cU = __ldg(c.cU + on);
-                o_cV = __ldg(c.cV + on);
-                o_AW = __ldg(c.AW + on);
-                o_AS = __ldg(c.AS + on);
-                o_mU = __ldg(c.mU + on);
-                o_mV = __ldg(c.mV + on);
-                o_rrAu = __ldg(c.rrAu + on);
-                o_rrAv = __ldg(c.rrAv + on);
+                const float2 a = __ldg(reinterpret_cast<const float2 *>(c.pUV) + on);
+                const float2 b = __ldg(reinterpret_cast<const float2 *>(c.pAWS) + on);
+                const float2 m = __ldg(reinterpret_cast<const float2 *>(c.pMUV) + on);
+                const float2 r = __ldg(reinterpret_cast<const float2 *>(c.pRR) + on);
+                o_cU = a.x; o_cV = a.y; o_AW = b.x; o_AS = b.y;
+                o_mU = m.x; o_mV = m.y; o_rrAu = r.x; o_rrAv = r.y;
             }
         } else if (t >= 4) {
+            // the U/V-point constants in pairs: four 8-byte loads
             const int64_t ob = (int64_t)gown * lp + gj;
-            cU = __ldg(c.cU + ob);
-            cV = __ldg(c.cV + ob);
-            AW = __ldg(c.AW + ob);
-            AS = __ldg(c.AS + ob);
-            mU = __ldg(c.mU + ob);
-            mV = __ldg(c.mV + ob);
-            rrAu = __ldg(c.rrAu + ob);
-            rrAv = __ldg(c.rrAv + ob);
+            const float2 a = __ldg(reinterpret_cast<const float2 *>(c.pUV) + ob);
+            const float2 b = __ldg(reinterpret_cast<const float2 *>(c.pAWS) + ob);
+            const float2 m = __ldg(reinterpret_cast<const float2 *>(c.pMUV) + ob);
+            const float2 r = __ldg(reinterpret_cast<const float2 *>(c.pRR) + ob);
+            cU = a.x; cV = a.y; AW = b.x; AS = b.y;
+            mU = m.x; mV = m.y; rrAu = r.x; rrAv = r.y;
         }
 
         // ---- A: e12 at Z points of row t
