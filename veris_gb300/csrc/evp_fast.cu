@@ -84,6 +84,12 @@ __global__ void fast_prep_kernel(VerisParams p, Fields<double> f, Dims d, int64_
     c.pMUV[2 * q + 1] = c.mV[q];
     c.pRR[2 * q] = c.rrAu[q];
     c.pRR[2 * q + 1] = c.rrAv[q];
+    c.pOc[2 * q] = c.uOc[q];
+    c.pOc[2 * q + 1] = c.vOc[q];
+    c.pMfPh[2 * q] = c.mfC[q];
+    c.pMfPh[2 * q + 1] = c.Ph[q];
+    c.pQrRz[2 * q] = c.qrA[q];
+    c.pQrRz[2 * q + 1] = c.rAz[q];
     if (p.useAdaptiveEVP)   // veris/evp_solver.py:65-73, the state-only factor of alphaC
         c.acf[q] = (T)(p.EVPcFac * f.recip_rA[o] / fmax(f.SeaIceMassC[o], 1e-4));
     if (BASAL) {

@@ -56,12 +56,15 @@ __device__ __forceinline__ void load_row(Row &r, const FastConsts<float> &c, con
     r.s1 = __ldg(io.s1 + o);
     r.s2 = __ldg(io.s2 + o);
     r.s12 = __ldg(io.s12 + o);
-    r.uo = __ldg(c.uOc + o);
-    r.vo = __ldg(c.vOc + o);
-    r.mf = __ldg(c.mfC + o);
-    r.ph = __ldg(c.Ph + o);
-    r.qr = __ldg(c.qrA + o);
-    r.rz = __ldg(c.rAz + o);
+    const float2 oc = __ldg(reinterpret_cast<const float2 *>(c.pOc) + o);
+    const float2 mp = __ldg(reinterpret_cast<const float2 *>(c.pMfPh) + o);
+    const float2 qz = __ldg(reinterpret_cast<const float2 *>(c.pQrRz) + o);
+    r.uo = oc.x;
+    r.vo = oc.y;
+    r.mf = mp.x;
+    r.ph = mp.y;
+    r.qr = qz.x;
+    r.rz = qz.y;
     r.bf = BASAL ? __ldg(c.bfac + o) : 0.f;
     r.ac = ADAPT ? __ldg(c.acf + o) : 0.f;
     r.f = __ldg(c.flags + o);
