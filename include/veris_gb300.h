@@ -307,6 +307,13 @@ int veris_evp_smem_solver_f32(const VerisGrid *g, const VerisParams *p, const Ve
  * Synchronises the stream.
  */
 int veris_evp_fast_status(const void *workspace, int32_t *status_host, veris_stream_t s);
+/*
+ * Failure-detection probe (no counterpart in the reference): one warp waits,
+ * with the TMA kernel's bounded mbarrier wait (`limit` polls, at most 2^20),
+ * on an mbarrier that it arrives on (`arrive` != 0) or that nothing arrives
+ * on; writes 0 or the timeout bit (1) to *status_device and returns.
+ */
+int veris_mbarrier_wait_probe(int32_t arrive, uint32_t limit, int32_t *status_device, veris_stream_t s);
 
 /*
  * No counterpart in the reference: an allocation-free form of

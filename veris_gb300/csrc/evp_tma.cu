@@ -511,3 +511,39 @@ int evp_tma_subcycles(const Dims &d, const HaloFill &h, const FastConsts<float> 
 }
 
 }  // namespace veris
+
+// ---------------------------------------------------------------------------
+// Probe of the bounded mbarrier wait the TMA kernel uses (failure detection
+// without a fault): one warp initialises an mbarrier expecting one arrival,
+// arrives on it or not, and waits on it with mbar_wait_bounded.  When nothing
+// arrives the wait gives up after `limit` polls and the probe sets the same
+// status bit the TMA kernel sets (S_TMA_TIMEOUT) in *status; the kernel then
+// returns normally and the context stays usable.
+namespace veris {
+namespace tma {
+
+__global__ void mbar_wait_probe_kernel(int arrive, uint32_t limit, int *status) {
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) mbar_init(&bar, 1);
+    fence_barrier_init();
+    __syncthreads();
+    if (arrive && threadIdx.x == 0)
+        asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(saddr(&bar))
+                     : "memory");
+    const bool ok = mbar_wait_bounded(&bar, 0u, limit);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        *status = ok ? 0 : S_TMA_TIMEOUT;
+        asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(saddr(&bar)) : "memory");
+    }
+}
+
+}  // namespace tma
+}  // namespace veris
+
+extern "C" int veris_mbarrier_wait_probe(int32_t arrive, uint32_t limit, int32_t *status_device, veris_stream_t s) {
+    using namespace veris;
+    VERIS_REQUIRE(status_device && limit > 0 && limit <= tma::WAIT_LIMIT, VERIS_ERR_ARG);
+    tma::mbar_wait_probe_kernel<<<1, 32, 0, (cudaStream_t)s>>>(arrive ? 1 : 0, limit, status_device);
+    return launch_status();
+}
