@@ -54,7 +54,7 @@ __global__ void fast_check_kernel(Fields<double> f, Dims d, int *viol) {
 // ------------------------------------------------------------------- prep
 template <class T, bool BASAL>
 __global__ void fast_prep_kernel(VerisParams p, Fields<double> f, Dims d, int64_t lp, FastConsts<T> c, T *u, T *v,
-                                 T *s1, T *s2, T *s12) {
+                                 T *s1, T *s2, T *s12, int paired) {
     const int j = blockIdx.x * 32 + threadIdx.x, i = blockIdx.y * 8 + threadIdx.y;
     if (i >= d.NX || j >= d.NY) return;
     const int64_t o = d.raw(i, j);
@@ -132,10 +132,17 @@ __global__ void fast_prep_kernel(VerisParams p, Fields<double> f, Dims d, int64_
         c.dyV_y[j] = (T)f.dyV[o];
         c.dyU_y[j] = (T)f.dyU[o];
     }
-    u[q] = (T)f.uIce[o];
-    v[q] = (T)f.vIce[o];
-    s1[q] = (T)f.sigma1[o];
-    s2[q] = (T)f.sigma2[o];
+    if (paired) {   // the register walk's layout: (u, v) over u's and v's buffers, (sigma1, sigma2) likewise
+        u[2 * q] = (T)f.uIce[o];
+        u[2 * q + 1] = (T)f.vIce[o];
+        s1[2 * q] = (T)f.sigma1[o];
+        s1[2 * q + 1] = (T)f.sigma2[o];
+    } else {
+        u[q] = (T)f.uIce[o];
+        v[q] = (T)f.vIce[o];
+        s1[q] = (T)f.sigma1[o];
+        s2[q] = (T)f.sigma2[o];
+    }
     s12[q] = (T)f.sigma12[o];
 }
 
@@ -182,10 +189,10 @@ int fast_prep(const Dims &d, const VerisParams &p, const Fields<double> &f, cons
     dim3 g2((d.NY + 31) / 32, (d.NX + 7) / 8);
     if (p.basalDragK2 != 0.0)
         fast_prep_kernel<T, true><<<g2, dim3(32, 8), 0, st>>>(p, f, d, lp, c, state0[0], state0[1], state0[2],
-                                                              state0[3], state0[4]);
+                                                              state0[3], state0[4], 0);
     else
         fast_prep_kernel<T, false><<<g2, dim3(32, 8), 0, st>>>(p, f, d, lp, c, state0[0], state0[1], state0[2],
-                                                               state0[3], state0[4]);
+                                                               state0[3], state0[4], 0);
     return launch_status();
 }
 
@@ -221,6 +228,9 @@ static int evp_fast(const VerisGrid *g, const VerisParams *p, const VerisFieldsF
     VERIS_REQUIRE(p && vs64 && uo && vo && s1o && s2o && s12o, VERIS_ERR_ARG);
     VERIS_REQUIRE(n >= 1, VERIS_ERR_ARG);
     const bool walker = sizeof(T) == 4 && (allow_tma >= 4 || allow_tma < 0);
+    // the walk's own subcycle chain runs on the paired state layout (not with
+    // a tape, whose slots the adjoint reads planar)
+    const bool paired = walker && tape == nullptr;
     if (walker ? walk_support(*p) : fast_support(*p)) return VERIS_ERR_UNSUPPORTED;
     const bool adapt = p->useAdaptiveEVP != 0;
     FastConsts<T> c;
@@ -241,9 +251,11 @@ static int evp_fast(const VerisGrid *g, const VerisParams *p, const VerisFieldsF
     for (int q = 0; q < 5; ++q) s0[q] = tape ? tslot(0, q) : state[0][q];
     dim3 g2((d.NY + 31) / 32, (d.NX + 7) / 8);
     if (basal)
-        fast_prep_kernel<T, true><<<g2, dim3(32, 8), 0, st>>>(*p, f, d, lp, c, s0[0], s0[1], s0[2], s0[3], s0[4]);
+        fast_prep_kernel<T, true><<<g2, dim3(32, 8), 0, st>>>(*p, f, d, lp, c, s0[0], s0[1], s0[2], s0[3], s0[4],
+                                                              paired ? 1 : 0);
     else
-        fast_prep_kernel<T, false><<<g2, dim3(32, 8), 0, st>>>(*p, f, d, lp, c, s0[0], s0[1], s0[2], s0[3], s0[4]);
+        fast_prep_kernel<T, false><<<g2, dim3(32, 8), 0, st>>>(*p, f, d, lp, c, s0[0], s0[1], s0[2], s0[3], s0[4],
+                                                               paired ? 1 : 0);
     int stt = launch_status();
     if (stt != VERIS_OK) return stt;
     const FastScalars<T> k = fast_scalars<T>(*p);
@@ -258,7 +270,7 @@ static int evp_fast(const VerisGrid *g, const VerisParams *p, const VerisFieldsF
                                                {nullptr, nullptr, nullptr, nullptr, nullptr}};
                     float *const to[5] = {tslot(it + 1, 0), tslot(it + 1, 1), tslot(it + 1, 2), tslot(it + 1, 3),
                                           tslot(it + 1, 4)};
-                    if ((stt = evp_walk_subcycles(adapt, d, h, c, k, from, to, lp, 1, basal, turn,
+                    if ((stt = evp_walk_subcycles(adapt, false, d, h, c, k, from, to, lp, 1, basal, turn,
                                                   allow_tma < 0 ? 0 : allow_tma, walk_variant, st)) != VERIS_OK)
                         return stt;
                     done = true;
@@ -279,7 +291,8 @@ static int evp_fast(const VerisGrid *g, const VerisParams *p, const VerisFieldsF
     }
     if constexpr (sizeof(T) == 4) {
         if (allow_tma >= 4 || allow_tma < 0)   // register-walking kernel, allow_tma rows per walk (< 0: auto)
-            return evp_walk_subcycles(adapt, d, h, c, k, state, outs, d.ld, n, basal, turn, allow_tma < 0 ? 0 : allow_tma,
+            return evp_walk_subcycles(adapt, paired, d, h, c, k, state, outs, d.ld, n, basal, turn,
+                                      allow_tma < 0 ? 0 : allow_tma,
                                       walk_variant, st);
         if (allow_tma) {
             stt = evp_tma_subcycles(d, h, c, k, state, outs, d.ld, n, status, basal, turn, st);

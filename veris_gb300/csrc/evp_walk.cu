@@ -21,7 +21,7 @@ template <>
 struct Variant<3> { static constexpr int UNROLL = 1, MINB = 4; static constexpr bool PRE = true; };
 constexpr int N_VARIANTS = N_WALK_VARIANTS;
 
-template <bool BASAL, bool TURN, int V, bool ADAPT>
+template <bool BASAL, bool TURN, int V, bool ADAPT, int L>
 __global__ void __launch_bounds__(WARPS * 32, Variant<V>::MINB)
 evp_walk_kernel(Dims d, int64_t lp, HaloFill h, FastConsts<float> c, FastScalars<float> k, FastIO<float> io,
                 int nstrips, int nwalks, int H) {
@@ -29,28 +29,28 @@ evp_walk_kernel(Dims d, int64_t lp, HaloFill h, FastConsts<float> c, FastScalars
     const int w = blockIdx.x * WARPS + (threadIdx.x >> 5);
     if (w >= nwalks) return;   // whole warps only
     const int strip = w % nstrips, rb = w / nstrips;
-    walk_strip<BASAL, TURN, Variant<V>::UNROLL, Variant<V>::PRE, ADAPT>(d, lp, h, c, k, io, rb * H, strip * TW, H,
-                                                                        lane);
+    walk_strip<BASAL, TURN, Variant<V>::UNROLL, Variant<V>::PRE, ADAPT, (L != 0), (L == 1)>(
+        d, lp, h, c, k, io, rb * H, strip * TW, H, lane);
 }
 
-template <bool B, bool R, int V, bool A>
+template <bool B, bool R, int V, bool A, int L>
 static int launch(const Dims &d, int64_t lp, const HaloFill &h, const FastConsts<float> &c,
                   const FastScalars<float> &k, const FastIO<float> &io, int H, cudaStream_t st) {
     const int nstrips = (d.NY + TW - 1) / TW, nblk = (d.NX + H - 1) / H;
     const int nwalks = nstrips * nblk;
-    evp_walk_kernel<B, R, V, A><<<(nwalks + WARPS - 1) / WARPS, WARPS * 32, 0, st>>>(d, lp, h, c, k, io, nstrips,
-                                                                                nwalks, H);
+    evp_walk_kernel<B, R, V, A, L><<<(nwalks + WARPS - 1) / WARPS, WARPS * 32, 0, st>>>(d, lp, h, c, k, io,
+                                                                                   nstrips, nwalks, H);
     return launch_status();
 }
 
 // walk length: the most rows per walk that still fits all walks in one wave
 // of resident warps (rows >= 8); ring overhead per walk is 4 rows
-template <bool B, bool R, int V, bool A>
+template <bool B, bool R, int V, bool A, int L>
 static int auto_rows(const Dims &d) {
     int dev = 0, sms = 0, per_sm = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) !=
                                                   cudaSuccess ||
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, evp_walk_kernel<B, R, V, A>, WARPS * 32, 0) !=
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, evp_walk_kernel<B, R, V, A, L>, WARPS * 32, 0) !=
             cudaSuccess || sms <= 0 || per_sm <= 0) {
         cudaGetLastError();
         return 16;
@@ -62,30 +62,41 @@ static int auto_rows(const Dims &d) {
     return rows < 8 ? 8 : (rows > 4096 ? 4096 : rows);
 }
 
-template <int V, bool A>
-static int launch_va(bool basal, bool turn, const Dims &d, int64_t lp, const HaloFill &h, const FastConsts<float> &c,
-                     const FastScalars<float> &k, const FastIO<float> &io, int H, cudaStream_t st) {
+template <int V, bool A, int L>
+static int launch_val(bool basal, bool turn, const Dims &d, int64_t lp, const HaloFill &h,
+                      const FastConsts<float> &c, const FastScalars<float> &k, const FastIO<float> &io, int H,
+                      cudaStream_t st) {
     if (H <= 0)
-        H = basal ? (turn ? auto_rows<true, true, V, A>(d) : auto_rows<true, false, V, A>(d))
-                  : (turn ? auto_rows<false, true, V, A>(d) : auto_rows<false, false, V, A>(d));
+        H = basal ? (turn ? auto_rows<true, true, V, A, L>(d) : auto_rows<true, false, V, A, L>(d))
+                  : (turn ? auto_rows<false, true, V, A, L>(d) : auto_rows<false, false, V, A, L>(d));
     if (basal)
-        return turn ? launch<true, true, V, A>(d, lp, h, c, k, io, H, st)
-                    : launch<true, false, V, A>(d, lp, h, c, k, io, H, st);
-    return turn ? launch<false, true, V, A>(d, lp, h, c, k, io, H, st)
-                : launch<false, false, V, A>(d, lp, h, c, k, io, H, st);
+        return turn ? launch<true, true, V, A, L>(d, lp, h, c, k, io, H, st)
+                    : launch<true, false, V, A, L>(d, lp, h, c, k, io, H, st);
+    return turn ? launch<false, true, V, A, L>(d, lp, h, c, k, io, H, st)
+                : launch<false, false, V, A, L>(d, lp, h, c, k, io, H, st);
+}
+
+// layout L: 0 planar state in and out, 1 paired in and out, 2 paired in, planar out
+template <int V, int L>
+static int launch_vl(bool adapt, bool basal, bool turn, const Dims &d, int64_t lp, const HaloFill &h,
+                     const FastConsts<float> &c, const FastScalars<float> &k, const FastIO<float> &io, int H,
+                     cudaStream_t st) {
+    return adapt ? launch_val<V, true, L>(basal, turn, d, lp, h, c, k, io, H, st)
+                 : launch_val<V, false, L>(basal, turn, d, lp, h, c, k, io, H, st);
 }
 
 template <int V>
-static int launch_v(bool adapt, bool basal, bool turn, const Dims &d, int64_t lp, const HaloFill &h,
+static int launch_v(int layout, bool adapt, bool basal, bool turn, const Dims &d, int64_t lp, const HaloFill &h,
                     const FastConsts<float> &c, const FastScalars<float> &k, const FastIO<float> &io, int H,
                     cudaStream_t st) {
-    return adapt ? launch_va<V, true>(basal, turn, d, lp, h, c, k, io, H, st)
-                 : launch_va<V, false>(basal, turn, d, lp, h, c, k, io, H, st);
+    if (layout == 1) return launch_vl<V, 1>(adapt, basal, turn, d, lp, h, c, k, io, H, st);
+    if (layout == 2) return launch_vl<V, 2>(adapt, basal, turn, d, lp, h, c, k, io, H, st);
+    return launch_vl<V, 0>(adapt, basal, turn, d, lp, h, c, k, io, H, st);
 }
 
 }  // namespace walk
 
-int evp_walk_subcycles(bool adapt, const Dims &d, const HaloFill &h, const FastConsts<float> &c,
+int evp_walk_subcycles(bool adapt, bool paired, const Dims &d, const HaloFill &h, const FastConsts<float> &c,
                        const FastScalars<float> &k,
                        float *const state[2][5], float *const outs[5], int64_t ldo, int n, bool basal, bool turn,
                        int rows, int variant, cudaStream_t st) {
@@ -97,12 +108,16 @@ int evp_walk_subcycles(bool adapt, const Dims &d, const HaloFill &h, const FastC
         float *const *dst = last ? outs : state[(it + 1) % 2];
         const FastIO<float> io{state[b][0], state[b][1], state[b][2], state[b][3], state[b][4],
                                dst[0], dst[1], dst[2], dst[3], dst[4], last ? ldo : lp};
+        // paired: the state buffers hold (u, v) over their u and v halves and
+        // (sigma1, sigma2) over their sigma1 and sigma2 halves; the last
+        // subcycle writes the caller's planar arrays
+        const int layout = paired ? (last ? 2 : 1) : 0;
         int stt;
         switch (variant) {
-        case 1: stt = walk::launch_v<1>(adapt, basal, turn, d, lp, h, c, k, io, rows, st); break;
-        case 2: stt = walk::launch_v<2>(adapt, basal, turn, d, lp, h, c, k, io, rows, st); break;
-        case 3: stt = walk::launch_v<3>(adapt, basal, turn, d, lp, h, c, k, io, rows, st); break;
-        default: stt = walk::launch_v<0>(adapt, basal, turn, d, lp, h, c, k, io, rows, st); break;
+        case 1: stt = walk::launch_v<1>(layout, adapt, basal, turn, d, lp, h, c, k, io, rows, st); break;
+        case 2: stt = walk::launch_v<2>(layout, adapt, basal, turn, d, lp, h, c, k, io, rows, st); break;
+        case 3: stt = walk::launch_v<3>(layout, adapt, basal, turn, d, lp, h, c, k, io, rows, st); break;
+        default: stt = walk::launch_v<0>(layout, adapt, basal, turn, d, lp, h, c, k, io, rows, st); break;
         }
         if (stt != VERIS_OK) return stt;
     }

@@ -47,14 +47,24 @@ struct Row {
     float rdxV, rdxU, dxU, dxV;   // metrics of the row
 };
 
-template <bool BASAL, bool ADAPT = false>
+// PIN: the state is paired, io.u holding (u, v) and io.s1 (sigma1, sigma2)
+template <bool BASAL, bool ADAPT = false, bool PIN = false>
 __device__ __forceinline__ void load_row(Row &r, const FastConsts<float> &c, const FastIO<float> &io, int64_t lp,
                                          int gi, int gj) {
     const int64_t o = (int64_t)gi * lp + gj;
-    r.u = __ldg(io.u + o);
-    r.v = __ldg(io.v + o);
-    r.s1 = __ldg(io.s1 + o);
-    r.s2 = __ldg(io.s2 + o);
+    if (PIN) {
+        const float2 uv = __ldg(reinterpret_cast<const float2 *>(io.u) + o);
+        const float2 ss = __ldg(reinterpret_cast<const float2 *>(io.s1) + o);
+        r.u = uv.x;
+        r.v = uv.y;
+        r.s1 = ss.x;
+        r.s2 = ss.y;
+    } else {
+        r.u = __ldg(io.u + o);
+        r.v = __ldg(io.v + o);
+        r.s1 = __ldg(io.s1 + o);
+        r.s2 = __ldg(io.s2 + o);
+    }
     r.s12 = __ldg(io.s12 + o);
     const float2 oc = __ldg(reinterpret_cast<const float2 *>(c.pOc) + o);
     const float2 mp = __ldg(reinterpret_cast<const float2 *>(c.pMfPh) + o);
@@ -81,7 +91,10 @@ __device__ __forceinline__ void load_row(Row &r, const FastConsts<float> &c, con
 // ADAPT: adaptive EVP (veris/evp_solver.py:65-73, 97-100, 148-150): alphaC
 // from zeta at each C point, alphaZ and the U/V betas averaged from the
 // alphaC of the neighbouring C points, carried across rows like zeta.
-template <bool BASAL, bool TURN, int UNROLL, bool PRE = false, bool ADAPT = false>
+// PIN / POUT: the input / output state is paired ((u, v) and (sigma1,
+// sigma2) in 8-byte pairs, sigma12 alone), the walk's own ping-pong layout.
+template <bool BASAL, bool TURN, int UNROLL, bool PRE = false, bool ADAPT = false, bool PIN = false,
+          bool POUT = false>
 __device__ __forceinline__ void walk_strip(const Dims &d, int64_t lp, const HaloFill &h, const FastConsts<float> &c,
                                            const FastScalars<float> &k, const FastIO<float> &io, int i0, int j0,
                                            int H, int lane) {
@@ -106,7 +119,7 @@ __device__ __forceinline__ void walk_strip(const Dims &d, int64_t lp, const Halo
     // row indices advance by one per step: wrapped incrementally (any walk length)
     int gnext = d.wxa(i0 - 2);   // row of the next prefetch
     int gown = d.wxa(i0 - 4);    // row of this step's own-point constants (row t-2)
-    load_row<BASAL, ADAPT>(Pf, c, io, lp, gnext, gj);
+    load_row<BASAL, ADAPT, PIN>(Pf, c, io, lp, gnext, gj);
     const int T = H + 4;   // rows i0-2 .. i0+H+1
     // UNROLL = 4 (the rotation period) would rename the row ages instead of
     // copying them; measured slower (register pressure), the kernels use 1
@@ -114,7 +127,7 @@ __device__ __forceinline__ void walk_strip(const Dims &d, int64_t lp, const Halo
     for (int t = 0; t < T; ++t) {
         N = Pf;
         gnext = gnext + 1 == d.NX ? 0 : gnext + 1;
-        if (t + 1 < T) load_row<BASAL, ADAPT>(Pf, c, io, lp, gnext, gj);
+        if (t + 1 < T) load_row<BASAL, ADAPT, PIN>(Pf, c, io, lp, gnext, gj);
         // own-point constants of row t-2 (stage D)
         float cU = 0.f, cV = 0.f, AW = 0.f, AS = 0.f, mU = 0.f, mV = 0.f, rrAu = 0.f, rrAv = 0.f;
         if (PRE) {
@@ -178,8 +191,12 @@ __device__ __forceinline__ void walk_strip(const Dims &d, int64_t lp, const Halo
             const int oi = i0 + t - 3;
             if (own_j && t >= 3 && t <= H + 2 && oi < d.NX) {
                 const int64_t wo = (int64_t)oi * ldo + jl;
-                io.s1o[wo] = s1;
-                io.s2o[wo] = s2;
+                if (POUT) {
+                    reinterpret_cast<float2 *>(io.s1o)[wo] = make_float2(s1, s2);
+                } else {
+                    io.s1o[wo] = s1;
+                    io.s2o[wo] = s2;
+                }
             }
             const uint32_t fe = N.f, fn = dnu(A.f);
             const float du0 = (A.u - A.uo) * one_if<float>(A.f, F_INU);
@@ -263,11 +280,19 @@ __device__ __forceinline__ void walk_strip(const Dims &d, int64_t lp, const Halo
             }
             if (own_j && oi < d.NX) {
                 if (images) {
-                    store_filled_ld(io.uo, ldo, d, h, oi, jl, un);
-                    store_filled_ld(io.vo, ldo, d, h, oi, jl, vnew);
+                    if (POUT) {
+                        store_filled_ld(reinterpret_cast<float2 *>(io.uo), ldo, d, h, oi, jl, make_float2(un, vnew));
+                    } else {
+                        store_filled_ld(io.uo, ldo, d, h, oi, jl, un);
+                        store_filled_ld(io.vo, ldo, d, h, oi, jl, vnew);
+                    }
                 } else {
-                    io.uo[(int64_t)oi * ldo + jl] = un;
-                    io.vo[(int64_t)oi * ldo + jl] = vnew;
+                    if (POUT) {
+                        reinterpret_cast<float2 *>(io.uo)[(int64_t)oi * ldo + jl] = make_float2(un, vnew);
+                    } else {
+                        io.uo[(int64_t)oi * ldo + jl] = un;
+                        io.vo[(int64_t)oi * ldo + jl] = vnew;
+                    }
                 }
             }
         }
