@@ -329,3 +329,18 @@ def test_engine_free_drift_step():
             e = G.rel_err(getattr(st.variables, k).cpu().numpy(), getattr(ref.variables, k).cpu().numpy())
             assert e <= tol, (precision, k, e)
         assert torch.equal(st.variables.sigma1, torch.as_tensor(arrays["sigma1"], device="cuda"))
+
+
+@pytest.mark.parametrize("nx,ny", ((120, 90), (61, 33)))
+def test_walk_with_both_halos_refreshed(nx, ny):
+    """veros_fill = False refreshes both halos from periodic images: the walk's
+    own state layout keeps a halo point's own stresses and its velocity
+    images apart."""
+    from veris_gb300.evp_solver import evp_solver_fast
+    st = _prepared(nx, ny, nx + 1, veros_fill=False)
+    smem = evp_solver_fast(st, "f32", "smem", n_subcycles=12)
+    for rows, variant in ((0, 2), (7, 0), (16, 3)):
+        walk = evp_solver_fast(st, "f32", "walk", n_subcycles=12, rows=rows, variant=variant)
+        for k in range(5):
+            e = G.rel_err(walk[k].double().cpu().numpy(), smem[k].double().cpu().numpy())
+            assert e <= 1e-5, (nx, ny, rows, variant, k, e)

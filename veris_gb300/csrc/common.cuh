@@ -118,6 +118,41 @@ __device__ __forceinline__ void store_filled(T *out, const Dims &d, const HaloFi
     store_filled_ld(out, d.ld, d, h, i, j, val);
 }
 
+// The same store for a point of the register walk's four-value state
+// (u, v, sigma1, sigma2): the own slot gets all four values unless the point
+// lies in a refreshed halo, where it gets only its own stresses (its u, v are
+// images); the image slots inside the refreshed halos get (u, v) only.
+__device__ __forceinline__ void store_filled_quad(float4 *out, int64_t ld, const Dims &d, const HaloFill &h, int i,
+                                                  int j, float4 val) {
+    float2 *half = reinterpret_cast<float2 *>(out);
+    const bool hx = h.x_fill && in_xhalo(d, h.olx, i);
+    const bool hy = h.y_fill && in_yhalo(d, h.oly, j);
+    const int64_t o = (int64_t)i * ld + j;
+    if (hx || hy) {
+        half[2 * o + 1] = make_float2(val.z, val.w);
+        return;
+    }
+    out[o] = val;
+    int ix[2] = {i, -1};
+    if (h.x_fill) {
+        if (i + d.nx < d.NX && in_xhalo(d, h.olx, i + d.nx)) ix[1] = i + d.nx;
+        else if (i - d.nx >= 0 && in_xhalo(d, h.olx, i - d.nx)) ix[1] = i - d.nx;
+    }
+    int jy[2] = {j, -1};
+    if (h.y_fill) {
+        if (j + d.ny < d.NY && in_yhalo(d, h.oly, j + d.ny)) jy[1] = j + d.ny;
+        else if (j - d.ny >= 0 && in_yhalo(d, h.oly, j - d.ny)) jy[1] = j - d.ny;
+    }
+#pragma unroll
+    for (int a = 0; a < 2; ++a)
+#pragma unroll
+        for (int b = 0; b < 2; ++b) {
+            if (a == 0 && b == 0) continue;
+            if (ix[a] < 0 || jy[b] < 0) continue;
+            half[2 * ((int64_t)ix[a] * ld + jy[b])] = make_float2(val.x, val.y);
+        }
+}
+
 inline HaloFill halo_fill_of(const VerisParams &p) {
     HaloFill h;
     h.olx = 2;

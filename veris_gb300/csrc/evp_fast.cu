@@ -132,11 +132,11 @@ __global__ void fast_prep_kernel(VerisParams p, Fields<double> f, Dims d, int64_
         c.dyV_y[j] = (T)f.dyV[o];
         c.dyU_y[j] = (T)f.dyU[o];
     }
-    if (paired) {   // the register walk's layout: (u, v) over u's and v's buffers, (sigma1, sigma2) likewise
-        u[2 * q] = (T)f.uIce[o];
-        u[2 * q + 1] = (T)f.vIce[o];
-        s1[2 * q] = (T)f.sigma1[o];
-        s1[2 * q + 1] = (T)f.sigma2[o];
+    if (paired) {   // the register walk's layout: (u, v, sigma1, sigma2) over the four buffers
+        u[4 * q] = (T)f.uIce[o];
+        u[4 * q + 1] = (T)f.vIce[o];
+        u[4 * q + 2] = (T)f.sigma1[o];
+        u[4 * q + 3] = (T)f.sigma2[o];
     } else {
         u[q] = (T)f.uIce[o];
         v[q] = (T)f.vIce[o];

@@ -156,9 +156,9 @@ bool evp_tma_available();
 // budget), reading state[0] first
 // compiled forms of the register-walking kernel (evp_walk.cu)
 constexpr int N_WALK_VARIANTS = 4;
-// paired: the state buffers hold the walk's paired layout ((u, v) and
-// (sigma1, sigma2) in 8-byte pairs over the u/v and sigma1/sigma2 halves,
-// written so by the prep); the last subcycle writes planar `outs`
+// paired: the state buffers hold the walk's own layout ((u, v, sigma1,
+// sigma2) in 16 bytes per point over the four buffers, sigma12 alone; the
+// prep writes the first state so); the last subcycle writes planar `outs`
 int evp_walk_subcycles(bool adapt, bool paired, const Dims &d, const HaloFill &h, const FastConsts<float> &c,
                        const FastScalars<float> &k,
                        float *const state[2][5], float *const outs[5], int64_t ldo, int n, bool basal, bool turn,

@@ -108,9 +108,8 @@ int evp_walk_subcycles(bool adapt, bool paired, const Dims &d, const HaloFill &h
         float *const *dst = last ? outs : state[(it + 1) % 2];
         const FastIO<float> io{state[b][0], state[b][1], state[b][2], state[b][3], state[b][4],
                                dst[0], dst[1], dst[2], dst[3], dst[4], last ? ldo : lp};
-        // paired: the state buffers hold (u, v) over their u and v halves and
-        // (sigma1, sigma2) over their sigma1 and sigma2 halves; the last
-        // subcycle writes the caller's planar arrays
+        // paired: the state buffers hold (u, v, sigma1, sigma2) per point over
+        // their four buffers; the last subcycle writes the caller's planar arrays
         const int layout = paired ? (last ? 2 : 1) : 0;
         int stt;
         switch (variant) {

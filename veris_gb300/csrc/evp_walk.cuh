@@ -47,18 +47,17 @@ struct Row {
     float rdxV, rdxU, dxU, dxV;   // metrics of the row
 };
 
-// PIN: the state is paired, io.u holding (u, v) and io.s1 (sigma1, sigma2)
+// PIN: the state is the walk's four-value layout, io.u holding (u, v, sigma1, sigma2)
 template <bool BASAL, bool ADAPT = false, bool PIN = false>
 __device__ __forceinline__ void load_row(Row &r, const FastConsts<float> &c, const FastIO<float> &io, int64_t lp,
                                          int gi, int gj) {
     const int64_t o = (int64_t)gi * lp + gj;
     if (PIN) {
-        const float2 uv = __ldg(reinterpret_cast<const float2 *>(io.u) + o);
-        const float2 ss = __ldg(reinterpret_cast<const float2 *>(io.s1) + o);
-        r.u = uv.x;
-        r.v = uv.y;
-        r.s1 = ss.x;
-        r.s2 = ss.y;
+        const float4 q = __ldg(reinterpret_cast<const float4 *>(io.u) + o);
+        r.u = q.x;
+        r.v = q.y;
+        r.s1 = q.z;
+        r.s2 = q.w;
     } else {
         r.u = __ldg(io.u + o);
         r.v = __ldg(io.v + o);
@@ -91,8 +90,10 @@ __device__ __forceinline__ void load_row(Row &r, const FastConsts<float> &c, con
 // ADAPT: adaptive EVP (veris/evp_solver.py:65-73, 97-100, 148-150): alphaC
 // from zeta at each C point, alphaZ and the U/V betas averaged from the
 // alphaC of the neighbouring C points, carried across rows like zeta.
-// PIN / POUT: the input / output state is paired ((u, v) and (sigma1,
-// sigma2) in 8-byte pairs, sigma12 alone), the walk's own ping-pong layout.
+// PIN / POUT: the input / output state is the walk's own ping-pong layout,
+// (u, v, sigma1, sigma2) in 16 bytes per point and sigma12 alone; with POUT
+// a row's stresses wait one walk step in registers and are stored with its
+// velocities.
 template <bool BASAL, bool TURN, int UNROLL, bool PRE = false, bool ADAPT = false, bool PIN = false,
           bool POUT = false>
 __device__ __forceinline__ void walk_strip(const Dims &d, int64_t lp, const HaloFill &h, const FastConsts<float> &c,
@@ -115,6 +116,7 @@ __device__ __forceinline__ void walk_strip(const Dims &d, int64_t lp, const Halo
     float cd_a = 0.f, cd_b = 0.f, cb_a = 0.f, cb_b = 0.f;
     float fv_a = 0.f, fv_b = 0.f, fu_a = 0.f, s12_a = 0.f;
     float aC_a = 0.f, aC_b = 0.f;   // adaptive alphaC of rows t-2, t-3
+    float hs1 = 0.f, hs2 = 0.f;     // POUT: sigma1, sigma2 of the row stage D stores this step
     float o_cU = 0.f, o_cV = 0.f, o_AW = 0.f, o_AS = 0.f, o_mU = 0.f, o_mV = 0.f, o_rrAu = 0.f, o_rrAv = 0.f;
     // row indices advance by one per step: wrapped incrementally (any walk length)
     int gnext = d.wxa(i0 - 2);   // row of the next prefetch
@@ -163,7 +165,7 @@ __device__ __forceinline__ void walk_strip(const Dims &d, int64_t lp, const Halo
         const float z2n = N.rz * (e12n * e12n);
 
         float zeta_new = 0.f, s11_new = 0.f, s22_new = 0.f, cd_new = 0.f, cb_new = 0.f, fv_new = 0.f, fu_new = 0.f;
-        float s12_new = 0.f, aC_new = 0.f;
+        float s12_new = 0.f, aC_new = 0.f, ns1 = 0.f, ns2 = 0.f;
         if (t >= 2) {
             // ---- B: C points of row t-1 (A holds its inputs, N the next row)
             const float mInC = one_if<float>(A.f, F_INC);
@@ -186,14 +188,14 @@ __device__ __forceinline__ void walk_strip(const Dims &d, int64_t lp, const Halo
             const float press = k.kp * zeta * delta;
             const float s1 = (A.s1 * am1 + (2.f * zeta * ep - press)) * ral * mC;
             const float s2 = (A.s2 * am1 + 0.5f * zeta * em) * ral * mC;
+            ns1 = s1;
+            ns2 = s2;
             s11_new = 0.5f * (s1 + s2) * dyV;
             s22_new = 0.5f * (s1 - s2) * A.dxU;
             const int oi = i0 + t - 3;
             if (own_j && t >= 3 && t <= H + 2 && oi < d.NX) {
                 const int64_t wo = (int64_t)oi * ldo + jl;
-                if (POUT) {
-                    reinterpret_cast<float2 *>(io.s1o)[wo] = make_float2(s1, s2);
-                } else {
+                if (!POUT) {
                     io.s1o[wo] = s1;
                     io.s2o[wo] = s2;
                 }
@@ -281,14 +283,15 @@ __device__ __forceinline__ void walk_strip(const Dims &d, int64_t lp, const Halo
             if (own_j && oi < d.NX) {
                 if (images) {
                     if (POUT) {
-                        store_filled_ld(reinterpret_cast<float2 *>(io.uo), ldo, d, h, oi, jl, make_float2(un, vnew));
+                        store_filled_quad(reinterpret_cast<float4 *>(io.uo), ldo, d, h, oi, jl,
+                                          make_float4(un, vnew, hs1, hs2));
                     } else {
                         store_filled_ld(io.uo, ldo, d, h, oi, jl, un);
                         store_filled_ld(io.vo, ldo, d, h, oi, jl, vnew);
                     }
                 } else {
                     if (POUT) {
-                        reinterpret_cast<float2 *>(io.uo)[(int64_t)oi * ldo + jl] = make_float2(un, vnew);
+                        reinterpret_cast<float4 *>(io.uo)[(int64_t)oi * ldo + jl] = make_float4(un, vnew, hs1, hs2);
                     } else {
                         io.uo[(int64_t)oi * ldo + jl] = un;
                         io.vo[(int64_t)oi * ldo + jl] = vnew;
@@ -316,6 +319,10 @@ __device__ __forceinline__ void walk_strip(const Dims &d, int64_t lp, const Halo
         s12_a = s12_new;
         aC_b = aC_a;
         aC_a = aC_new;
+        if (POUT) {
+            hs1 = ns1;
+            hs2 = ns2;
+        }
         gown = gown + 1 == d.NX ? 0 : gown + 1;
     }
 }
