@@ -76,18 +76,18 @@ __global__ void fast_prep_kernel(VerisParams p, Fields<double> f, Dims d, int64_
     c.vOc[q] = (T)f.vOcean[o];
     c.rrAu[q] = (T)f.recip_rAu[o];
     c.rrAv[q] = (T)f.recip_rAv[o];
-    c.pUV[2 * q] = c.cU[q];
-    c.pUV[2 * q + 1] = c.cV[q];
-    c.pAWS[2 * q] = c.AW[q];
-    c.pAWS[2 * q + 1] = c.AS[q];
-    c.pMUV[2 * q] = c.mU[q];
-    c.pMUV[2 * q + 1] = c.mV[q];
-    c.pRR[2 * q] = c.rrAu[q];
-    c.pRR[2 * q + 1] = c.rrAv[q];
-    c.pOc[2 * q] = c.uOc[q];
-    c.pOc[2 * q + 1] = c.vOc[q];
-    c.pMfPh[2 * q] = c.mfC[q];
-    c.pMfPh[2 * q + 1] = c.Ph[q];
+    c.q4U[4 * q] = c.cU[q];
+    c.q4U[4 * q + 1] = c.cV[q];
+    c.q4U[4 * q + 2] = c.AW[q];
+    c.q4U[4 * q + 3] = c.AS[q];
+    c.q4M[4 * q] = c.mU[q];
+    c.q4M[4 * q + 1] = c.mV[q];
+    c.q4M[4 * q + 2] = c.rrAu[q];
+    c.q4M[4 * q + 3] = c.rrAv[q];
+    c.q4O[4 * q] = c.uOc[q];
+    c.q4O[4 * q + 1] = c.vOc[q];
+    c.q4O[4 * q + 2] = c.mfC[q];
+    c.q4O[4 * q + 3] = c.Ph[q];
     c.pQrRz[2 * q] = c.qrA[q];
     c.pQrRz[2 * q + 1] = c.rAz[q];
     if (p.useAdaptiveEVP)   // veris/evp_solver.py:65-73, the state-only factor of alphaC

@@ -50,9 +50,9 @@ struct FastConsts {
     uint32_t *flags;
     T *rdxU_x, *rdxV_x, *dxV_x, *dxU_x;   // grid lengths varying with i
     T *xm4;    // the same four per row, interleaved (rdxV, rdxU, dxU, dxV): one 16-byte load
-    T *pUV;    // the U/V-point constants in pairs, pitch lp: (cU, cV), (AW, AS), (mU, mV), (rrAu, rrAv)
-    T *pAWS, *pMUV, *pRR;
-    T *pOc, *pMfPh, *pQrRz;   // row inputs in pairs: (uOc, vOc), (mfC, Ph), (qrA, rAz)
+    // the register walk's inputs in 16- and 8-byte groups, pitch lp:
+    // (cU, cV, AW, AS), (mU, mV, rrAu, rrAv), (uOc, vOc, mfC, Ph), (qrA, rAz)
+    T *q4U, *q4M, *q4O, *pQrRz;
     T *rdyV_y, *rdyU_y, *dyV_y, *dyU_y;   // grid lengths varying with j
 };
 constexpr int N_FAST_2D = 16;
@@ -79,8 +79,9 @@ size_t fast_layout(const Dims &d, char *base, FastConsts<T> *c, T *state[2][5], 
     T **ys[4] = {&c->rdyV_y, &c->rdyU_y, &c->dyV_y, &c->dyU_y};
     for (int q = 0; q < 4; ++q) *xs[q] = reinterpret_cast<T *>(take(fx));
     c->xm4 = reinterpret_cast<T *>(take(rup256((size_t)d.NX * 4 * sizeof(T))));
-    T **pairs[7] = {&c->pUV, &c->pAWS, &c->pMUV, &c->pRR, &c->pOc, &c->pMfPh, &c->pQrRz};
-    for (int q = 0; q < 7; ++q) *pairs[q] = reinterpret_cast<T *>(take(2 * f2));
+    T **quads[3] = {&c->q4U, &c->q4M, &c->q4O};
+    for (int q = 0; q < 3; ++q) *quads[q] = reinterpret_cast<T *>(take(4 * f2));
+    c->pQrRz = reinterpret_cast<T *>(take(2 * f2));
     for (int q = 0; q < 4; ++q) *ys[q] = reinterpret_cast<T *>(take(fy));
     for (int b = 0; b < 2; ++b)
         for (int q = 0; q < 5; ++q) state[b][q] = reinterpret_cast<T *>(take(f2));

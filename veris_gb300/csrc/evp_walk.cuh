@@ -65,13 +65,12 @@ __device__ __forceinline__ void load_row(Row &r, const FastConsts<float> &c, con
         r.s2 = __ldg(io.s2 + o);
     }
     r.s12 = __ldg(io.s12 + o);
-    const float2 oc = __ldg(reinterpret_cast<const float2 *>(c.pOc) + o);
-    const float2 mp = __ldg(reinterpret_cast<const float2 *>(c.pMfPh) + o);
+    const float4 om = __ldg(reinterpret_cast<const float4 *>(c.q4O) + o);
     const float2 qz = __ldg(reinterpret_cast<const float2 *>(c.pQrRz) + o);
-    r.uo = oc.x;
-    r.vo = oc.y;
-    r.mf = mp.x;
-    r.ph = mp.y;
+    r.uo = om.x;
+    r.vo = om.y;
+    r.mf = om.z;
+    r.ph = om.w;
     r.qr = qz.x;
     r.rz = qz.y;
     r.bf = BASAL ? __ldg(c.bfac + o) : 0.f;
@@ -137,22 +136,18 @@ __device__ __forceinline__ void walk_strip(const Dims &d, int64_t lp, const Halo
             if (t >= 3) {   // row t-1, for the next step
                 const int gn = gown + 1 == d.NX ? 0 : gown + 1;
                 const int64_t on = (int64_t)gn * lp + gj;
-                const float2 a = __ldg(reinterpret_cast<const float2 *>(c.pUV) + on);
-                const float2 b = __ldg(reinterpret_cast<const float2 *>(c.pAWS) + on);
-                const float2 m = __ldg(reinterpret_cast<const float2 *>(c.pMUV) + on);
-                const float2 r = __ldg(reinterpret_cast<const float2 *>(c.pRR) + on);
-                o_cU = a.x; o_cV = a.y; o_AW = b.x; o_AS = b.y;
-                o_mU = m.x; o_mV = m.y; o_rrAu = r.x; o_rrAv = r.y;
+                const float4 a = __ldg(reinterpret_cast<const float4 *>(c.q4U) + on);
+                const float4 m = __ldg(reinterpret_cast<const float4 *>(c.q4M) + on);
+                o_cU = a.x; o_cV = a.y; o_AW = a.z; o_AS = a.w;
+                o_mU = m.x; o_mV = m.y; o_rrAu = m.z; o_rrAv = m.w;
             }
         } else if (t >= 4) {
-            // the U/V-point constants in pairs: four 8-byte loads
+            // the U/V-point constants: two 16-byte loads
             const int64_t ob = (int64_t)gown * lp + gj;
-            const float2 a = __ldg(reinterpret_cast<const float2 *>(c.pUV) + ob);
-            const float2 b = __ldg(reinterpret_cast<const float2 *>(c.pAWS) + ob);
-            const float2 m = __ldg(reinterpret_cast<const float2 *>(c.pMUV) + ob);
-            const float2 r = __ldg(reinterpret_cast<const float2 *>(c.pRR) + ob);
-            cU = a.x; cV = a.y; AW = b.x; AS = b.y;
-            mU = m.x; mV = m.y; rrAu = r.x; rrAv = r.y;
+            const float4 a = __ldg(reinterpret_cast<const float4 *>(c.q4U) + ob);
+            const float4 m = __ldg(reinterpret_cast<const float4 *>(c.q4M) + ob);
+            cU = a.x; cV = a.y; AW = a.z; AS = a.w;
+            mU = m.x; mV = m.y; rrAu = m.z; rrAv = m.w;
         }
 
         // ---- A: e12 at Z points of row t
