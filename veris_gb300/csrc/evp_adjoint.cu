@@ -43,6 +43,7 @@ struct Io {
     const T *lu, *lv, *ls1, *ls2, *ls12; // adjoints of the outputs (pitch ldl)
     T *ou, *ov, *os1, *os2, *os12;       // adjoints of the inputs, accumulated (pitch lp)
     int64_t ldn, ldl;
+    int64_t sst = 1;   // element stride of u, v, un, vn: 1 planar, 4 in the register walk's (u, v, sigma1, sigma2) layout
 };
 
 // shared-memory regions (local coordinates, origin and size)
@@ -115,8 +116,8 @@ evp_adjoint_kernel(Dims d, int64_t lp, HaloFill h, FastConsts<T> c, FastScalars<
     for (int idx = tid; idx < RS::n(); idx += THREADS) {
         const int li = idx / RS::W + RS::r0, lj = idx % RS::W + RS::c0;
         const int64_t o = (int64_t)d.wxt(i0 + li) * lp + d.wyt(j0 + lj);
-        sU[idx] = io.u[o];
-        sV[idx] = io.v[o];
+        sU[idx] = io.u[o * io.sst];
+        sV[idx] = io.v[o * io.sst];
         sUo[idx] = c.uOc[o];
         sVo[idx] = c.vOc[o];
         sF[idx] = c.flags[o];
@@ -229,7 +230,7 @@ evp_adjoint_kernel(Dims d, int64_t lp, HaloFill h, FastConsts<T> c, FastScalars<
             if (BASAL) den += T(0.5) * AW * (sCb[RC::at(li, lj)] + sCb[RC::at(li - 1, lj)]);
             const bool guard = den == T(0);   // replaced by 1: a constant branch
             if (guard) den = T(1);
-            const T un = io.un[(int64_t)gi * io.ldn + gj];
+            const T un = io.un[((int64_t)gi * io.ldn + gj) * io.sst];
             const T lN = one_if<T>(f0, F_MU) * lu / den;
             const T lden = guard ? T(0) : -un * lu / den;
             atomic_add(&lU[XS(li, lj)], k.bU * mU * lN);
@@ -286,7 +287,7 @@ evp_adjoint_kernel(Dims d, int64_t lp, HaloFill h, FastConsts<T> c, FastScalars<
             if (BASAL) den += T(0.5) * AS * (sCb[RC::at(li, lj)] + sCb[RC::at(li, lj - 1)]);
             const bool guard = den == T(0);
             if (guard) den = T(1);
-            const T vnx = io.vn[(int64_t)gi * io.ldn + gj];
+            const T vnx = io.vn[((int64_t)gi * io.ldn + gj) * io.sst];
             const T lN = one_if<T>(f0, F_MV) * lv / den;
             const T lden = guard ? T(0) : -vnx * lv / den;
             atomic_add(&lV[XS(li, lj)], k.bU * mV * lN);
@@ -580,7 +581,8 @@ static int launch_adj_ti(const Dims &d, int64_t lp, const HaloFill &h, const Fas
 }
 
 // tile rows: 8 while 16-row tiles would leave SMs idle (fewer than two
-// tiles per SM), else 16 (less recomputed ring per cell)
+// tiles per SM), else 16 (less recomputed ring per cell); float32 goes down
+// to 4 the same way
 template <class T, bool B, bool R>
 static int launch_adj(const Dims &d, int64_t lp, const HaloFill &h, const FastConsts<T> &c, const FastScalars<T> &k,
                       const Io<T> &io, const Adj<T> &a, T rhoSea, cudaStream_t st) {
@@ -594,6 +596,13 @@ static int launch_adj(const Dims &d, int64_t lp, const HaloFill &h, const FastCo
         }
     }
     const long tiles16 = (long)((d.NY + TJ - 1) / TJ) * ((d.NX + 15) / 16);
+    if constexpr (sizeof(T) == 4) {
+        // float32 is bound by latency, not arithmetic: 4-row tiles (more
+        // recomputed ring, twice the CTAs) while 8-row tiles would leave SMs
+        // with fewer than two
+        const long tiles8 = (long)((d.NY + TJ - 1) / TJ) * ((d.NX + 7) / 8);
+        if (tiles8 < 2L * sms) return launch_adj_ti<T, B, R, 4>(d, lp, h, c, k, io, a, rhoSea, st);
+    }
     if (tiles16 < 2L * sms) return launch_adj_ti<T, B, R, 8>(d, lp, h, c, k, io, a, rhoSea, st);
     return launch_adj_ti<T, B, R, 16>(d, lp, h, c, k, io, a, rhoSea, st);
 }
@@ -724,13 +733,18 @@ static int evp_adjoint(const VerisGrid *g, const VerisParams *p, const VerisFiel
             if (cudaMemsetAsync(out[0], 0, 5 * pl.field, st) != cudaSuccess) return VERIS_ERR_LAUNCH;
             const int rs = taped ? ss : ss - s0;   // slot of this subcycle's input state
             Io<T> io;
+            // a float32 tape is written by the register walk in its own
+            // layout: (u, v, sigma1, sigma2) per point over the slot's first
+            // four fields
+            const bool quad = taped && sizeof(T) == 4;
             io.u = slot(segb, pl.field, rs, 0);
-            io.v = slot(segb, pl.field, rs, 1);
+            io.v = quad ? io.u + 1 : slot(segb, pl.field, rs, 1);
             io.s1 = slot(segb, pl.field, rs, 2);
             io.s2 = slot(segb, pl.field, rs, 3);
             io.s12 = slot(segb, pl.field, rs, 4);
             io.un = slot(segb, pl.field, rs + 1, 0);
-            io.vn = slot(segb, pl.field, rs + 1, 1);
+            io.vn = quad ? io.un + 1 : slot(segb, pl.field, rs + 1, 1);
+            io.sst = quad ? 4 : 1;
             io.ldn = lp;
             if (first) {
                 io.lu = lout[0]; io.lv = lout[1]; io.ls1 = lout[2]; io.ls2 = lout[3]; io.ls12 = lout[4];

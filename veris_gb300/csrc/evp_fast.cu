@@ -228,9 +228,9 @@ static int evp_fast(const VerisGrid *g, const VerisParams *p, const VerisFieldsF
     VERIS_REQUIRE(p && vs64 && uo && vo && s1o && s2o && s12o, VERIS_ERR_ARG);
     VERIS_REQUIRE(n >= 1, VERIS_ERR_ARG);
     const bool walker = sizeof(T) == 4 && (allow_tma >= 4 || allow_tma < 0);
-    // the walk's own subcycle chain runs on the paired state layout (not with
-    // a tape, whose slots the adjoint reads planar)
-    const bool paired = walker && tape == nullptr;
+    // the walk's own subcycle chain runs on its state layout; a float32 tape
+    // keeps that layout in every slot (the adjoint reads it so)
+    const bool paired = walker;
     if (walker ? walk_support(*p) : fast_support(*p)) return VERIS_ERR_UNSUPPORTED;
     const bool adapt = p->useAdaptiveEVP != 0;
     FastConsts<T> c;
@@ -270,8 +270,9 @@ static int evp_fast(const VerisGrid *g, const VerisParams *p, const VerisFieldsF
                                                {nullptr, nullptr, nullptr, nullptr, nullptr}};
                     float *const to[5] = {tslot(it + 1, 0), tslot(it + 1, 1), tslot(it + 1, 2), tslot(it + 1, 3),
                                           tslot(it + 1, 4)};
-                    if ((stt = evp_walk_subcycles(adapt, false, d, h, c, k, from, to, lp, 1, basal, turn,
-                                                  allow_tma < 0 ? 0 : allow_tma, walk_variant, st)) != VERIS_OK)
+                    if ((stt = evp_walk_subcycles(adapt, true, d, h, c, k, from, to, lp, 1, basal, turn,
+                                                  allow_tma < 0 ? 0 : allow_tma, walk_variant, st, true)) !=
+                        VERIS_OK)
                         return stt;
                     done = true;
                 }
@@ -281,6 +282,12 @@ static int evp_fast(const VerisGrid *g, const VerisParams *p, const VerisFieldsF
                              tslot(it + 1, 0), tslot(it + 1, 1), tslot(it + 1, 2), tslot(it + 1, 3), tslot(it + 1, 4),
                              lp};
                 if ((stt = fast_subcycle<T>(d, h, c, k, io, basal, turn, st)) != VERIS_OK) return stt;
+            }
+        }
+        if constexpr (sizeof(T) == 4) {
+            if (walker) {   // the last slot in the walk's layout
+                float *const o5[5] = {outs[0], outs[1], outs[2], outs[3], outs[4]};
+                return evp_walk_unpack(d, tslot(n, 0), tslot(n, 4), o5, d.ld, st);
             }
         }
         for (int q = 0; q < 5; ++q)

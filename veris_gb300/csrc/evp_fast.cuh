@@ -160,10 +160,15 @@ constexpr int N_WALK_VARIANTS = 4;
 // paired: the state buffers hold the walk's own layout ((u, v, sigma1,
 // sigma2) in 16 bytes per point over the four buffers, sigma12 alone; the
 // prep writes the first state so); the last subcycle writes planar `outs`
+// unless paired_outs
 int evp_walk_subcycles(bool adapt, bool paired, const Dims &d, const HaloFill &h, const FastConsts<float> &c,
                        const FastScalars<float> &k,
                        float *const state[2][5], float *const outs[5], int64_t ldo, int n, bool basal, bool turn,
-                       int rows, int variant, cudaStream_t st);
+                       int rows, int variant, cudaStream_t st, bool paired_outs = false);
+// the walk's layout (its first four fields at `quad`, sigma12 at `s12`, pitch
+// lp) -> five planar arrays of pitch ldo
+int evp_walk_unpack(const Dims &d, const float *quad, const float *s12, float *const outs[5], int64_t ldo,
+                    cudaStream_t st);
 
 template <class T>
 __device__ __forceinline__ T one_if(uint32_t f, uint32_t bit) { return (f & bit) ? T(1) : T(0); }

@@ -99,7 +99,7 @@ static int launch_v(int layout, bool adapt, bool basal, bool turn, const Dims &d
 int evp_walk_subcycles(bool adapt, bool paired, const Dims &d, const HaloFill &h, const FastConsts<float> &c,
                        const FastScalars<float> &k,
                        float *const state[2][5], float *const outs[5], int64_t ldo, int n, bool basal, bool turn,
-                       int rows, int variant, cudaStream_t st) {
+                       int rows, int variant, cudaStream_t st, bool paired_outs) {
     const int64_t lp = internal_pitch(d.NY);
     if ((rows != 0 && (rows < 4 || rows > 4096)) || variant < 0 || variant >= walk::N_VARIANTS) return VERIS_ERR_ARG;
     for (int it = 0; it < n; ++it) {
@@ -110,7 +110,7 @@ int evp_walk_subcycles(bool adapt, bool paired, const Dims &d, const HaloFill &h
                                dst[0], dst[1], dst[2], dst[3], dst[4], last ? ldo : lp};
         // paired: the state buffers hold (u, v, sigma1, sigma2) per point over
         // their four buffers; the last subcycle writes the caller's planar arrays
-        const int layout = paired ? (last ? 2 : 1) : 0;
+        const int layout = paired ? ((last && !paired_outs) ? 2 : 1) : 0;
         int stt;
         switch (variant) {
         case 1: stt = walk::launch_v<1>(layout, adapt, basal, turn, d, lp, h, c, k, io, rows, st); break;
@@ -121,6 +121,34 @@ int evp_walk_subcycles(bool adapt, bool paired, const Dims &d, const HaloFill &h
         if (stt != VERIS_OK) return stt;
     }
     return VERIS_OK;
+}
+
+}  // namespace veris
+
+namespace veris {
+
+// the walk's (u, v, sigma1, sigma2) layout (pitch lp) and planar sigma12 ->
+// five planar arrays of pitch ldo
+__global__ void unpack_walk_state_kernel(Dims d, int64_t lp, const float4 *q, const float *s12, float *u, float *v,
+                                         float *s1, float *s2, float *s12o, int64_t ldo) {
+    const int j = blockIdx.x * 32 + threadIdx.x, i = blockIdx.y * 8 + threadIdx.y;
+    if (i >= d.NX || j >= d.NY) return;
+    const int64_t o = (int64_t)i * lp + j, w = (int64_t)i * ldo + j;
+    const float4 a = q[o];
+    u[w] = a.x;
+    v[w] = a.y;
+    s1[w] = a.z;
+    s2[w] = a.w;
+    s12o[w] = s12[o];
+}
+
+int evp_walk_unpack(const Dims &d, const float *quad, const float *s12, float *const outs[5], int64_t ldo,
+                    cudaStream_t st) {
+    const int64_t lp = internal_pitch(d.NY);
+    dim3 g((d.NY + 31) / 32, (d.NX + 7) / 8);
+    unpack_walk_state_kernel<<<g, dim3(32, 8), 0, st>>>(d, lp, reinterpret_cast<const float4 *>(quad), s12,
+                                                         outs[0], outs[1], outs[2], outs[3], outs[4], ldo);
+    return launch_status();
 }
 
 }  // namespace veris
