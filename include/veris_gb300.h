@@ -266,7 +266,10 @@ int veris_bulkf_formula_lanl_f32(const VerisParams *p, int64_t n, const float *u
  * settings it does not cover (0 = all covered) and veris_evp_fast_check()
  * ORs into *violations_device the state properties it does not cover
  * (non-zero k1/k2 metric terms, masks other than 0/1, grid lengths varying
- * along both axes).  A non-zero answer means: use the plain form.
+ * along both axes).  A non-zero answer means: use the plain form.  Bit 128
+ * (cell areas rA, rAz, rAu, rAv varying along both axes) concerns only
+ * veris_evp_walk_solver_f32 and the float32 tape, which take the areas
+ * along j; the tile forms cover it.
  */
 size_t veris_evp_fast_workspace_bytes(const VerisGrid *g, int32_t elem_size);
 int veris_evp_fast_settings_check(const VerisParams *p);

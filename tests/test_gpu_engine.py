@@ -344,3 +344,26 @@ def test_walk_with_both_halos_refreshed(nx, ny):
         for k in range(5):
             e = G.rel_err(walk[k].double().cpu().numpy(), smem[k].double().cpu().numpy())
             assert e <= 1e-5, (nx, ny, rows, variant, k, e)
+
+
+def test_areas_along_both_axes_take_the_tile_form():
+    """Cell areas that vary along i as well: the engine runs the TMA-staged
+    form instead of the register walk (which holds the areas per column),
+    and the walk drop-in refuses the state."""
+    from veris_gb300.engine import SeaIceStep
+    from veris_gb300.evp_solver import evp_solver_fast
+    st = _prepared(96, 64, 5)
+    v = st.variables
+    scale = torch.linspace(0.9, 1.1, v.rA.shape[0], dtype=torch.float64, device="cuda")[:, None]
+    for n in ("rA", "rAu", "rAv", "rAz"):
+        getattr(v, n).mul_(scale)
+    for n, src in (("recip_rA", "rA"), ("recip_rAu", "rAu"), ("recip_rAv", "rAv")):
+        getattr(v, n).copy_(1.0 / getattr(v, src))
+    eng = SeaIceStep(st, precision="f32")
+    assert eng.area2d and eng.evp_form == "fast" and eng.f32_kernel == "tma"
+    with pytest.raises(ValueError):
+        evp_solver_fast(st, "f32", "walk", n_subcycles=3)
+    smem = evp_solver_fast(st, "f32", "smem", n_subcycles=10)
+    tma = evp_solver_fast(st, "f32", "tma", n_subcycles=10)
+    for k in range(5):
+        assert G.rel_err(tma[k].double().cpu().numpy(), smem[k].double().cpu().numpy()) <= 1e-5

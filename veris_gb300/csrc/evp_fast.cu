@@ -48,6 +48,9 @@ __global__ void fast_check_kernel(Fields<double> f, Dims d, int *viol) {
     if (f.recip_dyV[o] != f.recip_dyV[oj] || f.recip_dyU[o] != f.recip_dyU[oj] || f.dyV[o] != f.dyV[oj] ||
         f.dyU[o] != f.dyU[oj])
         v |= V_METRIC;
+    if (f.recip_rA[o] != f.recip_rA[oj] || f.rAz[o] != f.rAz[oj] || f.recip_rAu[o] != f.recip_rAu[oj] ||
+        f.recip_rAv[o] != f.recip_rAv[oj])
+        v |= V_AREA2D;
     if (v) atomicOr(viol, v);
 }
 
@@ -80,6 +83,8 @@ __global__ void fast_prep_kernel(VerisParams p, Fields<double> f, Dims d, int64_
     c.q4U[4 * q + 1] = c.cV[q];
     c.q4U[4 * q + 2] = c.AW[q];
     c.q4U[4 * q + 3] = c.AS[q];
+    c.pMUV[2 * q] = c.mU[q];
+    c.pMUV[2 * q + 1] = c.mV[q];
     c.q4M[4 * q] = c.mU[q];
     c.q4M[4 * q + 1] = c.mV[q];
     c.q4M[4 * q + 2] = c.rrAu[q];
@@ -131,6 +136,10 @@ __global__ void fast_prep_kernel(VerisParams p, Fields<double> f, Dims d, int64_
         c.rdyU_y[j] = (T)f.recip_dyU[o];
         c.dyV_y[j] = (T)f.dyV[o];
         c.dyU_y[j] = (T)f.dyU[o];
+        c.qrA_y[j] = (T)(0.25 * f.recip_rA[o]);
+        c.rAz_y[j] = (T)f.rAz[o];
+        c.rrAu_y[j] = (T)f.recip_rAu[o];
+        c.rrAv_y[j] = (T)f.recip_rAv[o];
     }
     if (paired) {   // the register walk's layout: (u, v, sigma1, sigma2) over the four buffers
         u[4 * q] = (T)f.uIce[o];

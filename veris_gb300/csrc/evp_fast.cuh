@@ -28,7 +28,8 @@ enum : uint32_t {
 
 // settings and state properties the fast forms do not cover
 enum : int {
-    V_ADAPT = 1, V_SLIP = 2, V_SECOND = 4, V_PRESS = 8, V_KTERMS = 16, V_MASKS = 32, V_METRIC = 64
+    V_ADAPT = 1, V_SLIP = 2, V_SECOND = 4, V_PRESS = 8, V_KTERMS = 16, V_MASKS = 32, V_METRIC = 64,
+    V_AREA2D = 128   // cell areas vary along both axes: the register walk (not the tile forms) needs them along j only
 };
 
 // device status word bits (first word of the fast workspace)
@@ -54,6 +55,8 @@ struct FastConsts {
     // (cU, cV, AW, AS), (mU, mV, rrAu, rrAv), (uOc, vOc, mfC, Ph), (qrA, rAz)
     T *q4U, *q4M, *q4O, *pQrRz;
     T *rdyV_y, *rdyU_y, *dyV_y, *dyU_y;   // grid lengths varying with j
+    T *qrA_y, *rAz_y, *rrAu_y, *rrAv_y;   // the register walk's cell areas (0.25/rA, rAz, 1/rAu, 1/rAv), along j
+    T *pMUV;   // (mU, mV) pairs, pitch lp: the register walk's U/V masses when its areas are 1-D
 };
 constexpr int N_FAST_2D = 16;
 
@@ -76,13 +79,14 @@ size_t fast_layout(const Dims &d, char *base, FastConsts<T> *c, T *state[2][5], 
     for (int q = 0; q < N_FAST_2D; ++q) *two[q] = reinterpret_cast<T *>(take(f2));
     c->flags = reinterpret_cast<uint32_t *>(take(fl));
     T **xs[4] = {&c->rdxU_x, &c->rdxV_x, &c->dxV_x, &c->dxU_x};
-    T **ys[4] = {&c->rdyV_y, &c->rdyU_y, &c->dyV_y, &c->dyU_y};
+    T **ys[8] = {&c->rdyV_y, &c->rdyU_y, &c->dyV_y, &c->dyU_y, &c->qrA_y, &c->rAz_y, &c->rrAu_y, &c->rrAv_y};
     for (int q = 0; q < 4; ++q) *xs[q] = reinterpret_cast<T *>(take(fx));
     c->xm4 = reinterpret_cast<T *>(take(rup256((size_t)d.NX * 4 * sizeof(T))));
     T **quads[3] = {&c->q4U, &c->q4M, &c->q4O};
     for (int q = 0; q < 3; ++q) *quads[q] = reinterpret_cast<T *>(take(4 * f2));
     c->pQrRz = reinterpret_cast<T *>(take(2 * f2));
-    for (int q = 0; q < 4; ++q) *ys[q] = reinterpret_cast<T *>(take(fy));
+    c->pMUV = reinterpret_cast<T *>(take(2 * f2));
+    for (int q = 0; q < 8; ++q) *ys[q] = reinterpret_cast<T *>(take(fy));
     for (int b = 0; b < 2; ++b)
         for (int q = 0; q < 5; ++q) state[b][q] = reinterpret_cast<T *>(take(f2));
     return off;

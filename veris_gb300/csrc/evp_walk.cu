@@ -29,7 +29,9 @@ evp_walk_kernel(Dims d, int64_t lp, HaloFill h, FastConsts<float> c, FastScalars
     const int w = blockIdx.x * WARPS + (threadIdx.x >> 5);
     if (w >= nwalks) return;   // whole warps only
     const int strip = w % nstrips, rb = w / nstrips;
-    walk_strip<BASAL, TURN, Variant<V>::UNROLL, Variant<V>::PRE, ADAPT, (L != 0), (L == 1)>(
+    // the single-domain walk takes the cell areas along j (the caller has
+    // checked that the state's areas vary along j only: V_AREA2D clear)
+    walk_strip<BASAL, TURN, Variant<V>::UNROLL, Variant<V>::PRE, ADAPT, (L != 0), (L == 1), true>(
         d, lp, h, c, k, io, rb * H, strip * TW, H, lane);
 }
 

@@ -48,7 +48,8 @@ struct Row {
 };
 
 // PIN: the state is the walk's four-value layout, io.u holding (u, v, sigma1, sigma2)
-template <bool BASAL, bool ADAPT = false, bool PIN = false>
+// A1D: the cell areas vary along j only (per-lane constants): qr, rz are not loaded
+template <bool BASAL, bool ADAPT = false, bool PIN = false, bool A1D = false>
 __device__ __forceinline__ void load_row(Row &r, const FastConsts<float> &c, const FastIO<float> &io, int64_t lp,
                                          int gi, int gj) {
     const int64_t o = (int64_t)gi * lp + gj;
@@ -66,7 +67,7 @@ __device__ __forceinline__ void load_row(Row &r, const FastConsts<float> &c, con
     }
     r.s12 = __ldg(io.s12 + o);
     const float4 om = __ldg(reinterpret_cast<const float4 *>(c.q4O) + o);
-    const float2 qz = __ldg(reinterpret_cast<const float2 *>(c.pQrRz) + o);
+    const float2 qz = A1D ? make_float2(0.f, 0.f) : __ldg(reinterpret_cast<const float2 *>(c.pQrRz) + o);
     r.uo = om.x;
     r.vo = om.y;
     r.mf = om.z;
@@ -92,9 +93,10 @@ __device__ __forceinline__ void load_row(Row &r, const FastConsts<float> &c, con
 // PIN / POUT: the input / output state is the walk's own ping-pong layout,
 // (u, v, sigma1, sigma2) in 16 bytes per point and sigma12 alone; with POUT
 // a row's stresses wait one walk step in registers and are stored with its
-// velocities.
+// velocities.  A1D: the cell areas (0.25/rA, rAz, 1/rAu, 1/rAv) vary along j
+// only and live in registers for the whole walk.
 template <bool BASAL, bool TURN, int UNROLL, bool PRE = false, bool ADAPT = false, bool PIN = false,
-          bool POUT = false>
+          bool POUT = false, bool A1D = false>
 __device__ __forceinline__ void walk_strip(const Dims &d, int64_t lp, const HaloFill &h, const FastConsts<float> &c,
                                            const FastScalars<float> &k, const FastIO<float> &io, int i0, int j0,
                                            int H, int lane) {
@@ -102,6 +104,13 @@ __device__ __forceinline__ void walk_strip(const Dims &d, int64_t lp, const Halo
     const int gj = d.wya(jl);
     const float rdyU = __ldg(c.rdyU_y + gj), rdyV = __ldg(c.rdyV_y + gj);
     const float dyV = __ldg(c.dyV_y + gj), dyU = __ldg(c.dyU_y + gj);
+    float qr_j = 0.f, rz_j = 0.f, rrAu_j = 0.f, rrAv_j = 0.f;
+    if (A1D) {
+        qr_j = __ldg(c.qrA_y + gj);
+        rz_j = __ldg(c.rAz_y + gj);
+        rrAu_j = __ldg(c.rrAu_y + gj);
+        rrAv_j = __ldg(c.rrAv_y + gj);
+    }
     const bool own_j = lane >= 2 && lane < 2 + TW && jl < d.NY;
     const bool images = (h.x_fill && (i0 < 4 || i0 + H > d.NX - 4)) || (h.y_fill && (j0 < 4 || j0 + TW > d.NY - 4));
     const int64_t ldo = io.ldo;
@@ -120,7 +129,7 @@ __device__ __forceinline__ void walk_strip(const Dims &d, int64_t lp, const Halo
     // row indices advance by one per step: wrapped incrementally (any walk length)
     int gnext = d.wxa(i0 - 2);   // row of the next prefetch
     int gown = d.wxa(i0 - 4);    // row of this step's own-point constants (row t-2)
-    load_row<BASAL, ADAPT, PIN>(Pf, c, io, lp, gnext, gj);
+    load_row<BASAL, ADAPT, PIN, A1D>(Pf, c, io, lp, gnext, gj);
     const int T = H + 4;   // rows i0-2 .. i0+H+1
     // UNROLL = 4 (the rotation period) would rename the row ages instead of
     // copying them; measured slower (register pressure), the kernels use 1
@@ -128,7 +137,7 @@ __device__ __forceinline__ void walk_strip(const Dims &d, int64_t lp, const Halo
     for (int t = 0; t < T; ++t) {
         N = Pf;
         gnext = gnext + 1 == d.NX ? 0 : gnext + 1;
-        if (t + 1 < T) load_row<BASAL, ADAPT, PIN>(Pf, c, io, lp, gnext, gj);
+        if (t + 1 < T) load_row<BASAL, ADAPT, PIN, A1D>(Pf, c, io, lp, gnext, gj);
         // own-point constants of row t-2 (stage D)
         float cU = 0.f, cV = 0.f, AW = 0.f, AS = 0.f, mU = 0.f, mV = 0.f, rrAu = 0.f, rrAv = 0.f;
         if (PRE) {
@@ -137,17 +146,27 @@ __device__ __forceinline__ void walk_strip(const Dims &d, int64_t lp, const Halo
                 const int gn = gown + 1 == d.NX ? 0 : gown + 1;
                 const int64_t on = (int64_t)gn * lp + gj;
                 const float4 a = __ldg(reinterpret_cast<const float4 *>(c.q4U) + on);
-                const float4 m = __ldg(reinterpret_cast<const float4 *>(c.q4M) + on);
                 o_cU = a.x; o_cV = a.y; o_AW = a.z; o_AS = a.w;
-                o_mU = m.x; o_mV = m.y; o_rrAu = m.z; o_rrAv = m.w;
+                if (A1D) {
+                    const float2 m = __ldg(reinterpret_cast<const float2 *>(c.pMUV) + on);
+                    o_mU = m.x; o_mV = m.y; o_rrAu = rrAu_j; o_rrAv = rrAv_j;
+                } else {
+                    const float4 m = __ldg(reinterpret_cast<const float4 *>(c.q4M) + on);
+                    o_mU = m.x; o_mV = m.y; o_rrAu = m.z; o_rrAv = m.w;
+                }
             }
         } else if (t >= 4) {
             // the U/V-point constants: two 16-byte loads
             const int64_t ob = (int64_t)gown * lp + gj;
             const float4 a = __ldg(reinterpret_cast<const float4 *>(c.q4U) + ob);
-            const float4 m = __ldg(reinterpret_cast<const float4 *>(c.q4M) + ob);
             cU = a.x; cV = a.y; AW = a.z; AS = a.w;
-            mU = m.x; mV = m.y; rrAu = m.z; rrAv = m.w;
+            if (A1D) {
+                const float2 m = __ldg(reinterpret_cast<const float2 *>(c.pMUV) + ob);
+                mU = m.x; mV = m.y; rrAu = rrAu_j; rrAv = rrAv_j;
+            } else {
+                const float4 m = __ldg(reinterpret_cast<const float4 *>(c.q4M) + ob);
+                mU = m.x; mV = m.y; rrAu = m.z; rrAv = m.w;
+            }
         }
 
         // ---- A: e12 at Z points of row t
@@ -157,7 +176,7 @@ __device__ __forceinline__ void walk_strip(const Dims &d, int64_t lp, const Halo
         const float hV = one_if<float>(N.f, F_MV) - one_if<float>(A.f, F_MV);
         const float us = up(N.u);
         const float e12n = rdyU * (mzh * (N.u - us) + hU * (N.u + us)) + N.rdxV * (mzh * (N.v - A.v) + hV * (N.v + A.v));
-        const float z2n = N.rz * (e12n * e12n);
+        const float z2n = (A1D ? rz_j : N.rz) * (e12n * e12n);
 
         float zeta_new = 0.f, s11_new = 0.f, s22_new = 0.f, cd_new = 0.f, cb_new = 0.f, fv_new = 0.f, fu_new = 0.f;
         float s12_new = 0.f, aC_new = 0.f, ns1 = 0.f, ns2 = 0.f;
@@ -167,7 +186,7 @@ __device__ __forceinline__ void walk_strip(const Dims &d, int64_t lp, const Halo
             const float vn = dn(A.v);
             const float e11 = (N.u - A.u) * A.rdxU * mInC;
             const float e22 = (vn - A.v) * rdyV * mInC;
-            const float e12c = A.qr * ((z2a + z2n) + (dn(z2a) + dn(z2n)));
+            const float e12c = (A1D ? qr_j : A.qr) * ((z2a + z2n) + (dn(z2a) + dn(z2n)));
             const float ep = e11 + e22, em = e11 - e22;
             const float delta = sqrt_approx(ep * ep + k.rsq * (em * em + 4.f * e12c));
             const float zeta = __fdividef(A.ph, delta + k.deltaMin);

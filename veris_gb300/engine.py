@@ -42,6 +42,9 @@ EVP_OUT = ("uIce", "vIce", "sigma1", "sigma2", "sigma12")
 GROWTH_OUT = ("hIceMean", "hSnowMean", "Area", "TSurf", "EmPmR", "forc_salt_surface_ice",
               "Qsw", "Qnet", "SeaIceLoad", "IcePenetSW", "recip_hIceMean")
 FILLED_AFTER_GROWTH = ("hIceMean", "hSnowMean", "Area", "forc_salt_surface_ice", "Qnet")
+# bit of veris_evp_fast_check: cell areas vary along both axes (the register
+# walk needs them along j only)
+V_AREA2D = 128
 HELD_FORCING = ("Qnet", "Qsw")
 
 
@@ -77,7 +80,16 @@ class SeaIceStep:
         e = lambda dt=torch.float64: torch.empty(self.shape, dtype=dt, device=self.device)
         self.evp_out = [e() for _ in EVP_OUT]
         self.tmp = [e() for _ in range(2)]
-        self.fast_violations = self._fast_violations()
+        viol = self._fast_violations()
+        # cell areas varying along both axes: only the register walk cannot
+        # take them (it holds them per column); the tile forms can
+        self.area2d = bool(viol & V_AREA2D)
+        self.fast_violations = viol & ~V_AREA2D
+        if self.area2d and precision == "f32" and self.f32_kernel == "walk":
+            if int(self.lib.veris_evp_fast_settings_check(ctypes.byref(self.params))):
+                self.fast_violations |= V_AREA2D   # the TMA form cannot run these settings either
+            else:
+                self.f32_kernel = "tma"
         if evp == "fast" and self.fast_violations:
             raise ValueError(f"the fast EVP form does not cover this state (violations {self.fast_violations:#x})")
         self.evp_form = "plain" if (evp == "plain" or self.fast_violations) else "fast"

@@ -83,11 +83,18 @@ def evp_solver_fast(state, precision="f32", form="tma", n_subcycles=None, return
     only: TMA-staged tiles), "walk" (float32 only: register-walking warps,
     ``rows`` output rows per walk) or "smem" (shared-memory tiles).  Results
     are in the arithmetic type.  Raises ``VerisError`` (status 7) for
-    settings the fast forms do not cover."""
+    settings the fast forms do not cover, and ``ValueError`` for the walk on
+    a state whose cell areas vary along both axes (it holds them per
+    column)."""
     import ctypes
     s = state.settings
     n = int(s.nEVPsteps if n_subcycles is None else n_subcycles)
     c = Call(state)
+    if precision == "f32" and form == "walk":
+        flag = torch.zeros(1, dtype=torch.int32, device=c.device)
+        check("evp_fast_check", c.lib.veris_evp_fast_check(*c.refs(), flag.data_ptr(), c.stream))
+        if int(flag.item()) & 128:
+            raise ValueError("the register walk needs cell areas varying along j only (V_AREA2D set)")
     dt = torch.float32 if precision == "f32" else torch.float64
     out = [torch.empty(c.shape, dtype=dt, device=c.device) for _ in range(5)]
     ws, wsb = c.workspace(c.lib.veris_evp_fast_workspace_bytes(c.refs()[0], 4 if precision == "f32" else 8))

@@ -91,6 +91,9 @@ class Trajectory:
         if self.n < 1:
             raise ValueError("n_steps must be >= 1")
         self.eng = SeaIceStep(state, precision, n_subcycles, evp="fast", hold_forcing=True)
+        if precision == "f32" and self.eng.area2d:
+            raise ValueError("float32 trajectories tape the register walk, which needs cell areas varying "
+                             "along j only; use precision='f64' for this grid")
         self.lib = self.eng.lib
         self.snaps = self.n - 1 if snapshots is None else max(0, min(int(snapshots), self.n - 1))
         self.K = int(evp_checkpoint_every)
