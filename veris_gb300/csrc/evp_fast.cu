@@ -121,6 +121,7 @@ __global__ void fast_prep_kernel(VerisParams p, Fields<double> f, Dims d, int64_
     fl |= fc > 0.0 ? F_SPOS : 0;
     fl |= fc < 0.0 ? F_SNEG : 0;
     c.flags[q] = fl;
+    c.flags16[q] = (uint16_t)fl;   // the flags use bits 0..10
     if (j == 0) {
         c.rdxU_x[i] = (T)f.recip_dxU[o];
         c.rdxV_x[i] = (T)f.recip_dxV[o];

@@ -57,6 +57,7 @@ struct FastConsts {
     T *rdyV_y, *rdyU_y, *dyV_y, *dyU_y;   // grid lengths varying with j
     T *qrA_y, *rAz_y, *rrAu_y, *rrAv_y;   // the register walk's cell areas (0.25/rA, rAz, 1/rAu, 1/rAv), along j
     T *pMUV;   // (mU, mV) pairs, pitch lp: the register walk's U/V masses when its areas are 1-D
+    uint16_t *flags16;   // the flag word's 11 bits, pitch lp: the register walk's copy
 };
 constexpr int N_FAST_2D = 16;
 
@@ -86,6 +87,7 @@ size_t fast_layout(const Dims &d, char *base, FastConsts<T> *c, T *state[2][5], 
     for (int q = 0; q < 3; ++q) *quads[q] = reinterpret_cast<T *>(take(4 * f2));
     c->pQrRz = reinterpret_cast<T *>(take(2 * f2));
     c->pMUV = reinterpret_cast<T *>(take(2 * f2));
+    c->flags16 = reinterpret_cast<uint16_t *>(take(rup256((size_t)d.NX * lp * sizeof(uint16_t))));
     for (int q = 0; q < 8; ++q) *ys[q] = reinterpret_cast<T *>(take(fy));
     for (int b = 0; b < 2; ++b)
         for (int q = 0; q < 5; ++q) state[b][q] = reinterpret_cast<T *>(take(f2));

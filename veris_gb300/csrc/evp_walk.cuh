@@ -76,7 +76,7 @@ __device__ __forceinline__ void load_row(Row &r, const FastConsts<float> &c, con
     r.rz = qz.y;
     r.bf = BASAL ? __ldg(c.bfac + o) : 0.f;
     r.ac = ADAPT ? __ldg(c.acf + o) : 0.f;
-    r.f = __ldg(c.flags + o);
+    r.f = __ldg(c.flags16 + o);
     const float4 m = __ldg(reinterpret_cast<const float4 *>(c.xm4) + gi);
     r.rdxV = m.x;
     r.rdxU = m.y;
