@@ -171,8 +171,12 @@ evp_batch_walk_kernel(const Member *mem, const int *walk_start, int nmem, int nw
         io.s2o = m.state[buf ^ 1][3];
         io.s12o = m.state[buf ^ 1][4];
         io.ldo = m.lp;
-        walk::walk_strip<BASAL, TURN, 1>(m.d, m.lp, m.h, m.c, k, io, (lt / nstrips) * H, (lt % nstrips) * walk::TW, H,
-                                         lane);
+        if ((__ldg(m.status + 1) & V_AREA2D) == 0)   // areas along j: held per lane
+            walk::walk_strip<BASAL, TURN, 1, false, false, false, false, true>(
+                m.d, m.lp, m.h, m.c, k, io, (lt / nstrips) * H, (lt % nstrips) * walk::TW, H, lane);
+        else
+            walk::walk_strip<BASAL, TURN, 1>(m.d, m.lp, m.h, m.c, k, io, (lt / nstrips) * H,
+                                             (lt % nstrips) * walk::TW, H, lane);
     }
 }
 
@@ -322,6 +326,10 @@ int veris_batch_prep_member_f32(int32_t n, const VerisGrid *grids, const VerisPa
     const Fields<double> &f = *reinterpret_cast<const Fields<double> *>(vs);
     cudaStream_t cs = (cudaStream_t)s;
     if ((st = fast_prep<float>(M.d, *p, f, M.c, M.state[0], cs)) != VERIS_OK) return st;
+    // the member's state checks into its status word 1: the walks take the
+    // cell areas along j (per lane) when they vary along j only
+    if (cudaMemsetAsync(M.status + 1, 0, sizeof(int), cs) != cudaSuccess) return VERIS_ERR_LAUNCH;
+    if ((st = veris_evp_fast_check(&grids[m], p, vs, M.status + 1, s)) != VERIS_OK) return st;
     dim3 g2((M.d.NY + 31) / 32, (M.d.NX + 7) / 8);
     forcing32_kernel<<<g2, dim3(32, 8), 0, cs>>>(f.WindForcingX, f.WindForcingY, M.d, M.lp, M.WX, M.WY);
     return launch_status();

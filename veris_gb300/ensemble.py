@@ -90,7 +90,9 @@ class Ensemble:
             flag.zero_()
             check("evp_fast_check", self.lib.veris_evp_fast_check(
                 ctypes.byref(call.grid), ctypes.byref(self.params), ctypes.byref(fields), flag.data_ptr(), stream))
-            if int(flag.item()):
+            # bit 128 (cell areas along both axes) only changes how the
+            # walks read the areas; the batch handles it per member
+            if int(flag.item()) & ~128:
                 raise ValueError(f"member {m} is outside the fast EVP form (violations {int(flag.item()):#x})")
             check("batch_prep_member", self.lib.veris_batch_prep_member_f32(
                 self.n, self.grids, ctypes.byref(self.params), self.ws.data_ptr(), wsb, m, ctypes.byref(fields),
