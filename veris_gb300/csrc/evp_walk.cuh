@@ -17,9 +17,12 @@
 // next row's inputs are loaded one step ahead.  Warps are independent; a CTA
 // is just a group of them.
 //
-// The inputs are read straight from the fast form's planar arrays (a
-// repacked float4/float2 layout was measured slower: its wider loads stalled
-// longer on the memory system at the same bytes).
+// The inputs come in 16-byte groups built by the fast form's preparation:
+// (uOc, vOc, mfC, Ph) per point, (cU, cV, AW, AS) and the U/V masses per U/V
+// point, the four row metrics per row, a 16-bit copy of the flag word, and
+// (with PIN) the state itself as (u, v, sigma1, sigma2).  The walk is bound
+// by its load/store instruction count and DRAM bytes, which these groups cut;
+// shuffles and arithmetic do not bind.
 #pragma once
 
 #include "evp_fast.cuh"
