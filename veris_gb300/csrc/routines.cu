@@ -141,11 +141,43 @@ __device__ __forceinline__ void tau_uv(const Ctx<T> &c, int i, int j, T &tauX, T
     tauY = T(0.5) * (ty0 + tys) * c.ld(c.f.iceMaskV, i, j);
 }
 
+// The U/V averages of the once-per-step C-point quantities (air stress,
+// ocean drag) take the C point of the output and its west or south
+// neighbour: a block first evaluates them at the (BY+1) x (BX+1) C points its
+// outputs touch (one evaluation, with its float64 square root, per point
+// instead of three), then averages from shared memory.  The evaluations are
+// the same calls with the same (wrapped) indices, so the results are
+// unchanged.
+template <class T, class F>
+__device__ __forceinline__ void tile_c_points(const Ctx<T> &c, T (*a)[BX + 1], T (*b)[BX + 1], F eval) {
+    const int i0 = blockIdx.y * BY - 1, j0 = blockIdx.x * BX - 1;
+    for (int e = threadIdx.y * BX + threadIdx.x; e < (BY + 1) * (BX + 1); e += BX * BY) {
+        const int r = e / (BX + 1), q = e - r * (BX + 1);
+        const int i = i0 + r, j = j0 + q;   // -1 at the first tiles: wrapped by the loads
+        T x = T(0), y = T(0);
+        if (i < c.d.NX && j < c.d.NY) eval(i, j, x, y);
+        a[r][q] = x;
+        if (b) b[r][q] = y;
+    }
+    __syncthreads();
+}
+
+// tau_uv from a block's tile of C-point stresses
 template <class T>
-__global__ void tau_xy_kernel(Ctx<T> c, T *tauX, T *tauY) {
+__device__ __forceinline__ void tau_uv_tile(const Ctx<T> &c, const T (*stx)[BX + 1], const T (*sty)[BX + 1], int i,
+                                            int j, T &tauX, T &tauY) {
+    const int r = threadIdx.y + 1, q = threadIdx.x + 1;
+    tauX = T(0.5) * (stx[r][q] + stx[r - 1][q]) * c.ld(c.f.iceMaskU, i, j);
+    tauY = T(0.5) * (sty[r][q] + sty[r][q - 1]) * c.ld(c.f.iceMaskV, i, j);
+}
+
+template <class T>
+__global__ void __launch_bounds__(BX * BY) tau_xy_kernel(Ctx<T> c, T *tauX, T *tauY) {
+    __shared__ T stx[BY + 1][BX + 1], sty[BY + 1][BX + 1];
+    tile_c_points(c, stx, sty, [&](int i, int j, T &x, T &y) { tau_c(c, i, j, x, y); });
     POINT_IJ
     T tX, tY;
-    tau_uv(c, i, j, tX, tY);
+    tau_uv_tile(c, stx, sty, i, j, tX, tY);
     tauX[k] = tX;
     tauY[k] = tY;
 }
@@ -164,10 +196,12 @@ __device__ __forceinline__ T phi_surf(const Ctx<T> &c, int i, int j) {
 }
 
 template <class T>
-__global__ void wind_forcing_kernel(Ctx<T> c, T *fxo, T *fyo) {
+__global__ void __launch_bounds__(BX * BY) wind_forcing_kernel(Ctx<T> c, T *fxo, T *fyo) {
+    __shared__ T stx[BY + 1][BX + 1], sty[BY + 1][BX + 1];
+    tile_c_points(c, stx, sty, [&](int i, int j, T &x, T &y) { tau_c(c, i, j, x, y); });
     POINT_IJ
     T tX, tY;
-    tau_uv(c, i, j, tX, tY);
+    tau_uv_tile(c, stx, sty, i, j, tX, tY);
     T fx = tX * c.ld(c.f.AreaW, i, j);
     T fy = tY * c.ld(c.f.AreaS, i, j);
     const T phi = phi_surf(c, i, j);
@@ -248,14 +282,16 @@ __global__ void stressdiv_kernel(Ctx<T> c, const T *s11, const T *s22, const T *
 
 // veris/ocean_stress.py:19-37 with the halo fill of :39 fused into the store
 template <class T>
-__global__ void ocean_stress_kernel(Ctx<T> c, HaloFill h, T *su, T *sv) {
-    POINT_IJ
-    (void)k;
+__global__ void __launch_bounds__(BX * BY) ocean_stress_kernel(Ctx<T> c, HaloFill h, T *su, T *sv) {
+    __shared__ T scd[BY + 1][BX + 1];
     const Fields<T> &f = c.f;
     const T *u = f.uIce, *v = f.vIce;
-    const T cd0 = ocean_drag_c(c, u, v, i, j);
-    const T cdw = ocean_drag_c(c, u, v, i - 1, j);
-    const T cds = ocean_drag_c(c, u, v, i, j - 1);
+    tile_c_points(c, scd, (T(*)[BX + 1]) nullptr,
+                  [&](int i, int j, T &x, T &) { x = ocean_drag_c(c, u, v, i, j); });
+    POINT_IJ
+    (void)k;
+    const int r = threadIdx.y + 1, q = threadIdx.x + 1;
+    const T cd0 = scd[r][q], cdw = scd[r - 1][q], cds = scd[r][q - 1];
     auto du = [&](int a, int b) { return c.ld(u, a, b) - c.ld(f.uOcean, a, b); };
     auto dv = [&](int a, int b) { return c.ld(v, a, b) - c.ld(f.vOcean, a, b); };
     const T sg = sgn(c.ld(f.fCori, i, j));
