@@ -97,6 +97,43 @@ def test_limiter_range():
     assert phi.min() >= 0 and phi.max() <= 2
 
 
+def test_advection_conserves_the_area_integral():
+    """On an all-ocean domain periodic in x the zonal flux divergence
+    telescopes and the meridional fluxes vanish at the y-halo land rows."""
+    from types import SimpleNamespace
+    from veris_gb300.synthetic import config_settings, make_state
+    a = make_state(36, 20, seed=5, land_fraction=0.0, ice_lat=0.0, init_velocity=0.3)
+    st = SimpleNamespace(variables=SimpleNamespace(**a), settings=config_settings("c1_4deg"))
+    v = st.variables
+    v.uIce, v.vIce = O.fill_overlap_uv(st, v.uIce.copy(), v.vIce.copy())
+    for k in ("hIceMean", "hSnowMean", "Area"):
+        setattr(v, k, O.fill_overlap(st, getattr(v, k).copy()))
+    I = (slice(2, -2), slice(2, -2))
+    for k, new in zip(("hIceMean", "hSnowMean", "Area"), O.Advection(st)):
+        old = getattr(v, k)
+        assert np.abs(new - old).max() > 1e-4 * np.abs(old).max(), k
+        s0, s1 = (v.rA[I] * old[I]).sum(), (v.rA[I] * new[I]).sum()
+        assert abs(s1 - s0) <= 1e-13 * abs(s0), (k, s0, s1)
+
+
+def test_step_zeroes_land():
+    """The outputs the reference masks are exactly zero on land after a step."""
+    from types import SimpleNamespace
+    from veris_gb300.synthetic import config_settings, make_state
+    a = make_state(36, 20, seed=6, land_fraction=0.3, ice_lat=0.0, init_velocity=0.2, init_stress=1000.0)
+    st = SimpleNamespace(variables=SimpleNamespace(**a), settings=config_settings("c1_4deg", nEVPsteps=10))
+    O.step(st)
+    v = st.variables
+    I = (slice(2, -2), slice(2, -2))
+    for k, m in (("uIce", "iceMaskU"), ("vIce", "iceMaskV"), ("sigma1", "iceMask"), ("sigma2", "iceMask"),
+                 ("hIceMean", "iceMask"), ("hSnowMean", "iceMask"), ("Area", "iceMask"),
+                 ("EmPmR", "maskInC"), ("forc_salt_surface_ice", "maskInC"),
+                 ("OceanStressU", "iceMaskU"), ("OceanStressV", "iceMaskV")):
+        land = getattr(v, m)[I] == 0
+        assert land.any(), m
+        assert np.all(getattr(v, k)[I][land] == 0.0), k
+
+
 def test_fill_overlap_idempotent():
     g = G.load("c1")
     st = G.initial_state(g)
