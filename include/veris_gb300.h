@@ -569,6 +569,18 @@ size_t veris_reduce_workspace_bytes(const VerisGrid *g);
 int veris_global_sum_f64(const VerisGrid *g, const double *A, const double *weight,
                          double *result, void *workspace, size_t workspace_bytes,
                          veris_stream_t s);
+/*
+ * No counterpart in the reference (NumPy carries NaN through silently):
+ * ORs `flag` into *status_device (device memory, sticky: the caller clears
+ * it) when any element of the n (1..8) padded arrays, halos included, is a
+ * NaN or an infinity.  Asynchronous; read the word after the stream.  The
+ * engine runs it once per step on its prognostic fields and reports
+ * VERIS_ERR_NAN.
+ */
+int veris_check_finite_f64(const VerisGrid *g, const double *const *arrays, int32_t n, int32_t flag,
+                           int32_t *status_device, veris_stream_t s);
+int veris_check_finite_f32(const VerisGrid *g, const float *const *arrays, int32_t n, int32_t flag,
+                           int32_t *status_device, veris_stream_t s);
 /* elementwise precision conversion of n values */
 int veris_convert_f64_to_f32(const double *src, float *dst, int64_t n, veris_stream_t s);
 int veris_convert_f32_to_f64(const float *src, double *dst, int64_t n, veris_stream_t s);

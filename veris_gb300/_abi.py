@@ -20,7 +20,9 @@ STATUS = {
     3: "non-finite value detected", 4: "device-side wait timed out",
     5: "CUDA launch or API call failed", 6: "invalid argument",
     7: "settings not supported by this entry point", 8: "workspace missing or too small",
+    9: "grid larger than a fixed-size entry point's scratch",
 }
+VERIS_ERR_NAN = 3
 
 
 class VerisError(RuntimeError):
@@ -197,6 +199,8 @@ SIGNATURES = {
     "veris_reduce_workspace_bytes": ([_G], _S),
     "veris_mbarrier_wait_probe": ([ctypes.c_int32, ctypes.c_uint32, _P, _P], _I),
     "veris_global_sum_f64": ([_G, _P, _P, _P, _P, _S, _P], _I),
+    "veris_check_finite_f64": ([_G, _P, ctypes.c_int32, ctypes.c_int32, _P, _P], _I),
+    "veris_check_finite_f32": ([_G, _P, ctypes.c_int32, ctypes.c_int32, _P, _P], _I),
     "veris_convert_f64_to_f32": ([_P, _P, _L, _P], _I),
     "veris_convert_f32_to_f64": ([_P, _P, _L, _P], _I),
 }

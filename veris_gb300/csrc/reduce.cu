@@ -53,6 +53,46 @@ __global__ void final_sum_kernel(const double *partial, double *result) {
     if (threadIdx.x == 0) *result = s;
 }
 
+// Non-finite detection over whole padded arrays (halos included): each
+// thread folds its elements into one flag, one warp vote, one atomicOr per
+// warp that saw a NaN or an infinity.  Sticky: the caller clears the word.
+constexpr int FIN_THREADS = 256;
+constexpr int FIN_MAX_ARRAYS = 8;
+
+template <class T>
+struct FiniteArgs {
+    const T *a[FIN_MAX_ARRAYS];
+};
+
+template <class T>
+__global__ void finite_check_kernel(FiniteArgs<T> args, Dims d, int32_t flag, int32_t *status) {
+    const T *a = args.a[blockIdx.y];
+    bool bad = false;
+    for (int i = blockIdx.x; i < d.NX; i += gridDim.x)   // rows, then columns: no index division
+        for (int j = threadIdx.x; j < d.NY; j += FIN_THREADS) bad |= !isfinite(a[d.raw(i, j)]);
+    if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(status, flag);
+}
+
+template <class T>
+static int check_finite(const VerisGrid *g, const T *const *arrays, int32_t n, int32_t flag, int32_t *status,
+                        veris_stream_t s) {
+    Dims d;
+    VERIS_CHECK_GRID(g, d);
+    VERIS_REQUIRE(arrays && status && n >= 1 && n <= FIN_MAX_ARRAYS && flag != 0, VERIS_ERR_ARG);
+    FiniteArgs<T> args{};
+    for (int k = 0; k < n; ++k) {
+        VERIS_REQUIRE(arrays[k], VERIS_ERR_ARG);
+        args.a[k] = arrays[k];
+    }
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0)
+        return VERIS_ERR_LAUNCH;
+    const int blocks = d.NX < sms * 4 ? d.NX : sms * 4;   // up to 4 CTAs per SM per array
+    finite_check_kernel<T><<<dim3(blocks, n), FIN_THREADS, 0, (cudaStream_t)s>>>(args, d, flag, status);
+    return launch_status();
+}
+
 }  // namespace veris
 
 using namespace veris;
@@ -62,6 +102,16 @@ extern "C" {
 size_t veris_reduce_workspace_bytes(const VerisGrid *g) {
     (void)g;
     return RED_BLOCKS * sizeof(double);
+}
+
+int veris_check_finite_f64(const VerisGrid *g, const double *const *arrays, int32_t n, int32_t flag,
+                           int32_t *status_device, veris_stream_t s) {
+    return check_finite<double>(g, arrays, n, flag, status_device, s);
+}
+
+int veris_check_finite_f32(const VerisGrid *g, const float *const *arrays, int32_t n, int32_t flag,
+                           int32_t *status_device, veris_stream_t s) {
+    return check_finite<float>(g, arrays, n, flag, status_device, s);
 }
 
 int veris_global_sum_f64(const VerisGrid *g, const double *A, const double *w, double *result, void *ws,

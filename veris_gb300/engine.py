@@ -41,6 +41,11 @@ DYNAMIC32 = ("uIce", "vIce", "sigma1", "sigma2", "sigma12",
 EVP_OUT = ("uIce", "vIce", "sigma1", "sigma2", "sigma12")
 GROWTH_OUT = ("hIceMean", "hSnowMean", "Area", "TSurf", "EmPmR", "forc_salt_surface_ice",
               "Qsw", "Qnet", "SeaIceLoad", "IcePenetSW", "recip_hIceMean")
+# the prognostic fields the once-per-step non-finite check reads: a NaN in
+# the dynamics reaches the velocities within the subcycles, one in the
+# thermodynamics the thickness or the surface temperature
+FINITE_CHECKED = ("uIce", "vIce", "hIceMean", "TSurf")
+STATUS_NONFINITE = 2
 FILLED_AFTER_GROWTH = ("hIceMean", "hSnowMean", "Area", "forc_salt_surface_ice", "Qnet")
 # bit of veris_evp_fast_check: cell areas vary along both axes (the register
 # walk needs them along j only)
@@ -50,7 +55,7 @@ HELD_FORCING = ("Qnet", "Qsw")
 
 class SeaIceStep:
     def __init__(self, state: VerisState, precision="f64", n_subcycles=None, evp="auto", hold_forcing=False,
-                 f32_kernel="walk", walk_rows=0, walk_variant=0):
+                 f32_kernel="walk", walk_rows=0, walk_variant=0, check_finite=True):
         if precision not in ("f64", "f32"):
             raise ValueError("precision must be 'f64' or 'f32'")
         if evp not in ("auto", "fast", "plain"):
@@ -119,6 +124,10 @@ class SeaIceStep:
         self.forcing = ({n: getattr(v, n).clone() for n in HELD_FORCING} if hold_forcing else None)
         self.graph = None
         self.launches_per_step = None
+        # sticky device status word: STATUS_NONFINITE once a step has left a
+        # NaN or an infinity in one of FINITE_CHECKED (one launch per step)
+        self.check_finite = bool(check_finite)
+        self.status_dev = torch.zeros(1, dtype=torch.int32, device=self.device)
         # fast forms: a buffer of veris_evp_tape_bytes() that the next eager
         # step's EVP fills with its subcycle states
         self.evp_tape = None
@@ -278,7 +287,25 @@ class SeaIceStep:
                                                              getattr(v, name).data_ptr(), st))
         n += len(FILLED_AFTER_GROWTH)
         mark("fill")
+        if self.check_finite:
+            ptrs = (ctypes.c_void_p * len(FINITE_CHECKED))(*[getattr(v, k).data_ptr() for k in FINITE_CHECKED])
+            check("check_finite", lib.veris_check_finite_f64(ctypes.byref(self.grid), ptrs, len(FINITE_CHECKED),
+                                                             STATUS_NONFINITE, self.status_dev.data_ptr(), st))
+            n += 1
         return n
+
+    def status(self):
+        """The sticky status bits of the steps so far (synchronises)."""
+        return int(self.status_dev.item())
+
+    def clear_status(self):
+        self.status_dev.zero_()
+
+    def check(self, status=None):
+        """Raise VerisError(VERIS_ERR_NAN) when a step left a NaN or an
+        infinity in the prognostic fields (``status``: a word already read)."""
+        if (self.status() if status is None else int(status)) & STATUS_NONFINITE:
+            raise _abi.VerisError("SeaIceStep: " + "/".join(FINITE_CHECKED), _abi.VERIS_ERR_NAN)
 
     def step(self):
         """Run one step (replays the CUDA graph when one was captured)."""

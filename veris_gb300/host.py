@@ -46,7 +46,7 @@ class HostCoupledStep:
         self.outputs = tuple(outputs)
         v = engine.state.variables
         self.h2d_bytes = sum(getattr(v, n).numel() * getattr(v, n).element_size() for n in self.inputs)
-        self.d2h_bytes = sum(getattr(v, n).numel() * getattr(v, n).element_size() for n in self.outputs)
+        self.d2h_bytes = sum(getattr(v, n).numel() * getattr(v, n).element_size() for n in self.outputs) + 4
         held = set(engine.forcing or ())   # restored on the main stream at the start of the step
         self.late = tuple(n for n in self.inputs if n in LATE_INPUTS and n not in held)
         self.early_out = tuple(n for n in self.outputs if n in EARLY_OUTPUTS)
@@ -54,6 +54,9 @@ class HostCoupledStep:
         self.graphs = {}
         self._side_in = torch.cuda.Stream(engine.device)
         self._side_out = torch.cuda.Stream(engine.device)
+        # the engine's status word comes back with the outputs: a step that
+        # left non-finite values raises VerisError(VERIS_ERR_NAN)
+        self._status_host = torch.zeros(1, dtype=torch.int32).pin_memory()
 
     def _enqueue(self, h_in, h_out, overlap):
         v = self.engine.state.variables
@@ -82,8 +85,14 @@ class HostCoupledStep:
         for n in self.outputs:
             if n not in early_out:
                 h_out[n].copy_(getattr(v, n), non_blocking=True)
+        self._status_host.copy_(self.engine.status_dev, non_blocking=True)
         if early_out:
             main.wait_stream(self._side_out)
+
+    def _checked(self, h_out):
+        if self.engine.check_finite:
+            self.engine.check(int(self._status_host[0]))
+        return h_out
 
     def host_buffers(self):
         """Pinned host copies of the current device state (inputs, outputs)."""
@@ -101,7 +110,7 @@ class HostCoupledStep:
         if not (self.use_graph and pinned):
             self._enqueue(h_in, h_out, overlap=pinned)
             torch.cuda.current_stream(dev).synchronize()
-            return h_out
+            return self._checked(h_out)
         key = (tuple(h_in[n].data_ptr() for n in self.inputs), tuple(h_out[n].data_ptr() for n in self.outputs))
         g = self.graphs.get(key)
         if g is None:
@@ -116,7 +125,7 @@ class HostCoupledStep:
             torch.cuda.current_stream(dev).wait_stream(s)
             torch.cuda.synchronize(dev)
             self.graphs[key] = g
-            return h_out
+            return self._checked(h_out)
         g.replay()
         torch.cuda.current_stream(dev).synchronize()
-        return h_out
+        return self._checked(h_out)
