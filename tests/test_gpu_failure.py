@@ -99,7 +99,13 @@ def test_engine_reports_a_nan_in_the_forcing(lib, precision):
     host = HostCoupledStep(eng)
     h_in, h_out = host.host_buffers()
     host.step(h_in, h_out)            # clean, through the host exchange
-    ice = np.argwhere(arrays["hIceMean"] > 0)[0]
+    # an interior ice point with wet U and V faces: the wind stress there
+    # feeds the momentum equation (a NaN in a halo point would stay in the
+    # halo, which the fill overwrites from the interior)
+    I = (slice(2, -2), slice(2, -2))
+    ok = ((arrays["hIceMean"][I] > 0) & (arrays["iceMaskU"][I] == 1) & (arrays["iceMaskV"][I] == 1)
+          & (arrays["iceMaskU"][3:-1, 2:-2] == 1))
+    ice = np.argwhere(ok)[0] + 2
     h_in["uWind"][tuple(ice)] = float("nan")
     with pytest.raises(VerisError) as e:
         host.step(h_in, h_out)
