@@ -26,6 +26,30 @@ int launch_status() {
     return e == cudaSuccess ? VERIS_OK : VERIS_ERR_LAUNCH;
 }
 
+int current_device() {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        return -1;
+    }
+    return dev >= 0 && dev < MAX_DEVICES ? dev : -1;
+}
+
+int sm_count() {
+    static std::atomic<int> cached[MAX_DEVICES];
+    const int dev = current_device();
+    if (dev < 0) return 0;
+    int n = cached[dev].load(std::memory_order_relaxed);
+    if (n == 0) {
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) {
+            cudaGetLastError();
+            return 0;
+        }
+        cached[dev].store(n, std::memory_order_relaxed);
+    }
+    return n;
+}
+
 template <class S, class D>
 __global__ void convert_kernel(const S *__restrict__ src, D *__restrict__ dst, int64_t n) {
     for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;

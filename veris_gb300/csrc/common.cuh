@@ -3,6 +3,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <atomic>
 #include <stdint.h>
 
 #include "veris_gb300.h"
@@ -169,6 +170,28 @@ inline HaloFill halo_fill_of(const VerisParams &p) {
 
 int check_grid(const VerisGrid *g, Dims *d);
 int launch_status();
+
+// One-time host-side configuration per device (kernel attributes, SM
+// counts): each call site keeps its own flags indexed by the current device,
+// so a process driving several GPUs configures every one of them.
+constexpr int MAX_DEVICES = 64;
+int current_device();   // -1 when unavailable or beyond MAX_DEVICES
+int sm_count();         // SMs of the current device (0 when unavailable)
+
+// raises kern's dynamic shared-memory limit to `bytes` once per device
+template <class K>
+inline bool smem_configured(std::atomic<bool> (&done)[MAX_DEVICES], K kern, int bytes) {
+    const int dev = current_device();
+    if (dev < 0) return false;
+    if (!done[dev].load(std::memory_order_acquire)) {
+        if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) != cudaSuccess) {
+            cudaGetLastError();
+            return false;
+        }
+        done[dev].store(true, std::memory_order_release);
+    }
+    return true;
+}
 
 }  // namespace veris
 

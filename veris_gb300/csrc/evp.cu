@@ -232,12 +232,8 @@ template <class T, bool A, bool Sd, bool B>
 static int launch_subcycle(const Ctx<T> &c, const HaloFill &h, const EvpIO<T> &io, cudaStream_t st) {
     auto kern = evp_subcycle_kernel<T, A, Sd, B>;
     const size_t sm = EvpSmem<T>::bytes();
-    static bool configured = false;
-    if (!configured) {
-        if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess)
-            return VERIS_ERR_LAUNCH;
-        configured = true;
-    }
+    static std::atomic<bool> configured[MAX_DEVICES];
+    if (!smem_configured(configured, kern, (int)sm)) return VERIS_ERR_LAUNCH;
     dim3 grid((c.d.NY + EVP_TJ - 1) / EVP_TJ, (c.d.NX + EVP_TI - 1) / EVP_TI);
     kern<<<grid, EVP_THREADS, sm, st>>>(c, h, io);
     return launch_status();

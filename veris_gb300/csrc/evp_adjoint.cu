@@ -569,12 +569,8 @@ static int launch_adj_ti(const Dims &d, int64_t lp, const HaloFill &h, const Fas
                          const FastScalars<T> &k, const Io<T> &io, const Adj<T> &a, T rhoSea, cudaStream_t st) {
     auto kern = evp_adjoint_kernel<T, B, R, TI>;
     const size_t sm = Smem<T, TI>::bytes();
-    static bool configured = false;
-    if (!configured) {
-        if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess)
-            return VERIS_ERR_LAUNCH;
-        configured = true;
-    }
+    static std::atomic<bool> configured[MAX_DEVICES];
+    if (!smem_configured(configured, kern, (int)sm)) return VERIS_ERR_LAUNCH;
     dim3 grid((d.NY + TJ - 1) / TJ, (d.NX + TI - 1) / TI);
     kern<<<grid, THREADS, sm, st>>>(d, lp, h, c, k, io, a, rhoSea);
     return launch_status();
@@ -586,15 +582,8 @@ static int launch_adj_ti(const Dims &d, int64_t lp, const HaloFill &h, const Fas
 template <class T, bool B, bool R>
 static int launch_adj(const Dims &d, int64_t lp, const HaloFill &h, const FastConsts<T> &c, const FastScalars<T> &k,
                       const Io<T> &io, const Adj<T> &a, T rhoSea, cudaStream_t st) {
-    static int sms = 0;
-    if (sms == 0) {
-        int dev = 0;
-        if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) !=
-                                                      cudaSuccess) {
-            cudaGetLastError();
-            sms = 152;
-        }
-    }
+    int sms = sm_count();
+    if (sms == 0) sms = 152;
     const long tiles16 = (long)((d.NY + TJ - 1) / TJ) * ((d.NX + 15) / 16);
     if constexpr (sizeof(T) == 4) {
         // float32 is bound by latency, not arithmetic: 4-row tiles (more

@@ -203,12 +203,8 @@ static int launch(const Member *mem, const int *ts, int nmem, int ntiles, const 
                   unsigned *queue, unsigned base, int blocks, cudaStream_t st) {
     auto kern = evp_batch_kernel<S, B, R>;
     const size_t sm = TileSmem<float, ShapeOf<S>::TI, ShapeOf<S>::TJ>::bytes();
-    static bool configured = false;
-    if (!configured) {
-        if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess)
-            return VERIS_ERR_LAUNCH;
-        configured = true;
-    }
+    static std::atomic<bool> configured[MAX_DEVICES];
+    if (!smem_configured(configured, kern, (int)sm)) return VERIS_ERR_LAUNCH;
     kern<<<blocks, FAST_THREADS, sm, st>>>(mem, ts, nmem, ntiles, k, buf, queue, base);
     return launch_status();
 }
@@ -239,14 +235,6 @@ static int launch_walk_s(bool basal, bool turn, const Member *mem, const int *ts
                     : launch_walk<true, false>(mem, ts, nmem, ntiles, k, buf, queue, base, blocks, H, st);
     return turn ? launch_walk<false, true>(mem, ts, nmem, ntiles, k, buf, queue, base, blocks, H, st)
                 : launch_walk<false, false>(mem, ts, nmem, ntiles, k, buf, queue, base, blocks, H, st);
-}
-
-static int sm_count() {
-    int dev = 0, n = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) !=
-                                                  cudaSuccess)
-        return 0;
-    return n;
 }
 
 }  // namespace batch

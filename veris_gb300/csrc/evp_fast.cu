@@ -181,12 +181,8 @@ static int launch_fast(const Dims &d, int64_t lp, const HaloFill &h, const FastC
                        const FastScalars<T> &k, const FastIO<T> &io, cudaStream_t st) {
     auto kern = evp_fast_kernel<T, B, R>;
     const size_t sm = FastSmem<T>::bytes();
-    static bool configured = false;
-    if (!configured) {
-        if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess)
-            return VERIS_ERR_LAUNCH;
-        configured = true;
-    }
+    static std::atomic<bool> configured[MAX_DEVICES];
+    if (!smem_configured(configured, kern, (int)sm)) return VERIS_ERR_LAUNCH;
     dim3 grid((d.NY + FastTile<T>::TJ - 1) / FastTile<T>::TJ, (d.NX + FastTile<T>::TI - 1) / FastTile<T>::TI);
     kern<<<grid, FAST_THREADS, sm, st>>>(d, lp, h, c, k, io);
     return launch_status();

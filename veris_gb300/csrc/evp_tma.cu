@@ -438,18 +438,10 @@ static bool encode(CUtensorMap *m, const void *base, bool is_uint, const Dims &d
     return res == CUDA_SUCCESS;
 }
 
-static int sm_count() {
-    static int n = 0;
-    if (n == 0) {
-        int dev = 0;
-        if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) !=
-                                                      cudaSuccess) {
-            cudaGetLastError();
-            n = 0;
-            return 1;
-        }
-    }
-    return n;
+// persistent grid: one CTA per SM (1 when the count is unavailable)
+static int persistent_ctas() {
+    const int n = sm_count();
+    return n > 0 ? n : 1;
 }
 
 template <bool B, bool R>
@@ -457,15 +449,11 @@ static int launch(const Maps &maps, const Dims &d, int64_t lp, const HaloFill &h
                   const FastScalars<float> &k, const Src &src, int buf, float *const dst[5], int64_t ldo,
                   int *status, cudaStream_t st) {
     auto kern = evp_tma_kernel<B, R>;
-    static bool configured = false;
-    if (!configured) {
-        if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES) != cudaSuccess)
-            return VERIS_ERR_LAUNCH;
-        configured = true;
-    }
+    static std::atomic<bool> configured[MAX_DEVICES];
+    if (!smem_configured(configured, kern, SMEM_BYTES)) return VERIS_ERR_LAUNCH;
     const int ntx = (d.NY + TO - 1) / TO, nti = (d.NX + TO - 1) / TO;
     const int ntiles = ntx * nti;
-    const int grid = ntiles < sm_count() ? ntiles : sm_count();
+    const int grid = ntiles < persistent_ctas() ? ntiles : persistent_ctas();
     kern<<<grid, THREADS, SMEM_BYTES, st>>>(maps, d, lp, h, c, k, src, buf, ntx, ntiles, dst[0], dst[1], dst[2],
                                             dst[3], dst[4], ldo, status);
     return launch_status();
