@@ -459,6 +459,16 @@ int veris_growth_f64(const VerisGrid *g, const VerisParams *p, const VerisFields
                      double *EmPmR, double *forc_salt_surface, double *Qsw, double *Qnet,
                      double *SeaIceLoad, double *IcePenetSW, double *recip_hIceMean,
                      veris_stream_t s);
+/*
+ * The same on the padded rows [row_begin, row_end) only (Growth is
+ * pointwise): a host exchange downloads the rows one launch finished while
+ * the next launch computes.  veris_growth_f64 is rows [0, nx+2*olx).
+ */
+int veris_growth_rows_f64(const VerisGrid *g, const VerisParams *p, const VerisFieldsF64 *vs,
+                          double *hIceMean, double *hSnowMean, double *Area, double *TSurf,
+                          double *EmPmR, double *forc_salt_surface, double *Qsw, double *Qnet,
+                          double *SeaIceLoad, double *IcePenetSW, double *recip_hIceMean,
+                          int32_t row_begin, int32_t row_end, veris_stream_t s);
 
 /* ---- adjoints of the step's other routines (float64) ------------------ */
 /*

@@ -97,18 +97,20 @@ def test_host_coupled_step_roundtrip():
     assert host.h2d_bytes == len(host.inputs) * st.variables.iceMask.numel() * 8
 
 
-@pytest.mark.parametrize("precision", ("f64", "f32"))
-def test_host_coupled_graph_equals_plain_steps(precision):
+@pytest.mark.parametrize("precision,veros_fill", [("f64", True), ("f32", True), ("f64", False)])
+def test_host_coupled_graph_equals_plain_steps(precision, veros_fill):
     """The captured host exchange (side-stream uploads of the Growth forcing,
-    early downloads of the dynamics outputs) gives the host exactly what an
-    engine step followed by plain copies gives, step after step, with new
-    host inputs every step."""
+    early downloads of the dynamics outputs and the clean-up overshoots,
+    Growth's outputs by row blocks while Growth runs, the rows the halo fill
+    rewrites after it; with both halos filled the filled fields wait for the
+    fill) gives the host exactly what an engine step followed by plain copies
+    gives, step after step, with new host inputs every step."""
     from veris_gb300.engine import SeaIceStep
     from veris_gb300.host import HostCoupledStep
     from veris_gb300.state import VerisState
     from veris_gb300.synthetic import config_settings, make_state
     arrays = make_state(120, 80, seed=2, init_velocity=0.05)
-    sett = config_settings("c3_1deg", nEVPsteps=40)
+    sett = config_settings("c3_1deg", nEVPsteps=40, veros_fill=veros_fill)
     a = VerisState.from_numpy(arrays, sett)
     b = VerisState.from_numpy(arrays, sett)
     host = HostCoupledStep(SeaIceStep(a, precision=precision))

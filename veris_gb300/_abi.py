@@ -196,6 +196,7 @@ SIGNATURES = {
     "veris_ridging_f64": ([_G, _Pa, _F, _P, _P], _I),
     "veris_solve4temp_f64": ([_G, _Pa, _F, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P], _I),
     "veris_growth_f64": ([_G, _Pa, _F] + [_P] * 11 + [_P], _I),
+    "veris_growth_rows_f64": ([_G, _Pa, _F] + [_P] * 11 + [ctypes.c_int32, ctypes.c_int32, _P], _I),
     "veris_reduce_workspace_bytes": ([_G], _S),
     "veris_mbarrier_wait_probe": ([ctypes.c_int32, ctypes.c_uint32, _P, _P], _I),
     "veris_global_sum_f64": ([_G, _P, _P, _P, _P, _S, _P], _I),

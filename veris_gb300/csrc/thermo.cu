@@ -485,10 +485,11 @@ struct GrowthPtrs {
     double *h, *hs, *A, *TSurf, *EmPmR, *forc_salt, *Qsw, *Qnet, *load, *pen, *rh;
 };
 
+// rows [i0, i1) of the padded array (Growth is pointwise)
 __global__ void __launch_bounds__(128) growth_kernel(VerisParams p, GrowthK gk, Fields<double> f, Dims d,
-                                                     GrowthPtrs out) {
-    const int j = blockIdx.x * 32 + threadIdx.x, i = blockIdx.y * 4 + threadIdx.y;
-    if (i >= d.NX || j >= d.NY) return;
+                                                     GrowthPtrs out, int i0, int i1) {
+    const int j = blockIdx.x * 32 + threadIdx.x, i = i0 + blockIdx.y * 4 + threadIdx.y;
+    if (i >= i1 || j >= d.NY) return;
     const int64_t o = d.raw(i, j);
     const GrowthOut<double> g = growth_point<double>(p, gk, f, o, __ldg(f.hIceMean + o), __ldg(f.hSnowMean + o),
                                                      __ldg(f.Area + o), __ldg(f.TSurf + o));
@@ -557,19 +558,30 @@ int veris_growth_adjoint_f64(const VerisGrid *g, const VerisParams *p, const Ver
     return launch_status();
 }
 
-int veris_growth_f64(const VerisGrid *g, const VerisParams *p, const VerisFieldsF64 *vs, double *h,
-                     double *hs, double *A, double *TSurf, double *EmPmR, double *forc_salt, double *Qsw,
-                     double *Qnet, double *load, double *pen, double *rh, veris_stream_t s) {
+int veris_growth_rows_f64(const VerisGrid *g, const VerisParams *p, const VerisFieldsF64 *vs, double *h,
+                          double *hs, double *A, double *TSurf, double *EmPmR, double *forc_salt, double *Qsw,
+                          double *Qnet, double *load, double *pen, double *rh, int32_t row_begin, int32_t row_end,
+                          veris_stream_t s) {
     Dims d;
     VERIS_CHECK_GRID(g, d);
     VERIS_REQUIRE(p && vs && h && hs && A && TSurf && EmPmR && forc_salt && Qsw && Qnet && load && pen && rh,
                   VERIS_ERR_ARG);
     VERIS_REQUIRE(p->nITC >= 1 && p->nITC <= 64, VERIS_ERR_ARG);
+    VERIS_REQUIRE(row_begin >= 0 && row_begin < row_end && row_end <= d.NX, VERIS_ERR_ARG);
     GrowthPtrs out{h, hs, A, TSurf, EmPmR, forc_salt, Qsw, Qnet, load, pen, rh};
-    dim3 gr((d.NY + 31) / 32, (d.NX + 3) / 4);
+    dim3 gr((d.NY + 31) / 32, (row_end - row_begin + 3) / 4);
     growth_kernel<<<gr, dim3(32, 4), 0, (cudaStream_t)s>>>(*p, growth_k(*p), *reinterpret_cast<const Fields<double> *>(vs), d,
-                                                            out);
+                                                            out, row_begin, row_end);
     return launch_status();
+}
+
+int veris_growth_f64(const VerisGrid *g, const VerisParams *p, const VerisFieldsF64 *vs, double *h,
+                     double *hs, double *A, double *TSurf, double *EmPmR, double *forc_salt, double *Qsw,
+                     double *Qnet, double *load, double *pen, double *rh, veris_stream_t s) {
+    Dims d;
+    VERIS_CHECK_GRID(g, d);
+    return veris_growth_rows_f64(g, p, vs, h, hs, A, TSurf, EmPmR, forc_salt, Qsw, Qnet, load, pen, rh, 0, d.NX,
+                                 s);
 }
 
 }  // extern "C"

@@ -169,12 +169,15 @@ class SeaIceStep:
                                                            self.stream))
 
     # --------------------------------------------------------------- step
-    def _enqueue(self, evp_events=None, marks=None):
+    def _enqueue(self, evp_events=None, marks=None, growth_chunks=1):
         """Enqueue one step on the current stream; returns the launch count.
-        ``marks(name)`` is called between phases (for event timing)."""
+        ``marks(name)`` is called between phases (for event timing);
+        with ``growth_chunks`` > 1 Growth runs as that many launches over
+        consecutive row blocks, each followed by ``marks("growth_rows",
+        (row_begin, row_end))``."""
         lib, v, st = self.lib, self.state.variables, self.stream
         r64 = self._refs(self.f64)
-        mark = marks if marks is not None else (lambda name: None)
+        mark = marks if marks is not None else (lambda name, rows=None: None)
         n = 0
         mark("start")
         if self.forcing is not None:
@@ -279,8 +282,16 @@ class SeaIceStep:
             v.os_hIceMean.data_ptr(), v.os_hSnowMean.data_ptr(), st))
         check("ridging", lib.veris_ridging_f64(*r64, v.Area.data_ptr(), st))
         mark("clean_up")
-        check("Growth", lib.veris_growth_f64(*r64, *[getattr(v, k).data_ptr() for k in GROWTH_OUT], st))
-        n += 3
+        outs = [getattr(v, k).data_ptr() for k in GROWTH_OUT]
+        if growth_chunks <= 1:
+            check("Growth", lib.veris_growth_f64(*r64, *outs, st))
+        else:
+            NX = self.shape[0]
+            for k in range(growth_chunks):
+                i0, i1 = NX * k // growth_chunks, NX * (k + 1) // growth_chunks
+                check("Growth", lib.veris_growth_rows_f64(*r64, *outs, i0, i1, st))
+                mark("growth_rows", (i0, i1))
+        n += 3 + max(growth_chunks, 1) - 1
         mark("growth")
         for name in FILLED_AFTER_GROWTH:
             check("fill_overlap", lib.veris_fill_overlap_f64(ctypes.byref(self.grid), ctypes.byref(self.params),
@@ -341,7 +352,7 @@ class SeaIceStep:
         {phase: milliseconds} after synchronising."""
         evs = []
 
-        def mark(name):
+        def mark(name, rows=None):
             e = torch.cuda.Event(enable_timing=True)
             e.record()
             evs.append((name, e))

@@ -28,6 +28,11 @@ LATE_INPUTS = ("theta", "ocSalt", "Qnet", "Qsw", "SWdown", "LWdown", "ATemp", "a
 # outputs final once the ice velocities and the ocean stress are: their
 # download overlaps advection and Growth
 EARLY_OUTPUTS = ("uIce", "vIce", "sigma1", "sigma2", "sigma12", "OceanStressU", "OceanStressV")
+# outputs final after the clean-up: their download overlaps Growth
+MID_OUTPUTS = ("os_hIceMean", "os_hSnowMean")
+# Growth runs as this many launches over row blocks; the rows of its outputs
+# that one launch finished are downloaded while the next computes
+GROWTH_CHUNKS = 4
 
 
 class HostCoupledStep:
@@ -36,9 +41,12 @@ class HostCoupledStep:
     With pinned host buffers the whole exchange is one CUDA graph per buffer
     set: the inputs the dynamics read are uploaded first, the forcing only
     Growth reads is uploaded on a second stream while the dynamics run, and
-    the velocities, stresses and ocean stress are downloaded on a third
-    stream while advection and Growth run; the rest follows Growth.  Other
-    host buffers take the same order eagerly on one stream."""
+    on a third stream the velocities, stresses and ocean stress are
+    downloaded while advection and Growth run, the overshoots of the
+    clean-up while Growth runs, and Growth's outputs by row blocks while
+    Growth computes the next block; the rows the halo fill rewrites follow
+    the fill.  Other host buffers take the same order eagerly on one
+    stream, Growth in one launch."""
 
     def __init__(self, engine, inputs=HOST_INPUTS, outputs=HOST_OUTPUTS, graph=True):
         self.engine = engine
@@ -50,6 +58,22 @@ class HostCoupledStep:
         held = set(engine.forcing or ())   # restored on the main stream at the start of the step
         self.late = tuple(n for n in self.inputs if n in LATE_INPUTS and n not in held)
         self.early_out = tuple(n for n in self.outputs if n in EARLY_OUTPUTS)
+        self.mid_out = tuple(n for n in self.outputs if n in MID_OUTPUTS)
+        # Growth's outputs go out by rows; the halo fill after Growth rewrites
+        # the x-halo rows of the filled fields (and, with the y halo filled
+        # too, columns of every row: those fields then wait for the fill)
+        from .engine import FILLED_AFTER_GROWTH, GROWTH_OUT
+        s = engine.state.settings
+        NX = engine.shape[0]
+        y_fill = not bool(getattr(s, "veros_fill", True))
+        self.row_out = {}   # name -> rows [lo, hi) final as soon as Growth wrote them
+        for n in self.outputs:
+            if n not in GROWTH_OUT or n in self.early_out or n in self.mid_out:
+                continue
+            if n not in FILLED_AFTER_GROWTH:
+                self.row_out[n] = (0, NX)
+            elif not y_fill:
+                self.row_out[n] = (int(s.olx), NX - int(s.olx))
         self.use_graph = graph
         self.graphs = {}
         self._side_in = torch.cuda.Stream(engine.device)
@@ -72,21 +96,48 @@ class HostCoupledStep:
                 for n in late:
                     getattr(v, n).copy_(h_in[n], non_blocking=True)
 
-        def mark(name):
-            if name == "ocean_stress" and early_out:
-                self._side_out.wait_stream(main)
-                with torch.cuda.stream(self._side_out):
-                    for n in early_out:
-                        h_out[n].copy_(getattr(v, n), non_blocking=True)
-            elif name == "clean_up" and late:   # Growth comes next
-                main.wait_stream(self._side_in)
+        mid_out = self.mid_out if overlap else ()
+        row_out = self.row_out if overlap else {}
+        done = {}   # rows of each row_out field already on their way
 
-        self.engine.launches_per_step = self.engine._enqueue(marks=mark)
+        def side(copies):
+            self._side_out.wait_stream(main)
+            with torch.cuda.stream(self._side_out):
+                for dst, src in copies:
+                    dst.copy_(src, non_blocking=True)
+
+        def mark(name, rows=None):
+            if name == "ocean_stress" and early_out:
+                side([(h_out[n], getattr(v, n)) for n in early_out])
+            elif name == "clean_up":
+                if mid_out:
+                    side([(h_out[n], getattr(v, n)) for n in mid_out])
+                if late:   # Growth comes next
+                    main.wait_stream(self._side_in)
+            elif name == "growth_rows" and row_out:
+                copies = []
+                for n, (lo, hi) in row_out.items():
+                    a, b = max(rows[0], lo), min(rows[1], hi)
+                    if a < b:
+                        copies.append((h_out[n][a:b], getattr(v, n)[a:b]))
+                        done.setdefault(n, []).append((a, b))
+                side(copies)
+
+        self.engine.launches_per_step = self.engine._enqueue(
+            marks=mark, growth_chunks=GROWTH_CHUNKS if row_out else 1)
+        NX = self.engine.shape[0]
         for n in self.outputs:
-            if n not in early_out:
-                h_out[n].copy_(getattr(v, n), non_blocking=True)
+            if n in early_out or n in mid_out:
+                continue
+            # the rows not sent yet (all of them for fields without early rows)
+            sent = sorted(done.get(n, []))
+            start = 0
+            for a, b in sent + [(NX, NX)]:
+                if start < a:
+                    h_out[n][start:a].copy_(getattr(v, n)[start:a], non_blocking=True)
+                start = max(start, b)
         self._status_host.copy_(self.engine.status_dev, non_blocking=True)
-        if early_out:
+        if early_out or mid_out or row_out:
             main.wait_stream(self._side_out)
 
     def _checked(self, h_out):
