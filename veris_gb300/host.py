@@ -21,10 +21,10 @@ HOST_OUTPUTS = ("hIceMean", "hSnowMean", "Area", "TSurf", "uIce", "vIce", "sigma
                 "recip_hIceMean", "OceanStressU", "OceanStressV", "os_hIceMean", "os_hSnowMean")
 
 
-# inputs only Growth reads (veris/growth.py, veris/solve4temp.py): their
-# upload overlaps the dynamics
+# inputs only the clean-up (TSurf) and Growth (veris/growth.py,
+# veris/solve4temp.py) read: their upload overlaps the dynamics
 LATE_INPUTS = ("theta", "ocSalt", "Qnet", "Qsw", "SWdown", "LWdown", "ATemp", "aqh", "precip", "snowfall",
-               "evap", "runoff")
+               "evap", "runoff", "wSpeed", "TSurf")
 # outputs final once the ice velocities and the ocean stress are: their
 # download overlaps advection and Growth
 EARLY_OUTPUTS = ("uIce", "vIce", "sigma1", "sigma2", "sigma12", "OceanStressU", "OceanStressV")
@@ -39,8 +39,9 @@ class HostCoupledStep:
     """Runs a ``SeaIceStep`` on host arrays: upload, step, download.
 
     With pinned host buffers the whole exchange is one CUDA graph per buffer
-    set: the inputs the dynamics read are uploaded first, the forcing only
-    Growth reads is uploaded on a second stream while the dynamics run, and
+    set: the inputs the dynamics read are uploaded first, the fields only
+    the clean-up and Growth read are uploaded on a second stream while the
+    dynamics run, and
     on a third stream the velocities, stresses and ocean stress are
     downloaded while advection and Growth run, the overshoots of the
     clean-up while Growth runs, and Growth's outputs by row blocks while
@@ -109,11 +110,10 @@ class HostCoupledStep:
         def mark(name, rows=None):
             if name == "ocean_stress" and early_out:
                 side([(h_out[n], getattr(v, n)) for n in early_out])
-            elif name == "clean_up":
-                if mid_out:
-                    side([(h_out[n], getattr(v, n)) for n in mid_out])
-                if late:   # Growth comes next
-                    main.wait_stream(self._side_in)
+            elif name == "advection" and late:   # the clean-up comes next
+                main.wait_stream(self._side_in)
+            elif name == "clean_up" and mid_out:
+                side([(h_out[n], getattr(v, n)) for n in mid_out])
             elif name == "growth_rows" and row_out:
                 copies = []
                 for n, (lo, hi) in row_out.items():
