@@ -72,8 +72,9 @@ def parse():
     ap.add_argument("--adjoint-steps", type=int, default=None)
     ap.add_argument("--adjoint-precision", default="f64", choices=("f64", "f32"))
     ap.add_argument("--snapshots", type=int, default=None, help="step snapshots (default: all)")
-    ap.add_argument("--evp-checkpoint-every", type=int, default=0,
-                    help="EVP subcycle checkpoint interval inside a step's adjoint (0: keep all)")
+    ap.add_argument("--evp-checkpoint-every", type=int, default=None,
+                    help="EVP subcycle checkpoint interval inside a step's adjoint "
+                         "(0: keep all; default: keep all when it fits in device memory)")
     ap.add_argument("--tape", default="auto", choices=("auto", "on", "off"),
                     help="keep every EVP subcycle state during the forward")
     ap.add_argument("--adjoint-repeats", type=int, default=2)

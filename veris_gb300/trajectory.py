@@ -72,7 +72,7 @@ def interior_mask(shape, olx=2, oly=2, device="cuda"):
 class Trajectory:
     """n float64 steps from the state's current values and their adjoint."""
 
-    def __init__(self, state, n_steps, n_subcycles=None, snapshots=None, evp_checkpoint_every=0, tape="auto",
+    def __init__(self, state, n_steps, n_subcycles=None, snapshots=None, evp_checkpoint_every=None, tape="auto",
                  tape_memory_fraction=0.6, precision="f64"):
         """``snapshots``: step snapshot slots (None: every step).  ``tape``:
         keep every EVP subcycle state of every step during the forward, so
@@ -80,7 +80,13 @@ class Trajectory:
         snapshotted and the tapes fit in ``tape_memory_fraction`` of the free
         device memory).  ``precision`` "f32": the forward is the engine's
         float32 step (float32 EVP and advection, float64 thermodynamics) and
-        the EVP adjoint runs in float32; the other adjoints stay float64."""
+        the EVP adjoint runs in float32; the other adjoints stay float64.
+        ``evp_checkpoint_every``: without tapes, the EVP adjoint of a step
+        recomputes its subcycles from checkpoints this many subcycles apart
+        (0: one segment, every subcycle state of the step stored, the
+        subcycles recomputed once; None: one segment when its store fits in
+        ``tape_memory_fraction`` of the free device memory, else the spacing
+        with the smallest workspace, about sqrt(subcycles))."""
         if precision not in ("f64", "f32"):
             raise ValueError("precision must be 'f64' or 'f32'")
         self.precision = precision
@@ -96,7 +102,8 @@ class Trajectory:
                              "along j only; use precision='f64' for this grid")
         self.lib = self.eng.lib
         self.snaps = self.n - 1 if snapshots is None else max(0, min(int(snapshots), self.n - 1))
-        self.K = int(evp_checkpoint_every)
+        self.K = 0 if evp_checkpoint_every is None else int(evp_checkpoint_every)
+        self._auto_K = evp_checkpoint_every is None
         self.cost, self.split = binomial_schedule(self.n, self.snaps)
         sh, dev = self.eng.shape, self.eng.device
         e = lambda: torch.empty(sh, dtype=torch.float64, device=dev)
@@ -155,6 +162,8 @@ class Trajectory:
             wsb = (self.lib.veris_evp_adjoint_taped_workspace_bytes_f32(g, self.eng.n_sub) if f32 else
                    self.lib.veris_evp_adjoint_taped_workspace_bytes(g, self.eng.n_sub))
         else:
+            if self._auto_K:
+                self.K = self._fitting_checkpoint_spacing(g, esize, tape_memory_fraction)
             wsb = self.lib.veris_evp_adjoint_workspace_bytes(g, esize, self.eng.n_sub, self.K)
         self.ws_evp = mk(wsb)
         # float32 EVP adjoint: its state adjoints in float32
@@ -284,6 +293,18 @@ class Trajectory:
         grads = {k: self.lam[k].clone() for k in CARRIED}
         coeffs = {k: self.lscal[i].clone() for i, k in enumerate(COEFFS)}
         return grads, coeffs, {k: t.clone() for k, t in self.ocean_grad.items()}
+
+    def _fitting_checkpoint_spacing(self, g, esize, fraction):
+        """0 (one segment: the subcycles recomputed once) when that workspace
+        fits in ``fraction`` of the free device memory; else the spacing
+        with the smallest workspace (checkpoints plus one segment, about
+        sqrt(subcycles) apart), which recomputes the subcycles twice."""
+        n = self.eng.n_sub
+        free = fraction * torch.cuda.mem_get_info(self.eng.device)[0]
+        ws = lambda K: int(self.lib.veris_evp_adjoint_workspace_bytes(g, esize, n, K))
+        if n < 2 or ws(0) <= free:
+            return 0
+        return min(range(1, n), key=ws)
 
     def _refs(self, table):
         return ctypes.byref(self.eng.grid), ctypes.byref(self.eng.params), ctypes.byref(table)
