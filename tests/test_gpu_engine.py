@@ -369,3 +369,25 @@ def test_areas_along_both_axes_take_the_tile_form():
     tma = evp_solver_fast(st, "f32", "tma", n_subcycles=10)
     for k in range(5):
         assert G.rel_err(tma[k].double().cpu().numpy(), smem[k].double().cpu().numpy()) <= 1e-5
+
+
+def test_growth_by_row_blocks_equals_one_launch():
+    """veris_growth_rows_f64 over uneven row blocks that tile the padded
+    array gives Growth's eleven outputs bit for bit; ranges outside the
+    array are refused before any launch."""
+    from veris_gb300.growth import Growth
+    from veris_gb300.state import Call
+    _g, st = gpu_state("moving")
+    whole = Growth(st)
+    c = Call(st)
+    out = c.empty(11)
+    NX = st.variables.iceMask.shape[0]
+    cuts = [0, 3, 7, NX // 2, NX - 1, NX]
+    for a, b in zip(cuts[:-1], cuts[1:]):
+        assert c.lib.veris_growth_rows_f64(*c.refs(), *[t.data_ptr() for t in out], a, b, c.stream) == 0
+    torch.cuda.synchronize()
+    for q, (x, y) in enumerate(zip(out, whole)):
+        assert torch.equal(x, y), q
+    ptrs = [t.data_ptr() for t in out]
+    for a, b in ((-1, 4), (4, 4), (5, 3), (0, NX + 1)):
+        assert c.lib.veris_growth_rows_f64(*c.refs(), *ptrs, a, b, c.stream) == 6, (a, b)
