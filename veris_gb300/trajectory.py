@@ -169,14 +169,24 @@ class Trajectory:
         # float32 EVP adjoint: its state adjoints in float32
         self.l32 = ([torch.empty(sh, dtype=torch.float32, device=dev) for _ in range(10)] if f32 else None)
         self.snap = {}
+        self._pool = []   # snapshot buffer sets no longer in use, reused before allocating
         self.stats = {"forward_steps": 0, "recomputed_steps": 0, "adjoint_steps": 0}
         self._graph_ok = False
         self.track_norms = False   # record |adjoint| after every step (a host sync per step)
 
     # ------------------------------------------------------------ state
     def _save(self):
+        """A copy of the carried state, in a buffer set from the pool when
+        one is free (no allocation inside a forward after the first)."""
         v = self.state.variables
-        return [getattr(v, k).clone() for k in CARRIED]
+        buf = self._pool.pop() if self._pool else [torch.empty_like(getattr(v, k)) for k in CARRIED]
+        for t, k in zip(buf, CARRIED):
+            t.copy_(getattr(v, k))
+        return buf
+
+    def _release(self, snap):
+        if snap is not None:
+            self._pool.append(snap)
 
     def _load(self, snap):
         v = self.state.variables
@@ -200,6 +210,7 @@ class Trajectory:
             x = self._save()
             self.eng.capture()          # its eager warm-up step moves the state
             self._load(x)
+            self._release(x)
             if self.tapes is not None:
                 dev = self.eng.device
                 g = torch.cuda.CUDAGraph()
@@ -222,6 +233,8 @@ class Trajectory:
         the snapshots of the schedule's first descent.  Leaves the final
         state in the state's variables."""
         self._ensure_graph()
+        for snap in self.snap.values():
+            self._release(snap)
         self.snap = {0: self._save()}
         keep, pos, left, t = set(), 0, self.n, self.snaps
         while left > 1 and t > 0:
@@ -266,7 +279,7 @@ class Trajectory:
         while stack:
             task = stack.pop()
             if task[0] == "free":
-                self.snap.pop(task[1], None)
+                self._release(self.snap.pop(task[1], None))
                 continue
             _, lo, hi, t = task
             if hi - lo == 1:
