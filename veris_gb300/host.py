@@ -35,6 +35,25 @@ MID_OUTPUTS = ("os_hIceMean", "os_hSnowMean")
 GROWTH_CHUNKS = 4
 
 
+def growth_row_plan(outputs, early_out, mid_out, NX, olx, veros_fill):
+    """{output name: padded rows [lo, hi) final as soon as Growth has
+    written them}.  Growth's outputs that the halo fill after Growth does not
+    touch are final on all rows; the filled ones are final on the rows the
+    x-halo fill leaves alone, unless the y halo is filled too (then columns
+    of every row change and they wait for the fill)."""
+    from .engine import FILLED_AFTER_GROWTH, GROWTH_OUT
+    y_fill = not bool(veros_fill)
+    plan = {}
+    for n in outputs:
+        if n not in GROWTH_OUT or n in early_out or n in mid_out:
+            continue
+        if n not in FILLED_AFTER_GROWTH:
+            plan[n] = (0, NX)
+        elif not y_fill:
+            plan[n] = (int(olx), NX - int(olx))
+    return plan
+
+
 class HostCoupledStep:
     """Runs a ``SeaIceStep`` on host arrays: upload, step, download.
 
@@ -60,21 +79,10 @@ class HostCoupledStep:
         self.late = tuple(n for n in self.inputs if n in LATE_INPUTS and n not in held)
         self.early_out = tuple(n for n in self.outputs if n in EARLY_OUTPUTS)
         self.mid_out = tuple(n for n in self.outputs if n in MID_OUTPUTS)
-        # Growth's outputs go out by rows; the halo fill after Growth rewrites
-        # the x-halo rows of the filled fields (and, with the y halo filled
-        # too, columns of every row: those fields then wait for the fill)
-        from .engine import FILLED_AFTER_GROWTH, GROWTH_OUT
+        # Growth's outputs go out by rows while Growth runs
         s = engine.state.settings
-        NX = engine.shape[0]
-        y_fill = not bool(getattr(s, "veros_fill", True))
-        self.row_out = {}   # name -> rows [lo, hi) final as soon as Growth wrote them
-        for n in self.outputs:
-            if n not in GROWTH_OUT or n in self.early_out or n in self.mid_out:
-                continue
-            if n not in FILLED_AFTER_GROWTH:
-                self.row_out[n] = (0, NX)
-            elif not y_fill:
-                self.row_out[n] = (int(s.olx), NX - int(s.olx))
+        self.row_out = growth_row_plan(self.outputs, self.early_out, self.mid_out, engine.shape[0], s.olx,
+                                       getattr(s, "veros_fill", True))
         self.use_graph = graph
         self.graphs = {}
         self._side_in = torch.cuda.Stream(engine.device)
