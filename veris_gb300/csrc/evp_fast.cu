@@ -9,10 +9,13 @@
 //   the six masks, the hemisphere and the "mass != 0" switches into one
 //   32-bit flag word per cell, and reduces the grid lengths (which vary along
 //   one axis only on the host model's grids) to 1-D vectors;
-// * float32: per subcycle the TMA-staged kernel (evp_tma.cu); where tensor
-//   maps cannot be built, and for float64, the shared-memory kernel below,
-//   which stages u, v, the ocean velocities and the flags of its tile plus a
-//   2-cell ring and reads every other array once per point it needs;
+// * float32: per subcycle the register-walking kernel (evp_walk.cu) or the
+//   TMA-staged kernel (evp_tma.cu); where tensor maps cannot be built, the
+//   shared-memory kernel below, which stages u, v, the ocean velocities and
+//   the flags of its tile plus a 2-cell ring and reads every other array
+//   once per point it needs;
+// * float64: the float64 tile kernel (evp_fast64.cu), arranged for GB300's
+//   float64 pipe;
 // * float32 instantiations contain no float64 arithmetic.
 //
 // Covers the default rheology (noSlip without second-order terms, no
@@ -79,24 +82,45 @@ __global__ void fast_prep_kernel(VerisParams p, Fields<double> f, Dims d, int64_
     c.vOc[q] = (T)f.vOcean[o];
     c.rrAu[q] = (T)f.recip_rAu[o];
     c.rrAv[q] = (T)f.recip_rAv[o];
-    c.q4U[4 * q] = c.cU[q];
-    c.q4U[4 * q + 1] = c.cV[q];
-    c.q4U[4 * q + 2] = c.AW[q];
-    c.q4U[4 * q + 3] = c.AS[q];
-    c.pMUV[2 * q] = c.mU[q];
-    c.pMUV[2 * q + 1] = c.mV[q];
-    c.q4M[4 * q] = c.mU[q];
-    c.q4M[4 * q + 1] = c.mV[q];
-    c.q4M[4 * q + 2] = c.rrAu[q];
-    c.q4M[4 * q + 3] = c.rrAv[q];
-    c.q4O[4 * q] = c.uOc[q];
-    c.q4O[4 * q + 1] = c.vOc[q];
-    c.q4O[4 * q + 2] = c.mfC[q];
-    c.q4O[4 * q + 3] = c.Ph[q];
-    c.pQrRz[2 * q] = c.qrA[q];
-    c.pQrRz[2 * q + 1] = c.rAz[q];
+    if constexpr (sizeof(T) == 4) {   // the register walk's grouped inputs
+        c.q4U[4 * q] = c.cU[q];
+        c.q4U[4 * q + 1] = c.cV[q];
+        c.q4U[4 * q + 2] = c.AW[q];
+        c.q4U[4 * q + 3] = c.AS[q];
+        c.pMUV[2 * q] = c.mU[q];
+        c.pMUV[2 * q + 1] = c.mV[q];
+        c.q4M[4 * q] = c.mU[q];
+        c.q4M[4 * q + 1] = c.mV[q];
+        c.q4M[4 * q + 2] = c.rrAu[q];
+        c.q4M[4 * q + 3] = c.rrAv[q];
+        c.q4O[4 * q] = c.uOc[q];
+        c.q4O[4 * q + 1] = c.vOc[q];
+        c.q4O[4 * q + 2] = c.mfC[q];
+        c.q4O[4 * q + 3] = c.Ph[q];
+        c.pQrRz[2 * q] = c.qrA[q];
+        c.pQrRz[2 * q + 1] = c.rAz[q];
+    }
     if (p.useAdaptiveEVP)   // veris/evp_solver.py:65-73, the state-only factor of alphaC
         c.acf[q] = (T)(p.EVPcFac * f.recip_rA[o] / fmax(f.SeaIceMassC[o], 1e-4));
+    if constexpr (sizeof(T) == 8) {   // the float64 subcycle's folded products
+        const double bU = p.evpBeta * rdt, bU1 = bU + rdt;
+        c.rsqrA[q] = f.recip_rA[o] / (p.PlasDefCoeff * p.PlasDefCoeff);
+        c.mf4[q] = 0.25 * f.SeaIceMassC[o] * f.fCori[o];
+        c.mUb1[q] = mU * bU1;
+        c.mVb1[q] = mV * bU1;
+        c.mUb[q] = bU * mU;
+        c.mVb[q] = bU * mV;
+        c.hAW[q] = 0.5 * p.cosWat * f.AreaW[o];
+        c.hAS[q] = 0.5 * p.cosWat * f.AreaS[o];
+        if (j == 0) {
+            c.rdxVh_x[i] = 0.5 * f.recip_dxV[o];
+            c.dxUh_x[i] = 0.5 * f.dxU[o];
+        }
+        if (i == 0) {
+            c.rdyUh_y[j] = 0.5 * f.recip_dyU[o];
+            c.dyVh_y[j] = 0.5 * f.dyV[o];
+        }
+    }
     if (BASAL) {
         const double A = f.Area[o];
         double b = 0.0;
@@ -161,8 +185,6 @@ template <class T>
 struct FastTile;
 template <>
 struct FastTile<float> { static constexpr int TI = 32, TJ = 32, MINB = 3; };
-template <>
-struct FastTile<double> { static constexpr int TI = 16, TJ = 32, MINB = 2; };
 
 template <class T>
 using FastSmem = TileSmem<T, FastTile<T>::TI, FastTile<T>::TJ>;
@@ -180,6 +202,7 @@ template <class T, bool B, bool R>
 static int launch_fast(const Dims &d, int64_t lp, const HaloFill &h, const FastConsts<T> &c,
                        const FastScalars<T> &k, const FastIO<T> &io, cudaStream_t st) {
     auto kern = evp_fast_kernel<T, B, R>;
+    static_assert(sizeof(T) == 4, "float64 subcycles run the float64 tile kernel (evp_fast64.cu)");
     const size_t sm = FastSmem<T>::bytes();
     static std::atomic<bool> configured[MAX_DEVICES];
     if (!smem_configured(configured, kern, (int)sm)) return VERIS_ERR_LAUNCH;
@@ -205,10 +228,16 @@ int fast_prep(const Dims &d, const VerisParams &p, const Fields<double> &f, cons
 template <class T>
 int fast_subcycle(const Dims &d, const HaloFill &h, const FastConsts<T> &c, const FastScalars<T> &k,
                   const FastIO<T> &io, bool basal, bool turn, cudaStream_t st) {
-    const int64_t lp = internal_pitch(d.NY);
-    if (basal)
-        return turn ? launch_fast<T, true, true>(d, lp, h, c, k, io, st) : launch_fast<T, true, false>(d, lp, h, c, k, io, st);
-    return turn ? launch_fast<T, false, true>(d, lp, h, c, k, io, st) : launch_fast<T, false, false>(d, lp, h, c, k, io, st);
+    if constexpr (sizeof(T) == 8) {
+        return fast64_subcycle(d, h, c, k, io, basal, turn, st);
+    } else {
+        const int64_t lp = internal_pitch(d.NY);
+        if (basal)
+            return turn ? launch_fast<T, true, true>(d, lp, h, c, k, io, st)
+                        : launch_fast<T, true, false>(d, lp, h, c, k, io, st);
+        return turn ? launch_fast<T, false, true>(d, lp, h, c, k, io, st)
+                    : launch_fast<T, false, false>(d, lp, h, c, k, io, st);
+    }
 }
 
 template int fast_prep<float>(const Dims &, const VerisParams &, const Fields<double> &, const FastConsts<float> &,
@@ -318,7 +347,9 @@ static int evp_fast(const VerisGrid *g, const VerisParams *p, const VerisFieldsF
         T *const *dst = last ? outs : state[(it + 1) % 2];
         FastIO<T> io{cur[0], cur[1], cur[2], cur[3], cur[4], dst[0], dst[1], dst[2], dst[3], dst[4],
                      last ? d.ld : lp};
-        if (basal)
+        if constexpr (sizeof(T) == 8)
+            stt = fast64_subcycle(d, h, c, k, io, basal, turn, st);
+        else if (basal)
             stt = turn ? launch_fast<T, true, true>(d, lp, h, c, k, io, st) : launch_fast<T, true, false>(d, lp, h, c, k, io, st);
         else
             stt = turn ? launch_fast<T, false, true>(d, lp, h, c, k, io, st) : launch_fast<T, false, false>(d, lp, h, c, k, io, st);

@@ -58,8 +58,18 @@ struct FastConsts {
     T *qrA_y, *rAz_y, *rrAu_y, *rrAv_y;   // the register walk's cell areas (0.25/rA, rAz, 1/rAu, 1/rAv), along j
     T *pMUV;   // (mU, mV) pairs, pitch lp: the register walk's U/V masses when its areas are 1-D
     uint16_t *flags16;   // the flag word's 11 bits, pitch lp: the register walk's copy
+    // float64 only (evp_fast64.cu): products the float64 subcycle would
+    // otherwise form on every subcycle, folded once per step
+    T *rsqrA;        // recip_rA / e^2 (C points)
+    T *mf4;          // 0.25 * SeaIceMassC * fCori
+    T *mUb1, *mVb1;  // mass * (beta + 1) / dt (U, V points)
+    T *mUb, *mVb;    // mass * beta / dt
+    T *hAW, *hAS;    // 0.5 * cos(water turning angle) * AreaW, AreaS
+    T *rdxVh_x, *dxUh_x;   // 0.5 * recip_dxV, 0.5 * dxU (along i)
+    T *rdyUh_y, *dyVh_y;   // 0.5 * recip_dyU, 0.5 * dyV (along j)
 };
 constexpr int N_FAST_2D = 16;
+constexpr int N_F64_2D = 8;
 
 __host__ __device__ inline int64_t internal_pitch(int NY) { return ((int64_t)NY + 7) / 8 * 8; }
 
@@ -89,6 +99,14 @@ size_t fast_layout(const Dims &d, char *base, FastConsts<T> *c, T *state[2][5], 
     c->pMUV = reinterpret_cast<T *>(take(2 * f2));
     c->flags16 = reinterpret_cast<uint16_t *>(take(rup256((size_t)d.NX * lp * sizeof(uint16_t))));
     for (int q = 0; q < 8; ++q) *ys[q] = reinterpret_cast<T *>(take(fy));
+    // the float64 subcycle's folded products (no space for float32)
+    const bool f64 = sizeof(T) == 8;
+    T **f64s[N_F64_2D] = {&c->rsqrA, &c->mf4, &c->mUb1, &c->mVb1, &c->mUb, &c->mVb, &c->hAW, &c->hAS};
+    for (int q = 0; q < N_F64_2D; ++q) *f64s[q] = reinterpret_cast<T *>(take(f64 ? f2 : 0));
+    c->rdxVh_x = reinterpret_cast<T *>(take(f64 ? fx : 0));
+    c->dxUh_x = reinterpret_cast<T *>(take(f64 ? fx : 0));
+    c->rdyUh_y = reinterpret_cast<T *>(take(f64 ? fy : 0));
+    c->dyVh_y = reinterpret_cast<T *>(take(f64 ? fy : 0));
     for (int b = 0; b < 2; ++b)
         for (int q = 0; q < 5; ++q) state[b][q] = reinterpret_cast<T *>(take(f2));
     return off;
@@ -149,6 +167,9 @@ int fast_prep(const Dims &d, const VerisParams &p, const Fields<double> &f, cons
 template <class T>
 int fast_subcycle(const Dims &d, const HaloFill &h, const FastConsts<T> &c, const FastScalars<T> &k,
                   const FastIO<T> &io, bool basal, bool turn, cudaStream_t st);
+// one float64 subcycle with the float64 tile kernel (evp_fast64.cu)
+int fast64_subcycle(const Dims &d, const HaloFill &h, const FastConsts<double> &c, const FastScalars<double> &k,
+                    const FastIO<double> &io, bool basal, bool turn, cudaStream_t st);
 
 // n float32 subcycles with the TMA-staged kernel, reading state[0] first and
 // writing the last subcycle into outs.  Returns VERIS_ERR_UNSUPPORTED (having
