@@ -8,19 +8,30 @@ Workload (default): the 0.25-degree single domain, 1440 x 720 interior cells,
 bench step is one full sea-ice time step (dynamics preparation, 500 EVP
 subcycles, ocean stress, advection, clean-up, growth, halo fills).
 
-The headline ``value`` runs the mixed-precision step (float32 EVP and
-advection, float64 thermodynamics and budgets) replayed as one CUDA graph,
+The headline ``value`` is the float64 step (the drop-in arithmetic, the
+same precision as the reference's NumPy path) replayed as one CUDA graph,
 with inputs resident in HBM; L2 is flushed (a 512 MiB write) before every
 timed step and the flush is outside the timed events.  The metric counts
-interior cells x subcycles over the whole step time.  Also reported: the
-plain float64 step on the same inputs, the float32-vs-float64 errors per
-field, the end-to-end rate through host buffers, the EVP kernel's roofline
-and a CPU baseline (the NumPy oracle on one core, bounded sample).
+interior cells x subcycles over the whole step time.  ``e2e`` is the same
+step through the host coupling (pinned host arrays uploaded, the step's
+outputs downloaded, every step).  ``roofline`` is the float64 subcycle
+kernel's: bound by GB300's float64 pipe (2 lanes per SM and cycle), with
+its HBM fraction beside it.
+
+Also reported, each in its own block: ``fp32`` (the mixed-precision step:
+float32 EVP and advection, float64 thermodynamics and budgets; its rate,
+end-to-end rate, walk-kernel HBM roofline, error against the float64 step
+after one and N steps, and the branch flips behind the error), ``c5``
+(the 3600 x 1800 grid: float64 and float32 step rates, walk roofline,
+float32 errors, and the error float64 arithmetic makes from inputs rounded
+to float32), ``routines`` (free drift, bulk formula, residuals),
+``conservation`` (float64 budgets of the timed steps) and ``cpu_baseline``
+(the NumPy oracle on one core, bounded sample).
 
 ``--impl reference`` times the reference's CPU algorithm (the NumPy oracle,
 a restatement of the reference that is bit-identical to it on the golden
-fixtures) on the host cores, each step a bounded sample extrapolated to a
-full 500-subcycle step.
+fixtures) on all host cores, each step a bounded sample of 20 subcycles
+extrapolated to a full step.
 
 With ``--gpus N > 1`` (under torchrun) every rank runs an independent replica
 (the workload does not shard: one domain per GPU), ``scaling`` is weak and
@@ -41,6 +52,10 @@ import numpy as np  # noqa: E402
 
 BYTES_PER_CELL_SUBCYCLE = {"f32": 83, "f64": 163}
 METRIC = "EVP Gcell-subcycles/s"
+# EVP subcycles each CPU sample times (the rest of the step is timed once)
+CPU_SAMPLE_SUBCYCLES = 20
+# float64 lanes GB300's float64 pipe retires per SM and cycle
+FP64_LANES_PER_SM_CYCLE = 2
 
 
 def parse():
@@ -50,10 +65,13 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=("ours", "reference"))
     ap.add_argument("--config", default="c2_quarterdeg")
-    ap.add_argument("--precision", default="f32", choices=("f32", "f64"))
+    ap.add_argument("--precision", default="f64", choices=("f32", "f64"),
+                    help="precision of the headline step (f64: the drop-in arithmetic)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-fp64", action="store_true", help="skip the float64 comparison leg")
+    ap.add_argument("--no-fp32", action="store_true", help="skip the float32 block")
+    ap.add_argument("--no-fp64", action="store_true", help="(--precision f32) skip the float64 comparison")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-c5", action="store_true", help="skip the 3600 x 1800 block")
     ap.add_argument("--adaptive", action="store_true", help="adaptive EVP (useAdaptiveEVP)")
     ap.add_argument("--no-routines", action="store_true",
                     help="skip the free-drift, bulk-formula and residual measurements")
@@ -127,6 +145,13 @@ def replica_value(cells_per_rank, subcycles, steps, ms_max, ws):
     return ws * cells_per_rank * subcycles * steps / (ms_max / 1e3) / 1e9
 
 
+def workload_config(name, c, sett, n_sub):
+    """The workload's defining keys, printed alike by both arms."""
+    return {"workload": name, "nx": c["nx"], "ny": c["ny"], "subcycles": int(n_sub),
+            "evpAlpha": float(sett.evpAlpha), "evpBeta": float(sett.evpBeta),
+            "adaptive_evp": bool(sett.useAdaptiveEVP), "dt_s": float(c["dt"]), "cells": c["nx"] * c["ny"]}
+
+
 # -------------------------------------------------------------------- clocks
 
 class ClockSampler:
@@ -186,33 +211,47 @@ class ClockSampler:
 
 # ---------------------------------------------------------------------- peaks
 
-def hbm_peak():
+def measured_peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
         with open(path) as f:
-            return float(json.load(f)["hbm_gbs"]), "measured"
-    except (OSError, KeyError, ValueError):
-        return 6800.0, "fallback"
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
 
 
-def recorded_traffic(kernel, workload):
-    """DRAM bytes per launch of ``kernel`` on ``workload`` from an ncu capture
-    (profiles/roofline_traffic.json), or None."""
+def hbm_peak():
+    hbm = measured_peaks().get("hbm_gbs")
+    return (float(hbm), "measured") if hbm else (6800.0, "fallback")
+
+
+def fp64_peak(sm_count):
+    """GB300's float64 pipe: 2 lanes per SM and cycle at the measured maximum
+    SM clock, in G float64 operations per second."""
+    mhz = measured_peaks().get("sm_max_mhz") or 2070.0
+    return FP64_LANES_PER_SM_CYCLE * sm_count * float(mhz) * 1e6 / 1e9, float(mhz)
+
+
+def recorded(kernel, workload, what="traffic"):
+    """A per-launch figure of ``kernel`` on ``workload`` from an ncu capture
+    (profiles/roofline_traffic.json): DRAM bytes ("traffic") or float64-pipe
+    lane operations ("fp64_lane_ops"); None when not recorded."""
     path = os.path.join(ROOT, "profiles", "roofline_traffic.json")
     try:
         with open(path) as f:
-            return json.load(f).get(f"{kernel}/{workload}")
+            rec = json.load(f)
     except (OSError, ValueError):
         return None
+    key = f"{kernel}/{workload}" + ("" if what == "traffic" else f":{what}")
+    return rec.get(key)
 
 
 # ----------------------------------------------------------------- CPU legs
 
-def cpu_sample(arrays, sett, n_sub_sample, n_sub_full):
-    """Time the oracle (the reference's NumPy algorithm, one core) on a
-    bounded sample: ``n_sub_sample`` EVP subcycles, one advection, one
-    growth; extrapolated to a step of ``n_sub_full`` subcycles.  Returns
-    (seconds per full step, sample description)."""
+def cpu_fixed(arrays, sett):
+    """The oracle (the reference's NumPy algorithm, one core) on the parts of
+    a step outside the EVP subcycles: dynamics preparation, ocean stress,
+    advection, clean-up, growth.  Returns (seconds, the prepared state)."""
     from types import SimpleNamespace
     import copy
     from oracle import veris_oracle as O
@@ -225,73 +264,108 @@ def cpu_sample(arrays, sett, n_sub_sample, n_sub_full):
     v.WindForcingX, v.WindForcingY = O.WindForcingXY(st)
     v.SeaIceStrength = O.SeaIceStrength(st)
     t1 = time.perf_counter()
-    c = O.evp_carry(st)
-    for _ in range(n_sub_sample):
-        O.evp_subcycle(st, c)
-    t2 = time.perf_counter()
-    v.uIce, v.vIce = c["u"], c["v"]
+    prepared = SimpleNamespace(variables=SimpleNamespace(**vars(v)), settings=st.settings)
     v.OceanStressU, v.OceanStressV = O.OceanStressUV(st)
     v.hIceMean, v.hSnowMean, v.Area = O.Advection(st)
     out = O.clean_up_advection(st)
     v.hIceMean, v.hSnowMean, v.Area, v.TSurf, v.os_hIceMean, v.os_hSnowMean = out
     v.Area = O.ridging(st)
     O.Growth(st)
-    t3 = time.perf_counter()
-    per_sub = (t2 - t1) / n_sub_sample
-    full = (t1 - t0) + per_sub * n_sub_full + (t3 - t2)
-    desc = (f"NumPy oracle, 1 thread: {n_sub_sample} EVP subcycles + preparation + advection + "
-            f"growth timed ({t3 - t0:.1f} s), extrapolated to {n_sub_full} subcycles per step")
-    return full, desc
+    t2 = time.perf_counter()
+    return (t1 - t0) + (t2 - t1), prepared
+
+
+def cpu_subcycles(prepared, n):
+    """Seconds per EVP subcycle of the oracle over n subcycles (one core)."""
+    from oracle import veris_oracle as O
+    c = O.evp_carry(prepared)
+    t0 = time.perf_counter()
+    for _ in range(n):
+        O.evp_subcycle(prepared, c)
+    return (time.perf_counter() - t0) / n
+
+
+def cpu_step_estimate(arrays, sett, n_sample, n_full):
+    """One-core seconds per full step: the fixed parts timed once, plus
+    ``n_sample`` subcycles timed and scaled to ``n_full``."""
+    fixed, prepared = cpu_fixed(arrays, sett)
+    per_sub = cpu_subcycles(prepared, n_sample)
+    return fixed + per_sub * n_full, fixed, per_sub
 
 
 def _reference_worker(job):
-    """One bounded sample of the oracle in a worker process (one core)."""
+    """One replica of the oracle in a worker process (one core): the fixed
+    parts timed once, then one sample of subcycles per bench step."""
     import os as _os
     _os.environ.setdefault("OMP_NUM_THREADS", "1")
-    config, seed, n_sample, n_full = job
+    config, seed, n_sample, steps, warmup = job
     from veris_gb300.synthetic import CONFIGS, make_state, config_settings
     c = CONFIGS[config]
     arrays = make_state(c["nx"], c["ny"], seed=seed)
     sett = config_settings(config)
-    cpu_sample(arrays, sett, n_sample, n_full)          # warm-up
-    return cpu_sample(arrays, sett, n_sample, n_full)
+    cpu_fixed(arrays, sett)                              # warm-up
+    fixed, prepared = cpu_fixed(arrays, sett)
+    for _ in range(warmup):
+        cpu_subcycles(prepared, 2)
+    per_sub = [cpu_subcycles(prepared, n_sample) for _ in range(steps)]
+    return fixed, per_sub
+
+
+def jax_probe():
+    """Whether the reference's JAX backend could be timed on this host."""
+    try:
+        import jax  # noqa: F401
+        return "importable (not timed: the reference's JAX path needs Veros)"
+    except Exception as e:   # noqa: BLE001
+        return f"unavailable: {type(e).__name__}: {e}"
 
 
 def run_reference(args):
     """The reference's CPU algorithm (the NumPy oracle) on all host cores:
     one independent replica of the workload per core (NumPy elementwise code
-    uses one core each), every replica timing a bounded sample of a step;
-    value = all replicas' cells x subcycles over the slowest one's time."""
+    uses one core each).  Every replica times the step's parts outside the
+    EVP once and, per bench step, a sample of 20 subcycles; a step's time is
+    the fixed parts plus the sample scaled to the step's subcycles, and the
+    value is all replicas' cells x subcycles over the slowest replica's time."""
     ws, rank = int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
     import multiprocessing as mp
-    from veris_gb300.synthetic import CONFIGS
+    from veris_gb300.synthetic import CONFIGS, config_settings
     c = CONFIGS[args.config]
+    sett = config_settings(args.config)
     n_full = args.subcycles or c["n_evp"]
+    sett.nEVPsteps = n_full
     cells = c["nx"] * c["ny"]
-    n_sample = 2
+    n_sample = min(CPU_SAMPLE_SUBCYCLES, n_full)
     cores = max(1, os.cpu_count() or 1)
     ctx = mp.get_context("spawn")
-    times = []
-    desc = ""
+    t0 = time.perf_counter()
     with ctx.Pool(cores) as pool:
-        for k in range(args.warmup + args.steps):
-            res = pool.map(_reference_worker, [(args.config, args.seed + r, n_sample, n_full) for r in range(cores)])
-            if k >= args.warmup:
-                times.append(max(t for t, _d in res))
-                desc = res[0][1]
-    sec = float(np.sum(times))
+        res = pool.map(_reference_worker, [(args.config, args.seed + r, n_sample, args.steps, args.warmup)
+                                           for r in range(cores)])
+    wall = time.perf_counter() - t0
+    # step k takes, on replica r, fixed_r + per_sub_r[k] * n_full; the job's
+    # step time is the slowest replica's
+    step_s = [max(fx + ps[k] * n_full for fx, ps in res) for k in range(args.steps)]
+    sec = float(np.sum(step_s))
     value = cores * cells * n_full * args.steps / sec / 1e9
-    sample = f"{cores} processes x ({desc})"
+    fixed_med = float(np.median([fx for fx, _ in res]))
+    sub_med = float(np.median([np.median(ps) for _, ps in res]))
+    sample = (f"{cores} processes, NumPy oracle on one core each: per bench step {n_sample} EVP subcycles "
+              f"timed and scaled x{n_full / n_sample:g} to {n_full}, plus the step's other routines "
+              f"(preparation, ocean stress, advection, clean-up, growth) timed once "
+              f"(median {fixed_med:.2f} s; {sub_med:.3f} s per subcycle)")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "Gcell-subcycles/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": sec / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": args.config, "nx": c["nx"], "ny": c["ny"], "subcycles": n_full,
-                   "dt_s": c["dt"], "cells": cells, "parallelism": f"{cores} CPU replicas",
-                   "l2": "n/a (CPU)"},
+        "config": workload_config(args.config, c, sett, n_full),
+        "run": {"parallelism": f"{cores} CPU replicas", "l2": "n/a (CPU)",
+                "extrapolation": {"subcycles_timed_per_step": n_sample, "subcycles_per_step": n_full,
+                                  "factor": n_full / n_sample},
+                "wall_s": wall, "jax_cpu": jax_probe()},
         "cpu_baseline": {"value": value, "unit": "Gcell-subcycles/s", "cores": cores, "kind": "port",
                          "sample": sample, "host_cpus": os.cpu_count()},
         "e2e": {"value": value, "unit": "Gcell-subcycles/s", "h2d_bytes_per_step": 0,
@@ -313,6 +387,290 @@ def rel_errors(a, b):
     return {"max_rel": float(d.max()) / scale, "rms_rel": float(d.pow(2).mean().sqrt()) / scale}
 
 
+def make_engine(arrays, sett, dev, precision, args, walk_variant=None, budgets=False):
+    """A captured SeaIceStep on a fresh device copy of ``arrays`` (the
+    capture runs one eager step first); the float32 walk is tuned on the
+    workload unless a variant is given."""
+    from veris_gb300.engine import SeaIceStep
+    from veris_gb300.state import VerisState
+    state = VerisState.from_numpy(arrays, sett, device=dev)
+    wv = max(0, args.walk_variant) if walk_variant is None else walk_variant
+    eng = SeaIceStep(state, precision=precision, evp=args.evp, f32_kernel=args.f32_kernel,
+                     walk_rows=args.walk_rows, walk_variant=wv, budgets=budgets)
+    tuning = None
+    if (precision == "f32" and eng.f32_kernel == "walk" and eng.evp_form == "fast" and walk_variant is None
+            and args.walk_variant < 0):
+        from veris_gb300.autotune import tune_walk
+        tuning = tune_walk(eng)
+    eng.capture()
+    return eng, tuning
+
+
+def time_steps(eng, steps, warmup, flush, ws, dev, clocks=None):
+    """CUDA-event milliseconds of ``steps`` graph replays (L2 flushed before
+    each, outside the events), max over ranks; and the host wall seconds."""
+    import torch
+    for _ in range(warmup):
+        eng.step()
+    torch.cuda.synchronize(dev)
+    if clocks is not None:
+        clocks.start()
+        time.sleep(0.3)
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    barrier(ws)
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    for k in range(steps):
+        flush.zero_()
+        starts[k].record()
+        eng.step()
+        ends[k].record()
+    torch.cuda.synchronize(dev)
+    barrier(ws)
+    wall = time.perf_counter() - t0
+    clk = clocks.stop() if clocks is not None else None
+    ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
+    return max_over_ranks(ms, ws), wall, clk
+
+
+def evp_kernel_name(eng):
+    if eng.evp_form != "fast":
+        return f"evp_subcycle_kernel<{'double' if eng.precision == 'f64' else 'float'}>"
+    if eng.precision == "f64":
+        return "evp_f64_kernel"
+    return "evp_walk_kernel" if eng.f32_kernel == "walk" else "evp_tma_kernel"
+
+
+def evp_launch_us(eng, n_sub, flush):
+    """Average microseconds per EVP subcycle launch: CUDA events on the
+    launching stream around an eager step's EVP phase (the once-per-step
+    fold of the constants included), median of three, L2 flushed first."""
+    ms = []
+    for _ in range(3):
+        flush.zero_()
+        ms.append(eng.timed_step())
+    return float(np.median(ms)) * 1e3 / n_sub
+
+
+def roofline_hbm(kernel, workload, cells, us, precision):
+    peak, kind = hbm_peak()
+    algo = BYTES_PER_CELL_SUBCYCLE[precision] * cells
+    achieved = algo / (us * 1e-6) / 1e9
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": recorded(kernel, workload), "kernel": kernel, "algorithmic_bytes_per_launch": algo,
+            "avg_launch_us": us, "peak_source": f"{kind} HBM copy bandwidth"}
+
+
+def roofline_fp64(kernel, workload, cells, us, sm_count):
+    """The float64 subcycle's roofline: GB300's float64 pipe (its bound),
+    with the HBM fraction of the algorithmic bytes beside it.  ``achieved``
+    = the kernel's float64-pipe lane operations per launch (ncu, recorded in
+    profiles/roofline_traffic.json) over the live launch duration."""
+    peak, mhz = fp64_peak(sm_count)
+    ops = recorded(kernel, workload, "fp64_lane_ops")
+    achieved = ops / (us * 1e-6) / 1e9 if ops else None
+    return {"bound": "fp64_pipe", "achieved": achieved, "peak": peak, "unit": "Gop/s",
+            "frac": achieved / peak if achieved else None, "traffic": recorded(kernel, workload),
+            "kernel": kernel, "avg_launch_us": us, "fp64_lane_ops_per_launch": ops,
+            "fp64_lane_ops_per_cell": ops / cells if ops else None,
+            "peak_source": f"{FP64_LANES_PER_SM_CYCLE} float64 lanes per SM and cycle x {sm_count} SMs x "
+                           f"{mhz:g} MHz (the measured maximum SM clock)",
+            "hbm": roofline_hbm(kernel, workload, cells, us, "f64")}
+
+
+def e2e_of(eng, args, ws, cells, n_sub):
+    """The step through the host coupling: pinned host inputs uploaded and
+    outputs downloaded every step (HostCoupledStep, one graph per step)."""
+    from veris_gb300.host import HostCoupledStep
+    host = HostCoupledStep(eng)
+    h_in, h_out = host.host_buffers()
+    for _ in range(max(3, args.warmup)):   # the first call captures the exchange graph
+        host.step(h_in, h_out)
+    barrier(ws)
+    t0 = time.perf_counter()
+    ke = max(3, args.steps // 2)
+    for _ in range(ke):
+        host.step(h_in, h_out)
+    e2e_s = max_over_ranks(time.perf_counter() - t0, ws)
+    return {"value": ws * cells * n_sub * ke / e2e_s / 1e9, "unit": "Gcell-subcycles/s",
+            "h2d_bytes_per_step": host.h2d_bytes, "d2h_bytes_per_step": host.d2h_bytes, "steps": ke,
+            "ms_per_step": e2e_s / ke * 1e3,
+            "api": "veris_gb300.host.HostCoupledStep.step (pinned host arrays)"}
+
+
+def branch_states(v, s):
+    """Which side of the step's switches each interior cell (or face) is on
+    at the state ``v`` (torch tensors on the device): the ocean-drag floor
+    (veris/dynamics_routines.py:21-52), the thin-ice cut-off and the area
+    clips (veris/clean_up.py:5-47), the surface-temperature clamp at melting
+    (veris/solve4temp.py:146-157), the upwind direction and the superbee
+    branch of the zonal flux of hIceMean (veris/advection.py:94-175)."""
+    import torch
+    I = (slice(2, -2), slice(2, -2))
+    du = (v.uIce - v.uOcean) * v.maskInU
+    dv = (v.vIce - v.vOcean) * v.maskInV
+    a = du + torch.roll(du, -1, 0)
+    b = dv + torch.roll(dv, -1, 1)
+    t = 0.25 * (a * a + b * b)
+    dc = torch.where(v.fCori < 0, s.waterIceDrag_south, s.waterIceDrag) * s.rhoSea
+    out = {"ocean_drag_floor": ((dc * dc * t <= s.cDragMin ** 2) & (v.iceMask != 0))[I],
+           "no_ice": (v.hIceMean <= 0)[I],
+           "area_at_1": (v.Area >= 1.0)[I],
+           "area_at_min": ((v.Area <= s.Area_min) & (v.hIceMean > 0))[I],
+           "tsurf_at_melting": ((v.TSurf >= s.celsius2K) & (v.hIceMean > 0))[I]}
+    h = v.hIceMean
+    mask = v.iceMaskU * v.maskInU
+    uT = v.uIce * v.dyG * v.iceMaskU
+    Rjp = (h[3:] - h[2:-1]) * mask[3:]
+    Rj = (h[2:-1] - h[1:-2]) * mask[2:-1]
+    Rjm = (h[1:-2] - h[:-3]) * mask[1:-2]
+    up = uT[2:-1] > 0
+    cr = torch.where(up, Rjm, Rjp)
+    cr = torch.where(Rj.abs() * s.CrMax > cr.abs(), cr / Rj, torch.sign(cr) * s.CrMax * torch.sign(Rj))
+    region = torch.bucketize(cr.nan_to_num(0.0).contiguous(),
+                             torch.tensor([0.0, 0.5, 1.0, 2.0], dtype=cr.dtype, device=cr.device))
+    out["upwind_direction"] = up[:, 2:-2]
+    out["superbee_branch"] = region[:, 2:-2]
+    return out
+
+
+def branch_flips(v_a, v_b, s):
+    """Cells (faces) where two states sit on different sides of a switch."""
+    sa, sb = branch_states(v_a, s), branch_states(v_b, s)
+    flips = {k: int((sa[k] != sb[k]).sum()) for k in sa}
+    flips["cells"] = int(sa["no_ice"].numel())
+    return flips
+
+
+def compare_precisions(arrays, sett, dev, args, n_steps, walk_variant):
+    """The float32 and float64 steps from the same initial state: field
+    errors and branch flips after one and after ``n_steps`` steps."""
+    import torch
+    names = ("uIce", "vIce", "hIceMean", "hSnowMean", "Area", "TSurf", "Qnet")
+    e32, _ = make_engine(arrays, sett, dev, "f32", args, walk_variant=walk_variant)   # capture ran step 1
+    e64, _ = make_engine(arrays, sett, dev, "f64", args)
+    torch.cuda.synchronize(dev)
+    v32, v64 = e32.state.variables, e64.state.variables
+    errs1 = {n: rel_errors(getattr(v32, n), getattr(v64, n)) for n in names}
+    flips1 = branch_flips(v32, v64, sett)
+    for _ in range(n_steps - 1):
+        e64.step()
+        e32.step()
+    torch.cuda.synchronize(dev)
+    errs = {n: rel_errors(getattr(v32, n), getattr(v64, n)) for n in names}
+    flips = branch_flips(v32, v64, sett)
+    return {"after_1_step": errs1, "steps": n_steps, "fields": errs,
+            "branch_flips": {"after_1_step": flips1, f"after_{n_steps}_steps": flips},
+            "definition": "max_rel = max|a-b| / max|b|, rms_rel = rms(a-b) / max|b|; a branch flip is an "
+                          "interior cell (face) on different sides of a switch in the two states"}
+
+
+def conservation_summary(eng, steps):
+    """The float64 budgets of the last ``steps`` recorded steps: the drift
+    of the ice and snow volumes and the ice area over them, what advection,
+    the clean-up and the thermodynamics changed per step, and the ocean's
+    heat, fresh-water and salt fluxes (area-weighted interior sums)."""
+    rec = {k: v[-steps:] for k, v in eng.budget_records().items()}
+
+    def drift(start, end):
+        a, b = float(rec[start][0]), float(rec[end][-1])
+        return {"first": a, "last": b, "rel_change": (b - a) / a if a else None}
+
+    adv = max(abs(float(x - y) / float(y)) if y else 0.0
+              for x, y in zip(rec["ice_volume_advected"], rec["ice_volume_start"]))
+    return {"steps": len(rec["ice_volume_start"]),
+            "ice_volume_m3": drift("ice_volume_start", "ice_volume_end"),
+            "snow_volume_m3": drift("snow_volume_start", "snow_volume_end"),
+            "ice_area_m2": drift("ice_area_start", "ice_area_end"),
+            "advection_ice_volume_rel_change_max": adv,
+            "cleanup_ice_volume_change_m3_per_step": float(np.mean(rec["ice_volume_cleaned"]
+                                                                   - rec["ice_volume_advected"])),
+            "ice_overshoot_m3_per_step": float(np.mean(rec["ice_overshoot"])),
+            "thermodynamic_ice_volume_change_m3_per_step": float(np.mean(rec["ice_volume_end"]
+                                                                         - rec["ice_volume_cleaned"])),
+            "ocean_heat_loss_W": float(np.mean(rec["ocean_heat_loss"])),
+            "fresh_water_flux_kg_s": float(np.mean(rec["fresh_water_flux"])),
+            "salt_flux_kg_s": float(np.mean(rec["salt_flux"])),
+            "how": "float64 area-weighted interior sums inside the step's graph (veris_budget_sums_f64)"}
+
+
+def fp32_block(arrays, sett, dev, args, flush, ws, workload, cells, n_sub):
+    """The mixed-precision step (float32 EVP and advection, float64
+    thermodynamics, budgets and master state) on the same workload."""
+    eng, tuning = make_engine(arrays, sett, dev, "f32", args)
+    ms, wall, _ = time_steps(eng, args.steps, args.warmup, flush, ws, dev)
+    value = replica_value(cells, n_sub, args.steps, ms, ws)
+    us = evp_launch_us(eng, n_sub, flush)
+    out = {"value": value, "unit": "Gcell-subcycles/s", "ms_per_step": ms / args.steps, "dtype": "f32",
+           "gpu_launches": eng.launches_per_step * args.steps,
+           "roofline": roofline_hbm(evp_kernel_name(eng), workload, cells, us, "f32"),
+           "evp_form": eng.evp_form, "f32_kernel": eng.f32_kernel,
+           "walk": {"rows": eng.walk_rows or "auto", "variant": eng.walk_variant, "tuning": tuning}}
+    if not args.no_e2e:
+        out["e2e"] = e2e_of(eng, args, ws, cells, n_sub)
+    wv = eng.walk_variant
+    del eng
+    out["error_vs_fp64"] = compare_precisions(arrays, sett, dev, args, max(2, args.warmup + args.steps), wv)
+    return out
+
+
+def c5_block(args, dev, flush):
+    """The 3600 x 1800 workload (500 subcycles, dt 600 s): float64 and
+    float32 step rates, the walk's HBM roofline, float32 errors after one
+    step, and the error float64 arithmetic makes from every input rounded to
+    float32 (the conditioning of the step at this resolution)."""
+    import torch
+    from veris_gb300.engine import SeaIceStep
+    from veris_gb300.state import VerisState
+    from veris_gb300.synthetic import CONFIGS, make_state, config_settings
+    name = "c5_tenthdeg"
+    c = CONFIGS[name]
+    arrays = make_state(c["nx"], c["ny"], seed=args.seed)
+    sett = config_settings(name)
+    n_sub = int(sett.nEVPsteps)
+    cells = c["nx"] * c["ny"]
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    out = {"config": workload_config(name, c, sett, n_sub)}
+    e64, _ = make_engine(arrays, sett, dev, "f64", args)
+    ms64, _, _ = time_steps(e64, 2, 1, flush, 1, dev)
+    us64 = evp_launch_us(e64, n_sub, flush)
+    out["fp64"] = {"value": cells * n_sub * 2 / (ms64 / 1e3) / 1e9, "ms_per_step": ms64 / 2, "steps": 2,
+                   "roofline": roofline_fp64(evp_kernel_name(e64), name, cells, us64, sms)}
+    del e64
+    e32, tuning = make_engine(arrays, sett, dev, "f32", args)
+    ms32, _, _ = time_steps(e32, 5, 2, flush, 1, dev)
+    us32 = evp_launch_us(e32, n_sub, flush)
+    wv = e32.walk_variant
+    out["fp32"] = {"value": cells * n_sub * 5 / (ms32 / 1e3) / 1e9, "ms_per_step": ms32 / 5, "steps": 5,
+                   "roofline": roofline_hbm(evp_kernel_name(e32), name, cells, us32, "f32"),
+                   "walk": {"variant": wv, "tuning": tuning}}
+    out["fp32_over_fp64_speedup"] = out["fp32"]["value"] / out["fp64"]["value"]
+    del e32
+    torch.cuda.empty_cache()
+    # one step from the same state: float64, float32, float64 on float32-rounded inputs
+    names = ("uIce", "vIce", "hIceMean", "hSnowMean", "Area")
+    runs = {}
+    for key, arr, prec in (("f64", arrays, "f64"), ("f32", arrays, "f32"),
+                           ("f64_rounded_inputs", {k: a.astype(np.float32).astype(np.float64)
+                                                   for k, a in arrays.items()}, "f64")):
+        st = VerisState.from_numpy(arr, sett, device=dev)
+        eng = SeaIceStep(st, precision=prec, walk_variant=wv)
+        eng.step()
+        torch.cuda.synchronize(dev)
+        runs[key] = st.variables
+        del eng
+    ref = runs["f64"]
+    out["error_after_1_step"] = {
+        k: {n: rel_errors(getattr(runs[k], n), getattr(ref, n)) for n in names} for k in ("f32", "f64_rounded_inputs")}
+    out["branch_flips_after_1_step"] = {k: branch_flips(runs[k], ref, sett) for k in ("f32", "f64_rounded_inputs")}
+    out["note"] = ("f64_rounded_inputs: float64 arithmetic throughout, every input rounded to float32 first; "
+                   "its error is the part of the float32 error no float32 arithmetic can remove")
+    del runs, ref
+    torch.cuda.empty_cache()
+    return out
+
+
 def run_ours(args):
     import torch
     ws, rank, local = dist_init(args)
@@ -322,8 +680,6 @@ def run_ours(args):
     if rank == 0 or ws == 1:
         build()
     barrier(ws)
-    from veris_gb300.engine import SeaIceStep
-    from veris_gb300.state import VerisState
     from veris_gb300.synthetic import CONFIGS, make_state, config_settings
 
     c = CONFIGS[args.config]
@@ -335,152 +691,69 @@ def run_ours(args):
         sett.evpAlpha = sett.evpBeta = float(args.evp_alpha_beta)
     if args.adaptive:
         sett.useAdaptiveEVP = True
-    n_sub = sett.nEVPsteps
+    n_sub = int(sett.nEVPsteps)
     cells = c["nx"] * c["ny"]
-
-    state = VerisState.from_numpy(arrays, sett, device=dev)
-    eng = SeaIceStep(state, precision=args.precision, evp=args.evp, f32_kernel=args.f32_kernel,
-                     walk_rows=args.walk_rows, walk_variant=max(0, args.walk_variant))
-    walk_tuning = None
-    if args.precision == "f32" and args.f32_kernel == "walk" and eng.evp_form == "fast" and args.walk_variant < 0:
-        from veris_gb300.autotune import tune_walk
-        walk_tuning = tune_walk(eng)
-    eng.capture()
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
-    for _ in range(args.warmup):
-        eng.step()
-    torch.cuda.synchronize(dev)
 
-    clocks = ClockSampler(local)
-    clocks.start()
-    time.sleep(0.3)
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    barrier(ws)
-    torch.cuda.synchronize(dev)
-    t_wall0 = time.perf_counter()
-    for k in range(args.steps):
-        flush.zero_()
-        starts[k].record()
-        eng.step()
-        ends[k].record()
-    torch.cuda.synchronize(dev)
-    barrier(ws)
-    wall = time.perf_counter() - t_wall0
-    clk = clocks.stop()
-    ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
-    ms = max_over_ranks(ms, ws)
+    # the headline step, graph-replayed, inputs resident
+    eng, tuning = make_engine(arrays, sett, dev, args.precision, args, budgets=True)
+    ms, wall, clk = time_steps(eng, args.steps, args.warmup, flush, ws, dev, clocks=ClockSampler(local))
+    conservation = conservation_summary(eng, args.steps)
     value = replica_value(cells, n_sub, args.steps, ms, ws)
-    launches = eng.launches_per_step * args.steps
-
-    # EVP kernel alone (eager, events around the subcycle loop on the launching stream)
-    evp_ms = []
-    for _ in range(3):
-        flush.zero_()
-        evp_ms.append(eng.timed_step())
-    evp_ms = float(np.median(evp_ms))
-    flush.zero_()
+    us = evp_launch_us(eng, n_sub, flush)
     phases = eng.phase_times()
-    per_launch_s = evp_ms / 1e3 / n_sub
-    algo_bytes = BYTES_PER_CELL_SUBCYCLE[args.precision] * cells
-    achieved = algo_bytes / per_launch_s / 1e9
-    peak, peak_kind = hbm_peak()
-    kernel = (("evp_walk_kernel" if args.f32_kernel == "walk" else "evp_tma_kernel")
-              if eng.evp_form == "fast" and args.precision == "f32" else
-              ("evp_fast_kernel" if eng.evp_form == "fast" else "evp_subcycle_kernel")
-              + f"<{'float' if args.precision == 'f32' else 'double'}>")
-    traffic = recorded_traffic(kernel, args.config)
-    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "traffic": traffic, "kernel": kernel,
-                "algorithmic_bytes_per_launch": algo_bytes, "avg_launch_us": per_launch_s * 1e6,
-                "peak_source": f"{peak_kind} HBM copy bandwidth"}
-
+    kernel = evp_kernel_name(eng)
+    roof = (roofline_fp64(kernel, args.config, cells, us, sms) if args.precision == "f64"
+            else roofline_hbm(kernel, args.config, cells, us, "f32"))
     line = {"metric": METRIC, "value": value, "unit": "Gcell-subcycles/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": args.precision, "data": "synthetic",
-            "config": {"workload": args.config, "nx": c["nx"], "ny": c["ny"], "subcycles": n_sub,
-                       "evpAlpha": float(sett.evpAlpha), "evpBeta": float(sett.evpBeta),
-                       "adaptive_evp": bool(sett.useAdaptiveEVP),
-                       "dt_s": c["dt"], "cells": cells, "precision": args.precision,
-                       "parallelism": "replicas" if ws > 1 else "single-gpu",
-                       "l2": "flushed before every timed step (512 MiB write)",
-                       "graph": "one CUDA graph per step", "evp_form": eng.evp_form,
-                       "f32_kernel": args.f32_kernel if args.precision == "f32" else None,
-                       "walk": {"rows": eng.walk_rows or "auto", "variant": eng.walk_variant,
-                                "tuning": walk_tuning}
-                       if args.f32_kernel == "walk" else None},
-            "roofline": roofline, "gpu_launches": launches, "clocks": clk,
-            "wall_s_timed_region": wall, "evp_ms_per_step": evp_ms,
+            "dtype": args.precision, "data": "synthetic (seeded generators of the workload's fields)",
+            "config": workload_config(args.config, c, sett, n_sub),
+            "run": {"parallelism": "replicas" if ws > 1 else "single-gpu",
+                    "l2": "flushed before every timed step (512 MiB write)", "graph": "one CUDA graph per step",
+                    "evp_form": eng.evp_form, "evp_kernel": kernel,
+                    "walk": ({"rows": eng.walk_rows or "auto", "variant": eng.walk_variant, "tuning": tuning}
+                             if args.precision == "f32" and eng.f32_kernel == "walk" else None)},
+            "roofline": roof, "gpu_launches": eng.launches_per_step * args.steps, "clocks": clk,
+            "conservation": conservation,
+            "wall_s_timed_region": wall, "evp_ms_per_step": us * n_sub / 1e3,
             "phase_ms": {k: round(v, 4) for k, v in phases.items()}}
-
-    # end-to-end through host buffers
     if not args.no_e2e:
-        from veris_gb300.host import HostCoupledStep
-        host = HostCoupledStep(eng)
-        h_in, h_out = host.host_buffers()
-        for _ in range(max(3, args.warmup)):   # the first call captures the exchange graph
-            host.step(h_in, h_out)
-        barrier(ws)
-        t0 = time.perf_counter()
-        ke = max(3, args.steps // 2)
-        for _ in range(ke):
-            host.step(h_in, h_out)
-        e2e_s = time.perf_counter() - t0
-        e2e_s = max_over_ranks(e2e_s, ws)
-        line["e2e"] = {"value": ws * cells * n_sub * ke / e2e_s / 1e9, "unit": "Gcell-subcycles/s",
-                       "h2d_bytes_per_step": host.h2d_bytes, "d2h_bytes_per_step": host.d2h_bytes,
-                       "steps": ke, "api": "veris_gb300.host.HostCoupledStep.step (pinned host arrays)"}
+        line["e2e"] = e2e_of(eng, args, ws, cells, n_sub)
+    del eng
+    torch.cuda.empty_cache()
 
-    # float64 drop-in arithmetic on the same inputs, and the float32 error
-    if not args.no_fp64 and args.precision == "f32":
-        n_cmp = max(2, args.warmup + args.steps)
-        names = ("uIce", "vIce", "hIceMean", "hSnowMean", "Area", "TSurf", "Qnet")
-        # both precisions from the same initial state; capture() runs step 1
-        st32 = VerisState.from_numpy(arrays, sett, device=dev)
-        e32 = SeaIceStep(st32, precision="f32", evp=args.evp, f32_kernel=args.f32_kernel,
-                         walk_rows=args.walk_rows, walk_variant=eng.walk_variant)
-        e32.capture()
-        st64 = VerisState.from_numpy(arrays, sett, device=dev)
-        e64 = SeaIceStep(st64, precision="f64", evp=args.evp)
-        e64.capture()
-        torch.cuda.synchronize(dev)
-        errs1 = {n: rel_errors(getattr(st32.variables, n), getattr(st64.variables, n)) for n in names}
-        t64 = []
-        for k in range(n_cmp - 1):
-            a = torch.cuda.Event(enable_timing=True)
-            b = torch.cuda.Event(enable_timing=True)
-            flush.zero_()
-            a.record()
-            e64.step()
-            b.record()
-            b.synchronize()
-            t64.append(a.elapsed_time(b))
-            e32.step()
-        torch.cuda.synchronize(dev)
-        fp64_ms = float(np.median(t64[-min(len(t64), args.steps):]))
-        fp64_value = cells * n_sub / (fp64_ms / 1e3) / 1e9
-        line["fp64"] = {"value": fp64_value, "ms_per_step": fp64_ms, "steps_compared": n_cmp,
-                        "evp_form": e64.evp_form}
-        line["fp32_over_fp64_speedup"] = (value / ws) / fp64_value
-        errs = {n: rel_errors(getattr(st32.variables, n), getattr(st64.variables, n)) for n in names}
-        line["fp32_error_vs_fp64"] = {"after_1_step": errs1, "steps": n_cmp, "fields": errs,
-                                      "definition": "max_rel = max|a-b| / max|b|, rms_rel = rms(a-b) / max|b|"}
+    if args.precision == "f64" and not args.no_fp32:
+        line["fp32"] = fp32_block(arrays, sett, dev, args, flush, ws, args.config, cells, n_sub)
+        line["fp32"]["speedup_vs_fp64"] = line["fp32"]["value"] / value
+    elif args.precision == "f32" and not args.no_fp64:
+        e64, _ = make_engine(arrays, sett, dev, "f64", args)
+        ms64, _, _ = time_steps(e64, max(1, args.steps // 2), 1, flush, ws, dev)
+        line["fp64"] = {"value": replica_value(cells, n_sub, max(1, args.steps // 2), ms64, ws),
+                        "ms_per_step": ms64 / max(1, args.steps // 2)}
+        del e64
+    torch.cuda.empty_cache()
 
-    if not args.no_routines:
+    if ws == 1 and not args.no_routines:
         line["routines"] = measure_routines(arrays, sett, dev, flush)
+    if ws == 1 and not args.no_c5 and args.config != "c5_tenthdeg":
+        line["c5"] = c5_block(args, dev, flush)
 
     if rank == 0 and not args.no_cpu_baseline:
-        sec, desc = cpu_sample(arrays, sett, 2, n_sub)
-        line["cpu_baseline"] = {"value": cells * n_sub / sec / 1e9, "unit": "Gcell-subcycles/s",
-                                "cores": 1, "kind": "port", "sample": desc,
-                                "host_cpus": os.cpu_count()}
+        n_sample = min(CPU_SAMPLE_SUBCYCLES, n_sub)
+        sec, fixed, per_sub = cpu_step_estimate(arrays, sett, n_sample, n_sub)
+        line["cpu_baseline"] = {
+            "value": cells * n_sub / sec / 1e9, "unit": "Gcell-subcycles/s", "cores": 1, "kind": "port",
+            "sample": (f"NumPy oracle, 1 thread: {n_sample} EVP subcycles timed ({per_sub * n_sample:.1f} s) and "
+                       f"scaled x{n_sub / n_sample:g} to {n_sub}, plus preparation, ocean stress, advection, "
+                       f"clean-up and growth timed once ({fixed:.1f} s)"),
+            "host_cpus": os.cpu_count()}
     if rank == 0:
         print(json.dumps(line))
     barrier(ws)
     return 0
-
-
 def _event_time(fn, repeats, flush):
     """Median CUDA-event time of ``repeats`` calls of ``fn`` (ms per call),
     each call timed alone with L2 flushed (512 MiB write) before it."""

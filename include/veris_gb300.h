@@ -580,6 +580,22 @@ int veris_global_sum_f64(const VerisGrid *g, const double *A, const double *weig
                          double *result, void *workspace, size_t workspace_bytes,
                          veris_stream_t s);
 /*
+ * The conservation diagnostics the step's global_sum calls would feed
+ * (veris/global_sum.py:1-4, called at veris/evp_solver.py:219,227; the
+ * budget quantities of veris/growth.py:296-383): n (1..16) deterministic
+ * float64 interior sums sum(fields[q] * weights[q]) (weights NULL, or
+ * weights[q] NULL: unweighted), written to ring[slot * 16 + first + q] with
+ * slot = *step_counter mod ring_steps (device memory); advance != 0 then
+ * increments *step_counter.  Fixed-order trees: bitwise reproducible;
+ * capturable in a CUDA graph.  Workspace: veris_budget_workspace_bytes().
+ */
+size_t veris_budget_workspace_bytes(void);
+int veris_budget_sums_f64(const VerisGrid *g, const double *const *fields,
+                          const double *const *weights, int32_t n, int32_t first,
+                          double *ring, int32_t ring_steps, int32_t *step_counter,
+                          int32_t advance, void *workspace, size_t workspace_bytes,
+                          veris_stream_t s);
+/*
  * No counterpart in the reference (NumPy carries NaN through silently):
  * ORs `flag` into *status_device (device memory, sticky: the caller clears
  * it) when any element of the n (1..8) padded arrays, halos included, is a

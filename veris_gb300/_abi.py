@@ -200,6 +200,9 @@ SIGNATURES = {
     "veris_reduce_workspace_bytes": ([_G], _S),
     "veris_mbarrier_wait_probe": ([ctypes.c_int32, ctypes.c_uint32, _P, _P], _I),
     "veris_global_sum_f64": ([_G, _P, _P, _P, _P, _S, _P], _I),
+    "veris_budget_workspace_bytes": ([], _S),
+    "veris_budget_sums_f64": ([_G, _P, _P, ctypes.c_int32, ctypes.c_int32, _P, ctypes.c_int32, _P, ctypes.c_int32,
+                               _P, _S, _P], _I),
     "veris_check_finite_f64": ([_G, _P, ctypes.c_int32, ctypes.c_int32, _P, _P], _I),
     "veris_check_finite_f32": ([_G, _P, ctypes.c_int32, ctypes.c_int32, _P, _P], _I),
     "veris_convert_f64_to_f32": ([_P, _P, _L, _P], _I),

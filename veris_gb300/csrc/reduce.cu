@@ -53,6 +53,47 @@ __global__ void final_sum_kernel(const double *partial, double *result) {
     if (threadIdx.x == 0) *result = s;
 }
 
+// Conservation diagnostics: up to BUD_MAX weighted interior sums in one
+// pass.  Block (b, q) sums rows b, b + BUD_BLOCKS, ... of field q times its
+// weight (rows then columns: no index division); one block then adds each
+// field's partials in index order and writes the sums into the step's slot
+// of a ring, the slot being the device step counter modulo the ring length.
+// Fixed grid, fixed trees: bitwise reproducible.
+constexpr int BUD_MAX = 16;
+constexpr int BUD_BLOCKS = 256;
+
+struct BudgetArgs {
+    const double *f[BUD_MAX];
+    const double *w[BUD_MAX];
+};
+
+__global__ void budget_partial_kernel(BudgetArgs a, Dims d, int olx, int oly, double *partial) {
+    const int q = blockIdx.y;
+    const double *f = a.f[q], *w = a.w[q];
+    double acc = 0.0;
+    for (int i = blockIdx.x; i < d.nx; i += BUD_BLOCKS) {
+        const int64_t row = d.raw(i + olx, oly);
+        for (int j = threadIdx.x; j < d.ny; j += RED_THREADS)
+            acc += w ? f[row + j] * w[row + j] : f[row + j];
+    }
+    const double s = block_sum(acc);
+    if (threadIdx.x == 0) partial[q * BUD_BLOCKS + blockIdx.x] = s;
+}
+
+__global__ void budget_final_kernel(const double *partial, int n, int first, double *ring, int ring_steps,
+                                    int32_t *counter, int advance) {
+    __shared__ int slot;
+    if (threadIdx.x == 0) slot = ((*counter % ring_steps) + ring_steps) % ring_steps;
+    __syncthreads();
+    for (int q = 0; q < n; ++q) {
+        double acc = 0.0;
+        for (int k = threadIdx.x; k < BUD_BLOCKS; k += RED_THREADS) acc += partial[q * BUD_BLOCKS + k];
+        const double s = block_sum(acc);
+        if (threadIdx.x == 0) ring[(int64_t)slot * BUD_MAX + first + q] = s;
+    }
+    if (advance && threadIdx.x == 0) *counter += 1;
+}
+
 // Non-finite detection over whole padded arrays (halos included): each
 // thread folds its elements into one flag, one warp vote, one atomicOr per
 // warp that saw a NaN or an infinity.  Sticky: the caller clears the word.
@@ -112,6 +153,30 @@ int veris_check_finite_f64(const VerisGrid *g, const double *const *arrays, int3
 int veris_check_finite_f32(const VerisGrid *g, const float *const *arrays, int32_t n, int32_t flag,
                            int32_t *status_device, veris_stream_t s) {
     return check_finite<float>(g, arrays, n, flag, status_device, s);
+}
+
+size_t veris_budget_workspace_bytes(void) { return (size_t)BUD_MAX * BUD_BLOCKS * sizeof(double); }
+
+int veris_budget_sums_f64(const VerisGrid *g, const double *const *fields, const double *const *weights,
+                          int32_t n, int32_t first, double *ring, int32_t ring_steps, int32_t *step_counter,
+                          int32_t advance, void *ws, size_t ws_bytes, veris_stream_t s) {
+    Dims d;
+    VERIS_CHECK_GRID(g, d);
+    VERIS_REQUIRE(fields && ring && step_counter && ring_steps >= 1, VERIS_ERR_ARG);
+    VERIS_REQUIRE(n >= 1 && first >= 0 && first + n <= BUD_MAX, VERIS_ERR_ARG);
+    VERIS_REQUIRE(ws && ws_bytes >= veris_budget_workspace_bytes(), VERIS_ERR_WORKSPACE);
+    BudgetArgs a{};
+    for (int q = 0; q < n; ++q) {
+        VERIS_REQUIRE(fields[q], VERIS_ERR_ARG);
+        a.f[q] = fields[q];
+        a.w[q] = weights ? weights[q] : nullptr;
+    }
+    cudaStream_t st = (cudaStream_t)s;
+    double *partial = static_cast<double *>(ws);
+    budget_partial_kernel<<<dim3(BUD_BLOCKS, n), RED_THREADS, 0, st>>>(a, d, g->olx, g->oly, partial);
+    budget_final_kernel<<<1, RED_THREADS, 0, st>>>(partial, n, first, ring, ring_steps, step_counter,
+                                                   advance ? 1 : 0);
+    return launch_status();
 }
 
 int veris_global_sum_f64(const VerisGrid *g, const double *A, const double *w, double *result, void *ws,

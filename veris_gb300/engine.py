@@ -51,11 +51,24 @@ FILLED_AFTER_GROWTH = ("hIceMean", "hSnowMean", "Area", "forc_salt_surface_ice",
 # walk needs them along j only)
 V_AREA2D = 128
 HELD_FORCING = ("Qnet", "Qsw")
+# float64 conservation diagnostics recorded every step (budgets=True): area-
+# weighted interior sums (veris/global_sum.py:1-4 is the hook the reference
+# leaves for them; the budget quantities are those of veris/growth.py:296-383)
+BUDGET_SLOTS = (
+    "ice_volume_start", "snow_volume_start", "ice_area_start",            # sum rA*(h, hs, A) entering the step
+    "ice_volume_advected", "snow_volume_advected", "ice_area_advected",   # after advection
+    "ice_volume_cleaned", "snow_volume_cleaned",                          # after clean-up and ridging
+    "ice_overshoot", "snow_overshoot",                                    # sum rA*(os_hIceMean, os_hSnowMean)
+    "ice_volume_end", "snow_volume_end", "ice_area_end",                  # leaving the step
+    "ocean_heat_loss", "fresh_water_flux", "salt_flux",                   # sum rA*(Qnet, EmPmR, forc_salt_surface_ice)
+)
+BUDGET_UNITS = ("m3", "m3", "m2", "m3", "m3", "m2", "m3", "m3", "m3", "m3", "m3", "m3", "m2", "W", "kg/s", "kg/s")
+BUDGET_RING = 4096
 
 
 class SeaIceStep:
     def __init__(self, state: VerisState, precision="f64", n_subcycles=None, evp="auto", hold_forcing=False,
-                 f32_kernel="walk", walk_rows=0, walk_variant=0, check_finite=True):
+                 f32_kernel="walk", walk_rows=0, walk_variant=0, check_finite=True, budgets=False):
         if precision not in ("f64", "f32"):
             raise ValueError("precision must be 'f64' or 'f32'")
         if evp not in ("auto", "fast", "plain"):
@@ -131,6 +144,15 @@ class SeaIceStep:
         # fast forms: a buffer of veris_evp_tape_bytes() that the next eager
         # step's EVP fills with its subcycle states
         self.evp_tape = None
+        # conservation diagnostics: BUDGET_SLOTS of every step into a ring
+        # of BUDGET_RING steps on the device (four sums calls per step)
+        self.budgets = bool(budgets)
+        if self.budgets:
+            self.budget_ring = torch.zeros((BUDGET_RING, len(BUDGET_SLOTS)), dtype=torch.float64,
+                                           device=self.device)
+            self.budget_count = torch.zeros(1, dtype=torch.int32, device=self.device)
+            self.budget_ws = torch.empty(self.lib.veris_budget_workspace_bytes(), dtype=torch.uint8,
+                                         device=self.device)
 
     def set_settings(self, **kw):
         """Change scalar settings (e.g. pStar, airIceDrag) between steps;
@@ -160,6 +182,32 @@ class SeaIceStep:
     def _refs(self, fields):
         return ctypes.byref(self.grid), ctypes.byref(self.params), ctypes.byref(fields)
 
+    def _budget(self, first, names, weighted, advance=False):
+        """Enqueue the float64 interior sums of ``names`` (times rA where
+        ``weighted``) into slots first.. of this step's ring row."""
+        v = self.state.variables
+        n = len(names)
+        fields = (ctypes.c_void_p * n)(*[getattr(v, k).data_ptr() for k in names])
+        rA = v.rA.data_ptr()
+        weights = (ctypes.c_void_p * n)(*[rA if w else None for w in weighted])
+        check("budget_sums", self.lib.veris_budget_sums_f64(
+            ctypes.byref(self.grid), fields, weights, n, first, self.budget_ring.data_ptr(), BUDGET_RING,
+            self.budget_count.data_ptr(), 1 if advance else 0, self.budget_ws.data_ptr(), self.budget_ws.numel(),
+            self.stream))
+        return 2
+
+    def budget_records(self):
+        """{slot name: float64 numpy array over the recorded steps, oldest
+        first} (synchronises; at most the last BUDGET_RING steps)."""
+        if not self.budgets:
+            raise RuntimeError("SeaIceStep was built without budgets")
+        import numpy as np
+        n = int(self.budget_count.item())
+        ring = self.budget_ring.cpu().numpy()
+        k = min(n, BUDGET_RING)
+        rows = np.array([ring[(n - k + t) % BUDGET_RING] for t in range(k)]).reshape(k, len(BUDGET_SLOTS))
+        return {name: rows[:, q] for q, name in enumerate(BUDGET_SLOTS)}
+
     def _to32(self, src, dst):
         check("convert", self.lib.veris_convert_f64_to_f32(src.data_ptr(), dst.data_ptr(), src.numel(),
                                                            self.stream))
@@ -183,6 +231,8 @@ class SeaIceStep:
         if self.forcing is not None:
             for name, t in self.forcing.items():
                 getattr(v, name).copy_(t)
+        if self.budgets:
+            n += self._budget(0, ("hIceMean", "hSnowMean", "Area"), (True,) * 3)
         check("SeaIceMass", lib.veris_sea_ice_mass_f64(*r64, v.SeaIceMassC.data_ptr(), v.SeaIceMassU.data_ptr(),
                                                        v.SeaIceMassV.data_ptr(), st))
         check("AreaWS", lib.veris_area_ws_f64(*r64, v.AreaW.data_ptr(), v.AreaS.data_ptr(), st))
@@ -275,12 +325,16 @@ class SeaIceStep:
             for name, t in zip(("hIceMean", "hSnowMean", "Area"), self.adv_out32):
                 self._to64(t, getattr(v, name))
             n += 3
+        if self.budgets:
+            n += self._budget(3, ("hIceMean", "hSnowMean", "Area"), (True,) * 3)
         mark("advection")
         # pointwise routines run in place on the state
         check("clean_up_advection", lib.veris_clean_up_advection_f64(
             *r64, v.hIceMean.data_ptr(), v.hSnowMean.data_ptr(), v.Area.data_ptr(), v.TSurf.data_ptr(),
             v.os_hIceMean.data_ptr(), v.os_hSnowMean.data_ptr(), st))
         check("ridging", lib.veris_ridging_f64(*r64, v.Area.data_ptr(), st))
+        if self.budgets:
+            n += self._budget(6, ("hIceMean", "hSnowMean", "os_hIceMean", "os_hSnowMean"), (True,) * 4)
         mark("clean_up")
         outs = [getattr(v, k).data_ptr() for k in GROWTH_OUT]
         if growth_chunks <= 1:
@@ -297,6 +351,9 @@ class SeaIceStep:
             check("fill_overlap", lib.veris_fill_overlap_f64(ctypes.byref(self.grid), ctypes.byref(self.params),
                                                              getattr(v, name).data_ptr(), st))
         n += len(FILLED_AFTER_GROWTH)
+        if self.budgets:
+            n += self._budget(10, ("hIceMean", "hSnowMean", "Area", "Qnet", "EmPmR", "forc_salt_surface_ice"),
+                              (True,) * 6, advance=True)
         mark("fill")
         if self.check_finite:
             ptrs = (ctypes.c_void_p * len(FINITE_CHECKED))(*[getattr(v, k).data_ptr() for k in FINITE_CHECKED])
