@@ -84,6 +84,8 @@ def parse():
                     help="float32 EVP kernel: register-walking warps or TMA-staged tiles")
     ap.add_argument("--walk-rows", type=int, default=0, help="rows per walk (0: from the grid and the SM count)")
     ap.add_argument("--walk-variant", type=int, default=-1, help="-1: tuned on the workload")
+    ap.add_argument("--f64-tile-rows", type=int, default=0, choices=(0, 16, 24, 32),
+                    help="rows per tile of the float64 subcycle kernel (0: the library's default)")
     ap.add_argument("--adjoint", action="store_true",
                     help="time a trajectory's forward + adjoint against its forward (float64)")
     ap.add_argument("--adjoint-config", default="c3_1deg")
@@ -680,6 +682,8 @@ def run_ours(args):
     if rank == 0 or ws == 1:
         build()
     barrier(ws)
+    from veris_gb300 import _abi
+    _abi.check("evp_f64_tile_rows", _abi.load().veris_evp_f64_tile_rows(args.f64_tile_rows))
     from veris_gb300.synthetic import CONFIGS, make_state, config_settings
 
     c = CONFIGS[args.config]

@@ -286,6 +286,15 @@ int veris_evp_fast_solver_f64(const VerisGrid *g, const VerisParams *p, const Ve
                               int32_t n_subcycles, double *uIce, double *vIce, double *sigma1,
                               double *sigma2, double *sigma12, void *workspace,
                               size_t workspace_bytes, veris_stream_t s);
+/*
+ * Tile height of the float64 fast-form subcycle kernel (every float64 fast
+ * form: solver, tapes, the adjoint's recomputed subcycles): 16, 24 or 32
+ * output rows by 32 columns per CTA (4, 3 or 2 CTAs per SM), 0 = the
+ * library's default.  Process-wide, for every later launch; same values
+ * for every height.  VERIS_ERR_ARG for other heights.  A tuning knob with no
+ * counterpart in the reference.
+ */
+int veris_evp_f64_tile_rows(int32_t rows);
 /* the float32 fast form without TMA staging (the shared-memory kernel only) */
 /*
  * The same float32 loop with the register-walking kernel: one warp per

@@ -27,8 +27,9 @@
 // * warps whose cells all have zero ice strength skip the viscosity's
 //   square root and division (zeta = 0, which the formula gives), warps on
 //   land skip the velocity division;
-// * 32x32 output tiles (ring work ~7% of the tile's, against ~14% for
-//   16x32 tiles), two 256-thread CTAs per SM.
+// * 24x32 output tiles by default, three 256-thread CTAs per SM (16- and
+//   32-row tiles: four and two; the larger the tile, the less ring work but
+//   the fewer resident warps to cover the float64 pipe's latency).
 #include "evp_fast.cuh"
 
 namespace veris {
@@ -88,7 +89,15 @@ __device__ __forceinline__ bool seed_range(double b) {
     return hi >= (64 << 20) && hi < (1984 << 20);
 }
 
-__device__ __forceinline__ bool is_zero(double x) { return (__double_as_longlong(x) << 1) == 0; }
+// the bits of x through a move the compiler cannot fold back into a float
+// comparison (which would run on the float64 pipe)
+__device__ __forceinline__ unsigned long long bits_of(double x) {
+    unsigned long long b;
+    asm("mov.b64 %0, %1;" : "=l"(b) : "d"(x));
+    return b;
+}
+
+__device__ __forceinline__ bool is_zero(double x) { return (bits_of(x) << 1) == 0; }
 
 // a / b for b in seed_range: r0 ~ 1/b, e = 1 - b*r0, 1/b = r0*(1 + e + e^2 + O(e^3))
 __device__ __forceinline__ double div_series(double a, double b) {
@@ -126,15 +135,18 @@ __device__ __forceinline__ double sqrt64(double x, unsigned m) {
 
 // x > y for x, y >= 0 (or -0); false when x is NaN, as the float comparison
 __device__ __forceinline__ bool gt_nonneg(double x, double y) {
-    const long long a = __double_as_longlong(x), b = __double_as_longlong(y);
+    const long long a = (long long)bits_of(x), b = (long long)bits_of(y);
     return a > b && a <= 0x7ff0000000000000LL;
 }
 
 // ------------------------------------------------------------------ tile
 constexpr int F64_THREADS = 256;
 
+// TI output rows x 32 columns per CTA; 16-, 24- and 32-row tiles fit 4, 3
+// and 2 CTAs per SM (smaller tiles: more resident warps, more ring work)
+template <int TI_>
 struct Smem64 {
-    static constexpr int TI = 32, TJ = 32;
+    static constexpr int TI = TI_, TJ = 32;
     static constexpr int WS = TJ + 4, HS = TI + 4, NS = WS * HS;   // u, v, flags: origin -2
     static constexpr int WZ = TJ + 3, HZ = TI + 3, NZ = WZ * HZ;   // e12 and rAz*e12^2: origin -1
     static constexpr int WB = TJ + 2, HB = TI + 2, NB = WB * HB;   // zeta: origin -1
@@ -143,12 +155,15 @@ struct Smem64 {
         return sizeof(double) * (size_t)(2 * NS + 2 * NZ + NB + (basal ? 6 : 5) * NC) + sizeof(uint32_t) * NS;
     }
 };
-static_assert(2 * (Smem64::bytes(true) + 1024) <= 228 * 1024, "two CTAs per SM");
+constexpr int f64_min_blocks(int ti) { return ti <= 16 ? 4 : (ti <= 24 ? 3 : 2); }
+static_assert(2 * (Smem64<32>::bytes(true) + 1024) <= 228 * 1024, "two 32-row CTAs per SM");
+static_assert(3 * (Smem64<24>::bytes(false) + 1024) <= 228 * 1024, "three 24-row CTAs per SM");
+static_assert(4 * (Smem64<16>::bytes(true) + 1024) <= 228 * 1024, "four 16-row CTAs per SM");
 
-template <bool BASAL, bool TURN>
-__global__ void __launch_bounds__(F64_THREADS, 2)
+template <int TI, bool BASAL, bool TURN>
+__global__ void __launch_bounds__(F64_THREADS, f64_min_blocks(TI))
 evp_f64_kernel(Dims d, int64_t lp, HaloFill h, FastConsts<double> c, F64Scalars k, FastIO<double> io) {
-    using S = Smem64;
+    using S = Smem64<TI>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     double *sU = reinterpret_cast<double *>(smem_raw);
     double *sV = sU + S::NS;
@@ -377,25 +392,52 @@ evp_f64_kernel(Dims d, int64_t lp, HaloFill h, FastConsts<double> c, F64Scalars 
 #undef IZZ
 }
 
-template <bool B, bool R>
+template <int TI, bool B, bool R>
 static int launch64(const Dims &d, int64_t lp, const HaloFill &h, const FastConsts<double> &c, const F64Scalars &k,
                     const FastIO<double> &io, cudaStream_t st) {
-    auto kern = evp_f64_kernel<B, R>;
-    const size_t sm = Smem64::bytes(B);
+    using S = Smem64<TI>;
+    auto kern = evp_f64_kernel<TI, B, R>;
+    const size_t sm = S::bytes(B);
     static std::atomic<bool> configured[MAX_DEVICES];
     if (!smem_configured(configured, kern, (int)sm)) return VERIS_ERR_LAUNCH;
-    dim3 grid((d.NY + Smem64::TJ - 1) / Smem64::TJ, (d.NX + Smem64::TI - 1) / Smem64::TI);
+    dim3 grid((d.NY + S::TJ - 1) / S::TJ, (d.NX + S::TI - 1) / S::TI);
     kern<<<grid, F64_THREADS, sm, st>>>(d, lp, h, c, k, io);
     return launch_status();
 }
+
+template <int TI>
+static int launch64_rows(const Dims &d, int64_t lp, const HaloFill &h, const FastConsts<double> &c,
+                         const F64Scalars &k, const FastIO<double> &io, bool basal, bool turn, cudaStream_t st) {
+    if (basal)
+        return turn ? launch64<TI, true, true>(d, lp, h, c, k, io, st) : launch64<TI, true, false>(d, lp, h, c, k, io, st);
+    return turn ? launch64<TI, false, true>(d, lp, h, c, k, io, st) : launch64<TI, false, false>(d, lp, h, c, k, io, st);
+}
+
+// rows per tile of later float64 subcycles (0: the default); process-wide
+static std::atomic<int> g_tile_rows{0};
+// measured on GB300 (500-subcycle workloads): 24 rows 209.7 / 1159.7 us per
+// subcycle on 1440x720 / 3600x1800, against 210.0 / 1180.5 (16) and
+// 229.0 / 1229.2 (32)
+constexpr int F64_DEFAULT_ROWS = 24;
 
 int fast64_subcycle(const Dims &d, const HaloFill &h, const FastConsts<double> &c, const FastScalars<double> &ks,
                     const FastIO<double> &io, bool basal, bool turn, cudaStream_t st) {
     const int64_t lp = internal_pitch(d.NY);
     const F64Scalars k = f64_scalars(ks);
-    if (basal)
-        return turn ? launch64<true, true>(d, lp, h, c, k, io, st) : launch64<true, false>(d, lp, h, c, k, io, st);
-    return turn ? launch64<false, true>(d, lp, h, c, k, io, st) : launch64<false, false>(d, lp, h, c, k, io, st);
+    const int rows = g_tile_rows.load(std::memory_order_relaxed);
+    switch (rows ? rows : F64_DEFAULT_ROWS) {
+        case 16: return launch64_rows<16>(d, lp, h, c, k, io, basal, turn, st);
+        case 24: return launch64_rows<24>(d, lp, h, c, k, io, basal, turn, st);
+        default: return launch64_rows<32>(d, lp, h, c, k, io, basal, turn, st);
+    }
 }
 
 }  // namespace veris
+
+using namespace veris;
+
+extern "C" int veris_evp_f64_tile_rows(int32_t rows) {
+    VERIS_REQUIRE(rows == 0 || rows == 16 || rows == 24 || rows == 32, VERIS_ERR_ARG);
+    g_tile_rows.store(rows, std::memory_order_relaxed);
+    return VERIS_OK;
+}
