@@ -338,9 +338,12 @@ int veris_mbarrier_wait_probe(int32_t arrive, uint32_t limit, int32_t *status_de
  * every GPU that loads the library until the process exits).  Larger grids
  * return VERIS_ERR_TOO_LARGE without launching anything.  The first call on a
  * device looks up the scratch's device address (cudaGetSymbolAddress) with
- * that device current: make that first call before any stream capture.
- * Calls share the scratch: calls that overlap on the GPU (different streams,
- * or host threads) race on it and must be serialised by the caller.
+ * that device current and keeps it for the life of the process: make that
+ * first call before any stream capture, and make no call after the device's
+ * primary context has been destroyed (cudaDeviceReset) -- the kept address
+ * would point at the old context's memory.  Calls share the scratch: calls
+ * that overlap on the GPU (different streams, or host threads) race on it
+ * and must be serialised by the caller.
  */
 #define VERIS_NOALLOC_MAX_CELLS 262144
 int veris_evp_solver_f64_noalloc(const VerisGrid *g, const VerisParams *p,

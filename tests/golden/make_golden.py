@@ -7,7 +7,9 @@ points the plugin imports (single-process NumPy semantics); the plugin's own
 
 Usage (in a container that holds the reference checkout):
 
-    python tests/golden/make_golden.py [--reference PATH]
+    python tests/golden/make_golden.py --reference PATH [--forcing | --plugin]
+
+(PATH: the reference checkout; or set VERIS_REFERENCE.)
 
 It writes one ``<case>.npz`` per case next to this script:
 
@@ -20,6 +22,10 @@ It writes one ``<case>.npz`` per case next to this script:
   back into the state;
 * ``forcing.npz`` (``--forcing``): free drift and the bulk formula, see
   ``run_forcing``;
+* ``setup_callsite.json`` and ``plugin.npz`` (``--plugin``): the call
+  sequence of the reference setup's sea-ice step as its source writes it
+  (``record_callsite``), and the plugin's ``set_inits`` on a host-model grid
+  (``run_set_inits``);
 * ``sub.<routine>.<output>``: single calls of the inner routines
   (strain rates, viscosities, drag coefficients, stress divergence, fluxes,
   limiter, solve4temp, one EVP subcycle) on the state after the dynamics
@@ -87,7 +93,10 @@ def _import_reference(ref):
     import veris.fill_overlap as fo
     import veris.freedrift_solver as fd
     import veris.heat_flux_MITgcm as heat_flux
-    return SimpleNamespace(fd=fd, heat_flux=heat_flux, area_mass=area_mass, dynsolver=dynsolver, dyn=dyn,
+    import importlib
+    set_inits = importlib.import_module("veris.set_inits")   # the package binds the name to the function
+    return SimpleNamespace(fd=fd, heat_flux=heat_flux, set_inits=set_inits, area_mass=area_mass,
+                           dynsolver=dynsolver, dyn=dyn,
                            averaging=averaging, evp=evp, ocean_stress=ocean_stress,
                            advection=advection, clean_up=clean_up, growth=growth,
                            s4t=s4t, fo=fo)
@@ -265,14 +274,116 @@ def run_forcing(R):
     return out
 
 
+SETUP = os.path.join("veris", "setup", "seaice_global_4deg", "seaice_global_4deg.py")
+
+
+def _table_names(path):
+    """The keyword names of the dict(...) table in a plugin module."""
+    import ast
+    for node in ast.walk(ast.parse(open(path).read())):
+        if isinstance(node, ast.Call) and isinstance(node.func, ast.Name) and node.func.id == "dict":
+            return [k.arg for k in node.keywords]
+    return []
+
+
+def record_callsite(ref):
+    """The sea-ice step of the reference setup as a call sequence: every
+    assignment in the setup's forcing kernel, from the SeaIceMass call to the
+    last halo fill, whose value is a call of a routine the setup imports
+    from the plugin; per call the routine, its module, its arguments
+    (``state`` or a state variable) and the variables it assigns.  Derived
+    from the setup's syntax tree; no code is executed."""
+    import ast
+    path = os.path.join(ref, SETUP)
+    tree = ast.parse(open(path).read())
+    imports = {}
+    for node in tree.body:
+        if isinstance(node, ast.ImportFrom) and node.module and node.module.startswith("veris."):
+            for a in node.names:
+                imports[a.asname or a.name] = node.module
+
+    def veris_call(stmt):
+        return (isinstance(stmt, ast.Assign) and isinstance(stmt.value, ast.Call)
+                and isinstance(stmt.value.func, ast.Name) and stmt.value.func.id in imports)
+
+    def name_of(expr):
+        if isinstance(expr, ast.Name):
+            return expr.id
+        if isinstance(expr, ast.Attribute) and isinstance(expr.value, ast.Name) and expr.value.id == "vs":
+            return "vs." + expr.attr
+        raise ValueError(f"unexpected argument {ast.dump(expr)}")
+
+    for fn in ast.walk(tree):
+        if not isinstance(fn, ast.FunctionDef):
+            continue
+        stmts = [st for st in fn.body if veris_call(st)]
+        first = [k for k, st in enumerate(stmts) if st.value.func.id == "SeaIceMass"]
+        if not first:
+            continue
+        calls = []
+        for st in stmts[first[0]:]:
+            tgt = st.targets[0]
+            elts = tgt.elts if isinstance(tgt, ast.Tuple) else [tgt]
+            calls.append({"line": st.lineno, "func": st.value.func.id, "module": imports[st.value.func.id],
+                          "args": [name_of(a) for a in st.value.args],
+                          "targets": [name_of(e)[3:] for e in elts]})
+        return {"source": SETUP.replace(os.sep, "/"), "function": fn.name,
+                "lines": [calls[0]["line"], calls[-1]["line"]], "calls": calls,
+                "plugin_settings": sorted(_table_names(os.path.join(ref, "veris", "settings.py"))),
+                "plugin_variables": sorted(_table_names(os.path.join(ref, "veris", "variables.py")))}
+    raise RuntimeError("no function of the setup calls SeaIceMass")
+
+
+def run_set_inits(R):
+    """``plugin.npz``: the reference's set_inits (veris/set_inits.py:6-59)
+    on a seeded host-model grid (3-level masks, 1-D grid spacings, 2-D
+    areas, depth and Coriolis)."""
+    rng = np.random.default_rng(11)
+    NX, NY, NZ = 30, 18, 3
+    ins = {
+        "maskT": (rng.random((NX, NY, NZ)) > 0.3).astype(np.float64),
+        "maskU": (rng.random((NX, NY, NZ)) > 0.35).astype(np.float64),
+        "maskV": (rng.random((NX, NY, NZ)) > 0.35).astype(np.float64),
+        "ht": 4000.0 * rng.random((NX, NY)),
+        "coriolis_t": 1.4e-4 * (rng.random((NX, NY)) - 0.5),
+        "dxt": 1e5 * (1.0 + rng.random(NX)), "dyt": 1e5 * (1.0 + rng.random(NY)),
+        "dxu": 1e5 * (1.0 + rng.random(NX)), "dyu": 1e5 * (1.0 + rng.random(NY)),
+        "area_t": 1e10 * (1.0 + rng.random((NX, NY))), "area_u": 1e10 * (1.0 + rng.random((NX, NY))),
+        "area_v": 1e10 * (1.0 + rng.random((NX, NY))),
+    }
+    state = SimpleNamespace(variables=SimpleNamespace(**{k: v.copy() for k, v in ins.items()}),
+                            settings=SimpleNamespace())
+    R.set_inits.set_inits(state)
+    out = {f"in.{k}": v for k, v in ins.items()}
+    for k, v in vars(state.variables).items():
+        if k not in ins:
+            out[f"out.{k}"] = np.array(v, dtype=np.float64)
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default=os.environ.get("VERIS_REFERENCE", "/root/reference"))
+    ap.add_argument("--reference", default=os.environ.get("VERIS_REFERENCE"),
+                    help="the reference checkout (default: $VERIS_REFERENCE)")
     ap.add_argument("--cases", nargs="*", default=list(CASES))
     ap.add_argument("--forcing", action="store_true", help="write forcing.npz only")
+    ap.add_argument("--plugin", action="store_true", help="write setup_callsite.json and plugin.npz only")
     args = ap.parse_args()
+    if not args.reference:
+        ap.error("give --reference PATH or set VERIS_REFERENCE")
     np.seterr(all="ignore")    # the reference's where() evaluates both branches
     R = _import_reference(args.reference)
+    if args.plugin:
+        site = record_callsite(args.reference)
+        path = os.path.join(HERE, "setup_callsite.json")
+        with open(path, "w") as f:
+            json.dump(site, f, indent=1)
+        print(f"{path}: {len(site['calls'])} calls, lines {site['lines']}")
+        out = run_set_inits(R)
+        path = os.path.join(HERE, "plugin.npz")
+        np.savez_compressed(path, **out)
+        print(f"{path}: {len(out)} arrays")
+        return
     if args.forcing:
         out = run_forcing(R)
         path = os.path.join(HERE, "forcing.npz")

@@ -1,7 +1,14 @@
 """The path at the workloads' full sizes.
 
+* 360 x 180 (the one-degree workload, 300 subcycles, dt 3600 s): one whole
+  float64 step of the drop-ins and of the step engine against the oracle,
+  bar 1e-10.
 * 1440 x 720 (the quarter-degree workload): one whole step against the
   oracle (two subcycles keep the NumPy side to seconds), bar 1e-10.
+* 3600 x 1800 (the tenth-degree workload): one whole float64 step with two
+  subcycles (advection and growth in full) against the oracle, bar 1e-10.
+* Members of the ensemble workload (sizes and wind scales drawn by its
+  generator, 100 subcycles): one float64 step each against the oracle.
 * 3600 x 1800 (the tenth-degree workload), properties that do not depend on
   an oracle: the float64 fast EVP form equals the plain float64 kernel to
   1e-10, the float32 walk equals the shared-memory float32 form to 1e-5, a
@@ -53,6 +60,54 @@ def test_quarter_degree_step_against_the_oracle():
               "Qnet", "EmPmR", "forc_salt_surface_ice"):
         e = G.rel_err(getattr(st.variables, k).cpu().numpy(), getattr(ref.variables, k))
         assert e <= 1e-10, (k, e)
+
+
+STEP_FIELDS = ("uIce", "vIce", "sigma1", "sigma2", "sigma12", "hIceMean", "hSnowMean", "Area", "TSurf",
+               "Qnet", "EmPmR", "forc_salt_surface_ice", "OceanStressU", "OceanStressV")
+
+
+def _step_against_oracle(arrays, sett, engine=False, tol=1e-10):
+    """One float64 step of the drop-ins (and of the float64 step engine, fast
+    EVP form) from ``arrays``, against the oracle's step."""
+    from types import SimpleNamespace
+    from oracle import veris_oracle as O
+    from veris_gb300 import model
+    from veris_gb300.engine import SeaIceStep
+    from veris_gb300.state import VerisState
+    ref = SimpleNamespace(variables=SimpleNamespace(**{k: v.copy() for k, v in arrays.items()}), settings=sett)
+    O.step(ref)
+    runs = {"drop-ins": VerisState.from_numpy(arrays, sett)}
+    model.step(runs["drop-ins"])
+    if engine:
+        runs["engine"] = VerisState.from_numpy(arrays, sett)
+        eng = SeaIceStep(runs["engine"], precision="f64")
+        assert eng.evp_form == "fast"
+        eng.step()
+    torch.cuda.synchronize()
+    for name, st in runs.items():
+        for k in STEP_FIELDS:
+            e = G.rel_err(getattr(st.variables, k).cpu().numpy(), getattr(ref.variables, k))
+            assert e <= tol, (name, k, e)
+
+
+def test_one_degree_step_against_the_oracle():
+    from veris_gb300.synthetic import config_settings, config_state
+    arrays = config_state("c3_1deg", seed=2, init_velocity=0.05, init_stress=500.0)
+    _step_against_oracle(arrays, config_settings("c3_1deg"), engine=True)
+
+
+def test_tenth_degree_step_against_the_oracle(tenth):
+    from veris_gb300.synthetic import config_settings
+    arrays, _sett = tenth
+    _step_against_oracle(arrays, config_settings("c5_tenthdeg", nEVPsteps=2), engine=True)
+
+
+@pytest.mark.parametrize("member", (0, 1, 2, 3))
+def test_ensemble_members_against_the_oracle(member):
+    from veris_gb300.synthetic import config_settings, ensemble_members, make_state
+    sp = ensemble_members(512, seed=0)[member]
+    arrays = make_state(sp["nx"], sp["ny"], seed=sp["seed"], wind_scale=sp["wind_scale"])
+    _step_against_oracle(arrays, config_settings("c4_ensemble"))
 
 
 @pytest.fixture(scope="module")

@@ -2,9 +2,11 @@
 import torch
 
 from ._abi import check
+from .hostarrays import accepts_host_state
 from .state import Call
 
 
+@accepts_host_state
 def Advection(state):
     """veris/advection.py:15-25 -> (hIceMean, hSnowMean, Area)."""
     c = Call(state)
@@ -15,6 +17,7 @@ def Advection(state):
     return h, hs, A
 
 
+@accepts_host_state
 def calc_Advection(state, field):
     """veris/advection.py:28-91 (extensive fields) -> the advected field."""
     c = Call(state)
@@ -25,6 +28,7 @@ def calc_Advection(state, field):
     return out
 
 
+@accepts_host_state
 def calc_ZonalFlux(state, field, uTrans):
     """veris/advection.py:94-129 -> the zonal flux, halo-filled."""
     c = Call(state)
@@ -34,6 +38,7 @@ def calc_ZonalFlux(state, field, uTrans):
     return F
 
 
+@accepts_host_state
 def calc_MeridionalFlux(state, field, vTrans):
     """veris/advection.py:132-167 -> the meridional flux, halo-filled."""
     c = Call(state)
@@ -44,8 +49,12 @@ def calc_MeridionalFlux(state, field, vTrans):
 
 
 def limiter(Cr):
-    """veris/advection.py:170-175: the superbee limiter, elementwise."""
+    """veris/advection.py:170-175: the superbee limiter, elementwise (a
+    NumPy array in, a NumPy array out)."""
     from ._abi import load
+    from .hostarrays import is_host_array, to_device, to_host
+    if is_host_array(Cr):
+        return to_host(limiter(to_device(Cr)))
     if not (isinstance(Cr, torch.Tensor) and Cr.is_cuda and Cr.dtype == torch.float64):
         raise TypeError("Cr must be a float64 CUDA tensor")
     Cr = Cr.contiguous()

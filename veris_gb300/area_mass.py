@@ -1,8 +1,10 @@
 """Drop-ins for veris/area_mass.py: ice mass and concentration at U/V points."""
 from ._abi import check
+from .hostarrays import accepts_host_state
 from .state import Call
 
 
+@accepts_host_state
 def AreaWS(state):
     """veris/area_mass.py:5-14 -> (AreaW, AreaS)."""
     c = Call(state)
@@ -11,6 +13,7 @@ def AreaWS(state):
     return AW, AS
 
 
+@accepts_host_state
 def SeaIceMass(state):
     """veris/area_mass.py:17-28 -> (SeaIceMassC, SeaIceMassU, SeaIceMassV)."""
     c = Call(state)

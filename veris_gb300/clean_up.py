@@ -1,8 +1,10 @@
 """Drop-ins for veris/clean_up.py."""
 from ._abi import check
+from .hostarrays import accepts_host_state
 from .state import Call
 
 
+@accepts_host_state
 def clean_up_advection(state):
     """veris/clean_up.py:5-39 -> (hIceMean, hSnowMean, Area, TSurf, os_hIceMean, os_hSnowMean)."""
     c = Call(state)
@@ -12,6 +14,7 @@ def clean_up_advection(state):
     return tuple(out)
 
 
+@accepts_host_state
 def ridging(state):
     """veris/clean_up.py:42-47 -> Area capped at 1."""
     c = Call(state)

@@ -1,9 +1,11 @@
 """Drop-ins for veris/dynamics_routines.py: ice strength, drag coefficients,
 strain rates, viscosities and stress divergence."""
 from ._abi import check
+from .hostarrays import accepts_host_state
 from .state import Call
 
 
+@accepts_host_state
 def SeaIceStrength(state):
     """veris/dynamics_routines.py:5-18 -> SeaIceStrength."""
     c = Call(state)
@@ -12,6 +14,7 @@ def SeaIceStrength(state):
     return P
 
 
+@accepts_host_state
 def ocean_drag_coeffs(state, uIce, vIce):
     """veris/dynamics_routines.py:21-52 -> cDrag at C points."""
     c = Call(state)
@@ -21,6 +24,7 @@ def ocean_drag_coeffs(state, uIce, vIce):
     return cd
 
 
+@accepts_host_state
 def basal_drag_coeffs(state, uIce, vIce):
     """veris/dynamics_routines.py:55-96 -> cBot at C points."""
     c = Call(state)
@@ -30,6 +34,7 @@ def basal_drag_coeffs(state, uIce, vIce):
     return cb
 
 
+@accepts_host_state
 def side_drag(state, uIce, vIce):
     """veris/dynamics_routines.py:99-140 -> (SideDragU, SideDragV)."""
     c = Call(state)
@@ -39,6 +44,7 @@ def side_drag(state, uIce, vIce):
     return sU, sV
 
 
+@accepts_host_state
 def strainrates(state, uIce, vIce):
     """veris/dynamics_routines.py:143-217 -> (e11, e22, e12)."""
     c = Call(state)
@@ -49,6 +55,7 @@ def strainrates(state, uIce, vIce):
     return e11, e22, e12
 
 
+@accepts_host_state
 def viscosities(state, e11, e22, e12):
     """veris/dynamics_routines.py:220-268 -> (zeta, eta, press)."""
     c = Call(state)
@@ -59,6 +66,7 @@ def viscosities(state, e11, e22, e12):
     return zeta, eta, press
 
 
+@accepts_host_state
 def stressdiv(state, sig11, sig22, sig12):
     """veris/dynamics_routines.py:284-303 -> (stressDivX, stressDivY)."""
     c = Call(state)

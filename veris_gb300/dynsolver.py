@@ -1,10 +1,12 @@
 """Drop-ins for veris/dynsolver.py: air-ice stress, wind forcing, solver dispatch."""
 from ._abi import check
+from .hostarrays import accepts_host_state
 from .state import Call
 from .evp_solver import evp_solver
 from .freedrift_solver import freedrift_solver
 
 
+@accepts_host_state
 def tauXY(state):
     """veris/dynsolver.py:7-47 -> (tauX, tauY) at U and V points."""
     c = Call(state)
@@ -13,6 +15,7 @@ def tauXY(state):
     return tX, tY
 
 
+@accepts_host_state
 def WindForcingXY(state):
     """veris/dynsolver.py:50-84 -> (WindForcingX, WindForcingY)."""
     c = Call(state)
@@ -22,6 +25,7 @@ def WindForcingXY(state):
     return fx, fy
 
 
+@accepts_host_state
 def IceVelocities(state):
     """veris/dynsolver.py:87-102 -> (uIce, vIce, sigma1, sigma2, sigma12).
 

@@ -2,6 +2,7 @@
 import torch
 
 from ._abi import check
+from .hostarrays import accepts_host_state
 from .state import Call
 
 
@@ -11,6 +12,7 @@ printEvpResidual = False
 last_residuals = None
 
 
+@accepts_host_state
 def evp_solver(state, n_subcycles=None):
     """veris/evp_solver.py:257-319 -> (uIce, vIce, sigma1, sigma2, sigma12).
 
@@ -39,6 +41,7 @@ def evp_solver(state, n_subcycles=None):
     return tuple(out)
 
 
+@accepts_host_state
 def evp_solver_residuals(state, n_subcycles=None, precision="f64"):
     """The loop with the residual diagnostics of veris/evp_solver.py:193-234
     -> (uIce, vIce, sigma1, sigma2, sigma12, resU, resSig).

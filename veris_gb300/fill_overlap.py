@@ -5,8 +5,14 @@ from ._abi import check, load, params_from_settings, VerisGrid
 
 
 def fill_overlap(state, A):
-    """veris/fill_overlap.py:6-18: fills A's halos in place and returns A."""
+    """veris/fill_overlap.py:6-18: fills A's halos in place and returns A
+    (a NumPy array is filled on the GPU and updated in place)."""
     import ctypes
+    from .hostarrays import is_host_array, to_device
+    if is_host_array(A):
+        t = fill_overlap(state, to_device(A))
+        A[...] = t.cpu().numpy()
+        return A
     s = state.settings
     if not (isinstance(A, torch.Tensor) and A.is_cuda and A.dim() == 2 and A.is_contiguous()):
         raise TypeError("A must be a contiguous 2-D CUDA tensor")

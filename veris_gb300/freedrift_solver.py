@@ -3,9 +3,11 @@ stress, one warp-walking kernel."""
 import torch
 
 from ._abi import check
+from .hostarrays import accepts_host_state
 from .state import Call
 
 
+@accepts_host_state
 def freedrift_solver(state):
     """veris/freedrift_solver.py:5-62 -> (uIce, vIce), float64.
 

@@ -4,10 +4,12 @@ import torch
 
 from . import _abi
 from ._abi import check
+from .hostarrays import accepts_host_arrays
 
 BULK_OUTPUTS = ("flwupa", "flha", "fsha", "df0dT", "ust", "vst", "evp", "ssq", "dEvdT")
 
 
+@accepts_host_arrays
 def bulkf_formula_lanl(state, uw, vw, ta, qa, tsf, ocn_mask, outputs=BULK_OUTPUTS):
     """veris/heat_flux_MITgcm.py:5-123 -> (flwupa, flha, fsha, df0dT, ust,
     vst, evp, ssq, dEvdT).

@@ -1,8 +1,10 @@
 """Drop-in for veris/ocean_stress.py."""
 from ._abi import check
+from .hostarrays import accepts_host_state
 from .state import Call
 
 
+@accepts_host_state
 def OceanStressUV(state):
     """veris/ocean_stress.py:8-40 -> (OceanStressU, OceanStressV), halo-filled."""
     c = Call(state)

@@ -124,6 +124,35 @@ SETTINGS = dict(
     ocean_emissivity=(0.985, float, "ocean surface emissivity"),
     gamma_blk=(0.010, float, "adiabatic lapse rate [K/m]"),
     grav=(9.81, float, "gravitational acceleration of the host model (bulk formulae)"),
+    # the rest of the plugin's forcing table (veris/settings.py:144-175): read
+    # by the host model's setup and by the bulk formulae that run before the
+    # step (the CESM ones are not part of this package); listed so that a
+    # setup finds every setting it knows
+    umin_o=(0.5, float, "minimum wind speed over the ocean [m/s]"),
+    umin_i=(1.0, float, "minimum wind speed over ice [m/s]"),
+    zref=(10.0, float, "reference height of the wind [m]"),
+    ztref=(2.0, float, "reference height of the air temperature [m]"),
+    bolzc=(1.38065e-23, float, "Boltzmann constant [J/K/molecule]"),
+    avogad=(6.02214e26, float, "Avogadro number [molecules/kmole]"),
+    rgas=(8314.47, float, "ideal gas constant [J/K/kmole]"),
+    mwdair=(28.966, float, "molecular weight of dry air [kg/kmole]"),
+    mwwv=(18.016, float, "molecular weight of water vapour [kg/kmole]"),
+    rdair=(287.042, float, "gas constant of dry air [J/K/kg]"),
+    rwv=(461.505, float, "gas constant of water vapour [J/K/kg]"),
+    cpwv=(1.810e3, float, "specific heat of water vapour [J/K/kg]"),
+    cpvir=(0.802, float, "specific-heat ratio term"),
+    p0=(1e5, float, "reference pressure of the potential temperature [Pa]"),
+    cappa=(0.286, float, "R / cp"),
+    zzsice=(0.0005, float, "ice surface roughness [m]"),
+    ch=(1e-3, float, "bulk transfer coefficient of sensible heat"),
+    ce=(1.15e-3, float, "bulk transfer coefficient of latent heat"),
+    eps2=(1e-20, float, "threshold"),
+    emissivity=(1.0, float, "surface emissivity"),
+    snow_emissivity=(0.98, float, "snow surface emissivity"),
+    ice_emissivity=(0.98, float, "ice surface emissivity"),
+    tf0kel=(273.15, float, "freezing temperature of fresh water [K]"),
+    ocean_albedo=(0.1, float, "ocean albedo"),
+    ice_albedo=(0.7, float, "ice albedo"),
 )
 
 

@@ -1,8 +1,10 @@
 """Drop-in for veris/solve4temp.py: the float64 surface-temperature Newton solve."""
 from ._abi import check
+from .hostarrays import accepts_host_state
 from .state import Call
 
 
+@accepts_host_state
 def solve4temp(state, hIceActual, hSnowActual, TSurfIn, TempFrz):
     """veris/solve4temp.py:5-174 -> (TSurfOut, F_io_net, F_ia_net, IcePenetSW, FWsublim)."""
     c = Call(state)
