@@ -22,6 +22,8 @@ It writes one ``<case>.npz`` per case next to this script:
   back into the state;
 * ``forcing.npz`` (``--forcing``): free drift and the bulk formula, see
   ``run_forcing``;
+* ``residuals.npz`` (``--residuals``): the reference's residual branch with
+  the two names it leaves unbound patched as ``run_residuals`` describes;
 * ``setup_callsite.json`` and ``plugin.npz`` (``--plugin``): the call
   sequence of the reference setup's sea-ice step as its source writes it
   (``record_callsite``), and the plugin's ``set_inits`` on a host-model grid
@@ -361,6 +363,68 @@ def run_set_inits(R):
     return out
 
 
+RESIDUAL_CASES = ("moving", "small_a", "small_b")
+RESIDUAL_SUBCYCLES = 8
+
+
+def run_residuals(R):
+    """``residuals.npz``: the reference's own residual branch
+    (veris/evp_solver.py:51-56, 191-230) on the state before the first EVP
+    call of three golden cases, 8 subcycles each.
+
+    As shipped the branch cannot run: it reads ``sigma11``/``sigma22``,
+    names nothing binds (its subcycle body computes ``sig11``/``sig22``).
+    What it means, and what is patched in here, in memory only: the stress
+    components 0.5 * (sigma1 +- sigma2) of the state at that point of the
+    body (the incoming state at :54-55, the updated one at :194-195).  The
+    patch rewrites those two names in the body's syntax tree; nothing else
+    changes.  The loop's final carry (which evp_solver drops) is captured by
+    wrapping the module's for_loop; its resSig and resU entries are the
+    residuals."""
+    import ast
+    import inspect
+    import textwrap
+    sys.path.insert(0, REPO)
+    from tests import golden_io as G
+    mod = R.evp
+    tree = ast.parse(textwrap.dedent(inspect.getsource(mod.evp_solver_body)))
+
+    class StressComponents(ast.NodeTransformer):
+        def visit_Name(self, node):
+            if isinstance(node.ctx, ast.Load) and node.id in ("sigma11", "sigma22"):
+                pm = ast.Add() if node.id == "sigma11" else ast.Sub()
+                both = ast.BinOp(ast.Name("sigma1", ast.Load()), pm, ast.Name("sigma2", ast.Load()))
+                return ast.copy_location(ast.BinOp(ast.Constant(0.5), ast.Mult(), both), node)
+            return node
+
+    tree = ast.fix_missing_locations(StressComponents().visit(tree))
+    body_orig, loop_orig = mod.evp_solver_body, mod.for_loop
+    exec(compile(tree, mod.__file__, "exec"), mod.__dict__)
+    carry = {}
+
+    def capture(lo, hi, body, arg):
+        carry["last"] = loop_orig(lo, hi, body, arg)
+        return carry["last"]
+
+    mod.for_loop = capture
+    out = {}
+    try:
+        for case in RESIDUAL_CASES:
+            g = G.load(case)
+            first_evp = [i for i, r, _o in G.sequence(g) if r == "IceVelocities"][0]
+            st = G.state_before(g, first_evp)
+            st.settings.computeEvpResidual = True
+            st.settings.nEVPsteps = RESIDUAL_SUBCYCLES
+            fields = mod.evp_solver(st)
+            for n, a in zip(("uIce", "vIce", "sigma1", "sigma2", "sigma12"), fields):
+                out[f"res.{case}.{n}"] = np.array(a, dtype=np.float64)
+            out[f"res.{case}.resSig"] = np.array(carry["last"][15], dtype=np.float64)
+            out[f"res.{case}.resU"] = np.array(carry["last"][16], dtype=np.float64)
+    finally:
+        mod.evp_solver_body, mod.for_loop = body_orig, loop_orig
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default=os.environ.get("VERIS_REFERENCE"),
@@ -368,11 +432,18 @@ def main():
     ap.add_argument("--cases", nargs="*", default=list(CASES))
     ap.add_argument("--forcing", action="store_true", help="write forcing.npz only")
     ap.add_argument("--plugin", action="store_true", help="write setup_callsite.json and plugin.npz only")
+    ap.add_argument("--residuals", action="store_true", help="write residuals.npz only")
     args = ap.parse_args()
     if not args.reference:
         ap.error("give --reference PATH or set VERIS_REFERENCE")
     np.seterr(all="ignore")    # the reference's where() evaluates both branches
     R = _import_reference(args.reference)
+    if args.residuals:
+        out = run_residuals(R)
+        path = os.path.join(HERE, "residuals.npz")
+        np.savez_compressed(path, **out)
+        print(f"{path}: {len(out)} arrays")
+        return
     if args.plugin:
         site = record_callsite(args.reference)
         path = os.path.join(HERE, "setup_callsite.json")

@@ -189,6 +189,26 @@ def test_evp_residuals_against_oracle(case):
         assert rel.max() <= 1e-8, f"{case} {name}: {rel.max():.3e}"
 
 
+@pytest.mark.parametrize("case", ("moving", "small_a", "small_b"))
+def test_evp_residuals_against_the_reference(case):
+    """The residuals of the reference's own branch (its two unbound names
+    patched to the stress components they stand for; residuals.npz, made by
+    tests/golden/make_golden.py --residuals), to the same 1e-8 as against
+    the oracle."""
+    import os
+    from veris_gb300.evp_solver import evp_solver_residuals
+    z = np.load(os.path.join(G.GOLDEN, "residuals.npz"))
+    n = len(z[f"res.{case}.resU"])
+    gst, _st = _residual_state(case, n)
+    out = evp_solver_residuals(gst, n)
+    for k, name in enumerate(("uIce", "vIce", "sigma1", "sigma2", "sigma12")):
+        assert_close(out[k], z[f"res.{case}.{name}"], f"{case} {name}")
+    for name, a in (("resU", out[5]), ("resSig", out[6])):
+        r = z[f"res.{case}.{name}"]
+        rel = np.abs(cpu(a) - r) / np.maximum(np.abs(r), 1e-300)
+        assert rel.max() <= 1e-8, f"{case} {name}: {rel.max():.3e}"
+
+
 def test_evp_residuals_deterministic_and_f32():
     from veris_gb300.evp_solver import evp_solver_residuals
     from veris_gb300.state import VerisState

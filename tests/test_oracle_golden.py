@@ -4,6 +4,8 @@ The oracle restates the reference's arithmetic in its order of operations, so
 the bar here is bit-exact equality (NaN == NaN never occurs: the fixtures are
 finite).
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -184,3 +186,21 @@ def test_evp_residuals_match_the_plain_loop():
     for a, b in zip((u, v, s1, s2, s12), ref):
         np.testing.assert_array_equal(a, b)
     assert resU.shape == (6,) and (resU > 0).all() and (resSig > 0).all()
+
+
+@pytest.mark.parametrize("case", ("moving", "small_a", "small_b"))
+def test_evp_residuals_against_the_reference(case):
+    """The residuals of the reference's own branch (veris/evp_solver.py:
+    51-56, 191-230, its two unbound names patched to the stress components
+    they stand for; tests/golden/make_golden.py --residuals) equal the
+    oracle's restatement, and the solve is unchanged."""
+    z = np.load(os.path.join(G.GOLDEN, "residuals.npz"))
+    g = G.load(case)
+    first_evp = [i for i, r, _o in G.sequence(g) if r == "IceVelocities"][0]
+    st = G.state_before(g, first_evp)
+    n = len(z[f"res.{case}.resU"])
+    out = O.evp_residuals(st, n=n)
+    for k, name in enumerate(("uIce", "vIce", "sigma1", "sigma2", "sigma12")):
+        np.testing.assert_array_equal(out[k], z[f"res.{case}.{name}"])
+    np.testing.assert_allclose(out[5], z[f"res.{case}.resU"], rtol=1e-14, atol=0)
+    np.testing.assert_allclose(out[6], z[f"res.{case}.resSig"], rtol=1e-14, atol=0)
