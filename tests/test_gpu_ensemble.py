@@ -123,3 +123,72 @@ def test_autotune_picks_a_candidate_and_restores_the_state(tmp_path, monkeypatch
             assert torch.equal(before[m][k], after[k])
     again = autotune.tune(ens, candidates=((0, 2), (1, 3), (3, 4)))
     assert again["cached"] and again["shape"] == res["shape"]
+
+
+FIELDS = ("uIce", "vIce", "hIceMean", "hSnowMean", "Area", "TSurf", "Qnet")
+
+
+def _member_arrays(seed=0):
+    from veris_gb300.synthetic import make_state
+    return [make_state(nx, ny, seed=seed + k, wind_scale=0.5 + 0.25 * k, init_velocity=0.05)
+            for k, (nx, ny) in enumerate(SIZES)]
+
+
+def test_full_steps_advance_every_member_like_a_single_domain_step():
+    """Whole steps (per-member preparation, the batched EVP, per-member ocean
+    stress, advection, clean-up, Growth and fills on parallel branches): each
+    member equals a single-domain float32 engine step whose EVP is the same
+    shared-memory tile (fed through the engine's external-EVP input) bit for
+    bit, and the float64 oracle's step to float32 tolerance."""
+    import copy
+    from types import SimpleNamespace
+    from oracle import veris_oracle as O
+    from veris_gb300.engine import SeaIceStep
+    from veris_gb300.ensemble import Ensemble
+    from veris_gb300.evp_solver import evp_solver_fast
+    from veris_gb300.state import VerisState
+    from veris_gb300.synthetic import config_settings
+    sett = config_settings("c4_ensemble", nEVPsteps=N_SUB)
+    arrays = _member_arrays()
+    members = [VerisState.from_numpy(a, sett) for a in arrays]
+    ens = Ensemble(members, N_SUB, shape=0, blocks_per_sm=2, full_step=True, branches=3)
+    ens.step()
+    torch.cuda.synchronize()
+    for m, a in enumerate(arrays):
+        st = VerisState.from_numpy(a, sett)
+        eng = SeaIceStep(st, precision="f32", evp="external", check_finite=False)
+        eng._enqueue_prep()
+        for t, r in zip(eng.evp_out32, evp_solver_fast(st, "f32", form="smem", n_subcycles=N_SUB)):
+            t.copy_(r)
+        eng._enqueue_evp()
+        eng._enqueue_post()
+        ref = SimpleNamespace(variables=SimpleNamespace(**{k: v.copy() for k, v in a.items()}),
+                              settings=copy.copy(sett))
+        O.step(ref)
+        torch.cuda.synchronize()
+        for k in FIELDS:
+            got = getattr(members[m].variables, k)
+            assert torch.equal(got, getattr(st.variables, k)), (m, k)
+            b = getattr(ref.variables, k)
+            e = float(np.abs(got.cpu().numpy() - b).max() / max(np.abs(b).max(), 1e-300))
+            assert e <= 1e-4, (m, k, e)
+
+
+def test_full_steps_graph_equals_eager():
+    from veris_gb300.ensemble import Ensemble
+    from veris_gb300.state import VerisState
+    from veris_gb300.synthetic import config_settings
+    sett = config_settings("c4_ensemble", nEVPsteps=N_SUB)
+    arrays = _member_arrays(5)
+    a = Ensemble([VerisState.from_numpy(x, sett) for x in arrays], N_SUB, shape=6, full_step=True, branches=4)
+    b = Ensemble([VerisState.from_numpy(x, sett) for x in arrays], N_SUB, shape=6, full_step=True, branches=4)
+    for _ in range(3):
+        a.step()
+    b.step()
+    b.capture()
+    b.step()
+    b.step()
+    torch.cuda.synchronize()
+    for m in range(len(arrays)):
+        for k in FIELDS:
+            assert torch.equal(getattr(a.members[m].variables, k), getattr(b.members[m].variables, k)), (m, k)

@@ -71,8 +71,10 @@ class SeaIceStep:
                  f32_kernel="walk", walk_rows=0, walk_variant=0, check_finite=True, budgets=False):
         if precision not in ("f64", "f32"):
             raise ValueError("precision must be 'f64' or 'f32'")
-        if evp not in ("auto", "fast", "plain"):
-            raise ValueError("evp must be 'auto', 'fast' or 'plain'")
+        if evp not in ("auto", "fast", "plain", "external"):
+            raise ValueError("evp must be 'auto', 'fast', 'plain' or 'external'")
+        if evp == "external" and precision != "f32":
+            raise ValueError("an external EVP (the batched ensemble's) takes float32 velocities and stresses")
         if f32_kernel not in ("tma", "walk"):
             raise ValueError("f32_kernel must be 'tma' or 'walk'")
         self.state = state
@@ -98,7 +100,7 @@ class SeaIceStep:
         e = lambda dt=torch.float64: torch.empty(self.shape, dtype=dt, device=self.device)
         self.evp_out = [e() for _ in EVP_OUT]
         self.tmp = [e() for _ in range(2)]
-        viol = self._fast_violations()
+        viol = 0 if evp == "external" else self._fast_violations()
         # cell areas varying along both axes: only the register walk cannot
         # take them (it holds them per column); the tile forms can
         self.area2d = bool(viol & V_AREA2D)
@@ -110,9 +112,11 @@ class SeaIceStep:
                 self.f32_kernel = "tma"
         if evp == "fast" and self.fast_violations:
             raise ValueError(f"the fast EVP form does not cover this state (violations {self.fast_violations:#x})")
-        self.evp_form = "plain" if (evp == "plain" or self.fast_violations) else "fast"
+        self.evp_form = ("external" if evp == "external" else
+                         "plain" if (evp == "plain" or self.fast_violations) else "fast")
         esize = 8 if precision == "f64" else 4
-        wsb = (self.lib.veris_evp_fast_workspace_bytes(ctypes.byref(self.grid), esize) if self.evp_form == "fast"
+        wsb = (256 if self.evp_form == "external" else
+               self.lib.veris_evp_fast_workspace_bytes(ctypes.byref(self.grid), esize) if self.evp_form == "fast"
                else self.lib.veris_evp_workspace_bytes(ctypes.byref(self.grid), esize))
         self.ws_evp = torch.empty(wsb, dtype=torch.uint8, device=self.device)
         self.ws_adv = torch.empty(self.lib.veris_advection_workspace_bytes(ctypes.byref(self.grid), 8),
@@ -223,11 +227,21 @@ class SeaIceStep:
         with ``growth_chunks`` > 1 Growth runs as that many launches over
         consecutive row blocks, each followed by ``marks("growth_rows",
         (row_begin, row_end))``."""
+        mark = marks if marks is not None else (lambda name, rows=None: None)
+        mark("start")
+        n = self._enqueue_prep()
+        mark("preparation")
+        n += self._enqueue_evp(evp_events)
+        mark("evp")
+        return n + self._enqueue_post(mark, growth_chunks)
+
+    def _enqueue_prep(self):
+        """The step up to the EVP: held forcing, the starting budgets and the
+        dynamics preparation (veris/setup/seaice_global_4deg/
+        seaice_global_4deg.py:879-888); returns the launch count."""
         lib, v, st = self.lib, self.state.variables, self.stream
         r64 = self._refs(self.f64)
-        mark = marks if marks is not None else (lambda name, rows=None: None)
         n = 0
-        mark("start")
         if self.forcing is not None:
             for name, t in self.forcing.items():
                 getattr(v, name).copy_(t)
@@ -239,8 +253,16 @@ class SeaIceStep:
         check("WindForcingXY", lib.veris_wind_forcing_xy_f64(*r64, v.WindForcingX.data_ptr(),
                                                              v.WindForcingY.data_ptr(), st))
         check("SeaIceStrength", lib.veris_sea_ice_strength_f64(*r64, v.SeaIceStrength.data_ptr(), st))
-        n += 4
-        mark("preparation")
+        return n + 4
+
+    def _enqueue_evp(self, evp_events=None):
+        """IceVelocities (veris/dynsolver.py:87-102): the EVP loop (or free
+        drift) and the results into the float64 state; with an external EVP
+        the caller has written the float32 results to ``evp_out32`` and this
+        only converts them.  Returns the launch count."""
+        lib, v, st = self.lib, self.state.variables, self.stream
+        r64 = self._refs(self.f64)
+        n = 0
         if evp_events:
             evp_events[0].record()
         ws = (self.ws_evp.data_ptr(), self.ws_evp.numel(), st)
@@ -260,6 +282,15 @@ class SeaIceStep:
                 self._to32(v.uIce, self.evp_out32[0])
                 self._to32(v.vIce, self.evp_out32[1])
                 n += 5
+        elif self.evp_form == "external":
+            for name in ("hIceMean", "hSnowMean", "Area"):   # the float32 advection's inputs
+                self._to32(getattr(v, name), self.v32[name])
+            n += 3
+            if evp_events:
+                evp_events[1].record()
+            for name, t in zip(EVP_OUT, self.evp_out32):
+                self._to64(t, getattr(v, name))
+            n += len(EVP_OUT)
         elif self.precision == "f64" and self.evp_tape is not None:
             # keep every subcycle's state (gradients of many steps); eager only
             tape = self.evp_tape
@@ -306,7 +337,17 @@ class SeaIceStep:
             for name, t in zip(EVP_OUT, self.evp_out32):
                 self._to64(t, getattr(v, name))
             n += len(EVP_OUT)
-        mark("evp")
+        return n
+
+    def _enqueue_post(self, mark=None, growth_chunks=1):
+        """The step after the EVP: ocean stress, advection, clean-up,
+        ridging, Growth, the halo fills, the closing budgets and the
+        non-finite check (seaice_global_4deg.py:894-932); returns the launch
+        count."""
+        lib, v, st = self.lib, self.state.variables, self.stream
+        r64 = self._refs(self.f64)
+        mark = mark if mark is not None else (lambda name, rows=None: None)
+        n = 0
         check("OceanStressUV", lib.veris_ocean_stress_uv_f64(*r64, v.OceanStressU.data_ptr(),
                                                              v.OceanStressV.data_ptr(), st))
         n += 1

@@ -3,14 +3,25 @@
 ``Ensemble`` folds every member's float64 state into one device workspace
 (float32 fast form: constants + ping-pong state per member) and advances all
 members by one subcycle per launch of a persistent kernel that pulls tiles
-from a global work queue.  One ensemble step is
+from a global work queue.
+
+With ``full_step=True`` one ensemble step is the whole sea-ice step of every
+member (veris/setup/seaice_global_4deg/seaice_global_4deg.py:879-932):
+
+    per member: dynamics preparation, fold of its EVP constants and state
+    -> n_subcycles batched EVP launches over all members
+    -> per member: velocities and stresses back into its float64 state, ocean
+       stress, float32 advection, clean-up, ridging, float64 Growth, halo fills
+
+with the per-member work spread over parallel branches (streams), captured
+with the batched launches as one CUDA graph.  Without it (the dynamics-only
+form) one step is
 
     refold (momentum constant from the current velocities; not on the first step)
     -> n_subcycles batched launches
 
-and is captured as one CUDA graph.  The members' thermodynamic state (ice
-strength, masses, areas, wind forcing) is folded once at construction and
-held fixed: the ensemble advances the EVP dynamics of each member.
+and the members' thermodynamic state (ice strength, masses, areas, wind
+forcing) is folded once at construction and held fixed.
 
 ``sequential_baseline`` runs the same members one after another through the
 single-domain float32 solver (one call per member), the comparison the
@@ -56,10 +67,13 @@ def _fields_of(state):
 class Ensemble:
     """n_subcycles float32 fast-form subcycles per step for many domains."""
 
-    def __init__(self, members, n_subcycles, shape=0, blocks_per_sm=0, prepare=True):
+    def __init__(self, members, n_subcycles, shape=0, blocks_per_sm=0, prepare=True, full_step=False,
+                 branches=16):
         """``members``: float64 VerisStates on one GPU sharing their settings
         (they may differ in size and fields).  With ``prepare`` the dynamics
-        preparation runs on each member first."""
+        preparation runs on each member first.  ``full_step``: every step is
+        the whole sea-ice step of every member, the per-member work on
+        ``branches`` parallel streams."""
         if not members:
             raise ValueError("an ensemble needs at least one member")
         self.lib = _abi.load()
@@ -100,6 +114,15 @@ class Ensemble:
         self.buf = 0
         self.first = True
         self.graphs = {}
+        self.full_step = bool(full_step)
+        if self.full_step:
+            from .engine import SeaIceStep
+            self.members = members
+            # the members' own steps around the batched EVP (no EVP of their own)
+            self.engines = [SeaIceStep(st, precision="f32", evp="external", check_finite=False)
+                            for st in members]
+            self.calls = [_fields_of(st)[0] for st in members]
+            self.branches = [torch.cuda.Stream(self.device) for _ in range(max(1, int(branches)))]
 
     @property
     def stream(self):
@@ -115,8 +138,47 @@ class Ensemble:
             self.n_sub if n_sub is None else int(n_sub), buf, int(refold), self.shape, self.blocks_per_sm,
             self.stream))
 
+    def _enqueue_full(self):
+        """One whole sea-ice step of every member (see the module notes)."""
+        main = torch.cuda.current_stream(self.device)
+        wsb = self.ws.numel()
+        nb = len(self.branches)
+        for b in self.branches:
+            b.wait_stream(main)
+        for m, eng in enumerate(self.engines):
+            with torch.cuda.stream(self.branches[m % nb]):
+                eng._enqueue_prep()
+                check("batch_prep_member", self.lib.veris_batch_prep_member_f32(
+                    self.n, self.grids, ctypes.byref(self.params), self.ws.data_ptr(), wsb, m,
+                    ctypes.byref(self.calls[m].fields), eng.stream))
+        for b in self.branches:
+            main.wait_stream(b)
+        check("batch_evp", self.lib.veris_batch_evp_f32(
+            self.n, self.grids, ctypes.byref(self.params), self.ws.data_ptr(), wsb, self.n_sub, 0, 0,
+            self.shape, self.blocks_per_sm, main.cuda_stream))
+        end = self.n_sub & 1
+        for b in self.branches:
+            b.wait_stream(main)
+        for m, eng in enumerate(self.engines):
+            with torch.cuda.stream(self.branches[m % nb]):
+                check("batch_copy_state", self.lib.veris_batch_copy_state_f32(
+                    self.n, self.grids, ctypes.byref(self.params), self.ws.data_ptr(), wsb, m, end,
+                    *[t.data_ptr() for t in eng.evp_out32], eng.stream))
+                eng._enqueue_evp()
+                eng._enqueue_post()
+        for b in self.branches:
+            main.wait_stream(b)
+
     def step(self):
         """One ensemble step (a captured graph when ``capture`` ran)."""
+        if self.full_step:
+            g = self.graphs.get("full")
+            if g is not None:
+                g.replay()
+            else:
+                self._enqueue_full()
+            self.buf = self.n_sub & 1
+            return
         refold = not self.first
         key = (refold, self.buf)
         g = self.graphs.get(key)
@@ -131,6 +193,16 @@ class Ensemble:
         """Capture the steady-state step (with refold) for each start buffer
         it can meet; the first step after construction still runs eagerly
         (run it before capturing: it also configures the kernels)."""
+        if self.full_step:
+            g = torch.cuda.CUDAGraph()
+            s = torch.cuda.Stream(self.device)
+            s.wait_stream(torch.cuda.current_stream(self.device))
+            with torch.cuda.stream(s):
+                with torch.cuda.graph(g, stream=s):   # records only: nothing runs
+                    self._enqueue_full()
+            torch.cuda.current_stream(self.device).wait_stream(s)
+            self.graphs["full"] = g
+            return
         bufs = (0, 1) if self.n_sub & 1 else (self.buf,)
         for b in bufs:
             g = torch.cuda.CUDAGraph()
@@ -147,7 +219,8 @@ class Ensemble:
         self.graphs = {}
 
     def state(self, m, dtype=torch.float32):
-        """{name: tensor} of member m's current velocities and stresses."""
+        """{name: tensor} of member m's current velocities and stresses (the
+        batch's state after the last EVP)."""
         out = {k: torch.empty(self.shapes[m], dtype=torch.float32, device=self.device) for k in EVP_STATE}
         check("batch_copy_state", self.lib.veris_batch_copy_state_f32(
             self.n, self.grids, ctypes.byref(self.params), self.ws.data_ptr(), self.ws.numel(), m, self.buf,
