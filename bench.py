@@ -84,8 +84,9 @@ def parse():
                     help="float32 EVP kernel: register-walking warps or TMA-staged tiles")
     ap.add_argument("--walk-rows", type=int, default=0, help="rows per walk (0: from the grid and the SM count)")
     ap.add_argument("--walk-variant", type=int, default=-1, help="-1: tuned on the workload")
-    ap.add_argument("--f64-tile-rows", type=int, default=0, choices=(0, 16, 24, 32),
-                    help="rows per tile of the float64 subcycle kernel (0: the library's default)")
+    ap.add_argument("--f64-tile-rows", type=int, default=-1, choices=(-1, 0, 16, 24, 32),
+                    help="rows per tile of the float64 subcycle kernel (0: the library's default; "
+                         "-1: tuned on the workload)")
     ap.add_argument("--adjoint", action="store_true",
                     help="time a trajectory's forward + adjoint against its forward (float64)")
     ap.add_argument("--adjoint-config", default="c3_1deg")
@@ -389,7 +390,7 @@ def rel_errors(a, b):
     return {"max_rel": float(d.max()) / scale, "rms_rel": float(d.pow(2).mean().sqrt()) / scale}
 
 
-def make_engine(arrays, sett, dev, precision, args, walk_variant=None, budgets=False):
+def make_engine(arrays, sett, dev, precision, args, walk_variant=None, budgets=False, tune=False):
     """A captured SeaIceStep on a fresh device copy of ``arrays`` (the
     capture runs one eager step first); the float32 walk is tuned on the
     workload unless a variant is given."""
@@ -404,6 +405,9 @@ def make_engine(arrays, sett, dev, precision, args, walk_variant=None, budgets=F
             and args.walk_variant < 0):
         from veris_gb300.autotune import tune_walk
         tuning = tune_walk(eng)
+    if precision == "f64" and eng.evp_form == "fast" and args.f64_tile_rows < 0 and tune:
+        from veris_gb300.autotune import tune_f64_tile
+        tuning = tune_f64_tile(eng)
     eng.capture()
     return eng, tuning
 
@@ -634,11 +638,11 @@ def c5_block(args, dev, flush):
     cells = c["nx"] * c["ny"]
     sms = torch.cuda.get_device_properties(dev).multi_processor_count
     out = {"config": workload_config(name, c, sett, n_sub)}
-    e64, _ = make_engine(arrays, sett, dev, "f64", args)
+    e64, tuning64 = make_engine(arrays, sett, dev, "f64", args, tune=True)
     ms64, _, _ = time_steps(e64, 2, 1, flush, 1, dev)
     us64 = evp_launch_us(e64, n_sub, flush)
     out["fp64"] = {"value": cells * n_sub * 2 / (ms64 / 1e3) / 1e9, "ms_per_step": ms64 / 2, "steps": 2,
-                   "roofline": roofline_fp64(evp_kernel_name(e64), name, cells, us64, sms)}
+                   "roofline": roofline_fp64(evp_kernel_name(e64), name, cells, us64, sms), "f64_tile": tuning64}
     del e64
     e32, tuning = make_engine(arrays, sett, dev, "f32", args)
     ms32, _, _ = time_steps(e32, 5, 2, flush, 1, dev)
@@ -683,7 +687,7 @@ def run_ours(args):
         build()
     barrier(ws)
     from veris_gb300 import _abi
-    _abi.check("evp_f64_tile_rows", _abi.load().veris_evp_f64_tile_rows(args.f64_tile_rows))
+    _abi.check("evp_f64_tile_rows", _abi.load().veris_evp_f64_tile_rows(max(0, args.f64_tile_rows)))
     from veris_gb300.synthetic import CONFIGS, make_state, config_settings
 
     c = CONFIGS[args.config]
@@ -701,7 +705,7 @@ def run_ours(args):
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
 
     # the headline step, graph-replayed, inputs resident
-    eng, tuning = make_engine(arrays, sett, dev, args.precision, args, budgets=True)
+    eng, tuning = make_engine(arrays, sett, dev, args.precision, args, budgets=True, tune=True)
     ms, wall, clk = time_steps(eng, args.steps, args.warmup, flush, ws, dev, clocks=ClockSampler(local))
     conservation = conservation_summary(eng, args.steps)
     value = replica_value(cells, n_sub, args.steps, ms, ws)
@@ -719,7 +723,8 @@ def run_ours(args):
                     "l2": "flushed before every timed step (512 MiB write)", "graph": "one CUDA graph per step",
                     "evp_form": eng.evp_form, "evp_kernel": kernel,
                     "walk": ({"rows": eng.walk_rows or "auto", "variant": eng.walk_variant, "tuning": tuning}
-                             if args.precision == "f32" and eng.f32_kernel == "walk" else None)},
+                             if args.precision == "f32" and eng.f32_kernel == "walk" else None),
+                    "f64_tile": tuning if args.precision == "f64" else None},
             "roofline": roof, "gpu_launches": eng.launches_per_step * args.steps, "clocks": clk,
             "conservation": conservation,
             "wall_s_timed_region": wall, "evp_ms_per_step": us * n_sub / 1e3,

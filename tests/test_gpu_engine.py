@@ -391,3 +391,39 @@ def test_growth_by_row_blocks_equals_one_launch():
     ptrs = [t.data_ptr() for t in out]
     for a, b in ((-1, 4), (4, 4), (5, 3), (0, NX + 1)):
         assert c.lib.veris_growth_rows_f64(*c.refs(), *ptrs, a, b, c.stream) == 6, (a, b)
+
+
+def test_float64_tile_heights_give_the_same_values_and_the_tuner_picks_one():
+    """The float64 subcycle's tile height (16, 24, 32 rows) changes only the
+    launch: every height gives the same values bit for bit; the tuner keeps
+    one of them and leaves the state alone."""
+    import ctypes
+    from veris_gb300 import _abi
+    from veris_gb300.autotune import tune_f64_tile
+    from veris_gb300.engine import SeaIceStep
+    from veris_gb300.state import Call, VerisState
+    from veris_gb300.synthetic import config_settings, make_state
+    arrays = make_state(150, 70, seed=4, init_velocity=0.1, init_stress=800.0, ice_lat=30.0)
+    sett = config_settings("c1_4deg", nEVPsteps=9)
+    st = VerisState.from_numpy(arrays, sett)
+    lib = _abi.load()
+    c = Call(st)
+    ws, wsb = c.workspace(lib.veris_evp_fast_workspace_bytes(c.refs()[0], 8))
+    res = []
+    try:
+        for rows in (16, 24, 32):
+            assert lib.veris_evp_f64_tile_rows(rows) == 0
+            out = c.empty(5)
+            assert lib.veris_evp_fast_solver_f64(*c.refs(), 9, *[t.data_ptr() for t in out], ws, wsb, c.stream) == 0
+            res.append(out)
+        assert lib.veris_evp_f64_tile_rows(20) == 6
+        for out in res[1:]:
+            for a, b in zip(out, res[0]):
+                assert torch.equal(a, b)
+        eng = SeaIceStep(VerisState.from_numpy(arrays, sett), precision="f64")
+        before = eng.state.variables.uIce.clone()
+        t = tune_f64_tile(eng, subcycles=3, repeats=1)
+        assert t["rows"] in (16, 24, 32) and len(t["trials"]) == 3
+        assert torch.equal(before, eng.state.variables.uIce)
+    finally:
+        lib.veris_evp_f64_tile_rows(0)

@@ -1,7 +1,6 @@
-"""Autotuners: the launch shape of the batched ensemble, and the compiled
-register budget of the single-domain walking EVP kernel.
-
-Ensemble: 
+"""Autotuners: the launch shape of the batched ensemble, the compiled
+register budget of the single-domain walking EVP kernel, and the tile
+height of the float64 EVP kernel.
 
 For an ``Ensemble`` it times every candidate (tile shape x CTAs per SM) on a
 few subcycles with CUDA events, keeps the fastest and caches the choice per
@@ -119,3 +118,42 @@ def tune_walk(eng, variants=(0, 1, 2, 3), subcycles=10, repeats=3):
     eng.walk_variant = best["variant"]
     eng.graph = None
     return {"variant": best["variant"], "trials": trials}
+
+
+F64_TILE_ROWS = (16, 24, 32)
+
+
+def tune_f64_tile(eng, rows=F64_TILE_ROWS, subcycles=10, repeats=3):
+    """Pick the float64 EVP kernel's tile height (16, 24 or 32 rows of 32
+    columns: 4, 3 or 2 CTAs per SM; smaller tiles keep more warps resident
+    to cover the float64 pipe's latency, larger ones do less ring work) for
+    a float64 ``SeaIceStep`` by timing ``subcycles`` subcycles of the
+    engine's state for each (outputs to scratch: the state is not advanced).
+    Sets the choice process-wide (veris_evp_f64_tile_rows) and drops the
+    engine's captured graph."""
+    from ._abi import check
+    if eng.precision != "f64" or eng.evp_form != "fast":
+        raise ValueError("tune_f64_tile: a float64 engine with the fast EVP form")
+    outs = [torch.empty(eng.shape, dtype=torch.float64, device=eng.device) for _ in range(5)]
+    ptrs = [t.data_ptr() for t in outs]
+    ws = (eng.ws_evp.data_ptr(), eng.ws_evp.numel(), eng.stream)
+    r64 = eng._refs(eng.f64)
+    trials = []
+    for r in rows:
+        check("evp_f64_tile_rows", eng.lib.veris_evp_f64_tile_rows(r))
+        run = lambda n: check("evp_fast_f64", eng.lib.veris_evp_fast_solver_f64(*r64, n, *ptrs, *ws))
+        run(2)
+        times = []
+        for _ in range(repeats):
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record()
+            run(subcycles)
+            b.record()
+            b.synchronize()
+            times.append(a.elapsed_time(b) / subcycles)
+        trials.append({"rows": r, "ms_per_subcycle": sorted(times)[len(times) // 2]})
+    best = min(trials, key=lambda t: t["ms_per_subcycle"])
+    check("evp_f64_tile_rows", eng.lib.veris_evp_f64_tile_rows(best["rows"]))
+    eng.graph = None
+    return {"rows": best["rows"], "trials": trials}
