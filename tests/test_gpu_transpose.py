@@ -1,0 +1,76 @@
+"""Dot-product tests of the hand-written adjoint kernels.
+
+For each routine y = f(x) of the step and random x-directions dx and
+y-weights w: <J dx, w> = <dx, J^T w>, with J dx the exact tangent of the
+oracle's restatement of the routine (forward-mode derivatives through NumPy,
+tests/tangent.py, itself checked against centred differences on the CPU) and
+J^T w from the GPU adjoint kernel.  No finite differences, no step size: the
+two sides agree to rounding (bar 1e-10 of the magnitude of the terms).
+Routines: the dynamics preparation (SeaIceMass, AreaWS, WindForcingXY,
+SeaIceStrength), the EVP loop (3 subcycles: every input state field and
+step-constant field), advection, clean-up with ridging, and Growth with
+solve4temp.  States: the reference's own recorded states (golden fixtures),
+jittered off exact ties, directions off the branch switches as in
+tests/transpose_cases.py.
+"""
+import numpy as np
+import pytest
+
+from tests.transpose_cases import CASES, directions, golden_state, jitter, tangent
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-10
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _lib():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from veris_gb300 import _abi
+    return _abi.load()
+
+
+def _adjoint(case, gst, lam):
+    from veris_gb300 import adjoint as A
+    if case == "prep":
+        out, _scal = A.prep_adjoint(gst, lam)
+        return out
+    if case == "advection":
+        fields, vel = A.advection_adjoint(gst, lam)
+        return dict(fields, **vel)
+    if case == "cleanup":
+        return A.cleanup_adjoint(gst, lam)
+    if case == "growth":
+        return A.growth_adjoint(gst, lam)
+    if case == "evp":
+        state, fields, _drag = A.evp_adjoint(gst, lam, n_subcycles=3)
+        return dict(state, **fields)
+    raise KeyError(case)
+
+
+@pytest.mark.parametrize("golden", ["moving", "c1", "small_b"])
+@pytest.mark.parametrize("case", list(CASES))
+def test_adjoint_is_the_transpose_of_the_tangent(case, golden):
+    from veris_gb300.state import VerisState
+    if case == "evp" and golden == "small_b":
+        pytest.skip("second-order boundary terms: the EVP adjoint covers the fast form's settings")
+    rng = np.random.default_rng(5)
+    st = jitter(golden_state(case, golden), rng)
+    _routine, ins, outs, _f = CASES[case]
+    dx = directions(st, ins, rng)
+    jd = tangent(case, st, dx)
+    w = {k: rng.standard_normal(jd[k].shape) for k in outs}
+    lhs_terms = [w[k] * jd[k] for k in outs]
+    lhs = sum(float(t.sum()) for t in lhs_terms)
+
+    gst = VerisState.from_numpy(vars(st.variables), st.settings)
+    lam = {k: torch.as_tensor(w[k], device="cuda") for k in outs}
+    adj = _adjoint(case, gst, lam)
+    torch.cuda.synchronize()
+    rhs_terms = [dx[k] * adj[k].cpu().numpy() for k in ins]
+    rhs = sum(float(t.sum()) for t in rhs_terms)
+    mag = sum(float(np.abs(t).sum()) for t in lhs_terms + rhs_terms)
+    assert mag > 0
+    assert abs(lhs - rhs) <= TOL * mag, f"{case}/{golden}: <J dx, w> {lhs:.12e} <dx, J^T w> {rhs:.12e}"
