@@ -288,9 +288,10 @@ int veris_evp_fast_solver_f64(const VerisGrid *g, const VerisParams *p, const Ve
                               size_t workspace_bytes, veris_stream_t s);
 /*
  * Tile height of the float64 fast-form subcycle kernel (every float64 fast
- * form: solver, tapes, the adjoint's recomputed subcycles): 16, 24 or 32
- * output rows by 32 columns per CTA (4, 3 or 2 CTAs per SM), 0 = the
- * library's default.  Process-wide, for every later launch; same values
+ * form: solver, tapes, the adjoint's recomputed subcycles): work units of
+ * at most 16, 24 or 32 output rows by 32 columns per CTA (4, 3 or 2 CTAs per
+ * SM; the launch ends on a round of smaller units), 0 = the library's
+ * default.  Process-wide, for every later launch; same values
  * for every height.  VERIS_ERR_ARG for other heights.  A tuning knob with no
  * counterpart in the reference.
  */

@@ -27,9 +27,11 @@
 // * warps whose cells all have zero ice strength skip the viscosity's
 //   square root and division (zeta = 0, which the formula gives), warps on
 //   land skip the velocity division;
-// * 24x32 output tiles by default, three 256-thread CTAs per SM (16- and
-//   32-row tiles: four and two; the larger the tile, the less ring work but
-//   the fewer resident warps to cover the float64 pipe's latency).
+// * work units of at most 24 rows x 32 columns by default, three 256-thread
+//   CTAs per SM (16 and 32 rows: four and two; the larger the unit, the
+//   less ring work but the fewer resident warps to cover the float64 pipe's
+//   latency), the launch ending on a round of small units so that the SMs
+//   run out of work together.
 #include "evp_fast.cuh"
 
 namespace veris {
@@ -160,9 +162,20 @@ static_assert(2 * (Smem64<32>::bytes(true) + 1024) <= 228 * 1024, "two 32-row CT
 static_assert(3 * (Smem64<24>::bytes(false) + 1024) <= 228 * 1024, "three 24-row CTAs per SM");
 static_assert(4 * (Smem64<16>::bytes(true) + 1024) <= 228 * 1024, "four 16-row CTAs per SM");
 
+// Work units, one per CTA, in dispatch order: first the P1 pieces of rows
+// [0, R1) of every 32-column strip, then the P2 smaller pieces of rows
+// [R1, NX) of every strip (at most TI rows each, for which the shared memory
+// is sized).  The hardware hands CTAs to SMs in block order as slots free up,
+// so the launch ends on the small pieces and the SMs run out of work
+// together instead of on a thin last wave of full tiles.
+struct F64Units {
+    int P1, R1, P2, U1;
+};
+
 template <int TI, bool BASAL, bool TURN>
 __global__ void __launch_bounds__(F64_THREADS, f64_min_blocks(TI))
-evp_f64_kernel(Dims d, int64_t lp, HaloFill h, FastConsts<double> c, F64Scalars k, FastIO<double> io) {
+evp_f64_kernel(Dims d, int64_t lp, HaloFill h, FastConsts<double> c, F64Scalars k, FastIO<double> io,
+               F64Units w) {
     using S = Smem64<TI>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     double *sU = reinterpret_cast<double *>(smem_raw);
@@ -178,7 +191,18 @@ evp_f64_kernel(Dims d, int64_t lp, HaloFill h, FastConsts<double> c, F64Scalars 
     double *sCb = sFu + S::NC;    // basal drag only
     uint32_t *sF = reinterpret_cast<uint32_t *>(sCb + (BASAL ? S::NC : 0));
     double *sS12 = sZq;
-    const int i0 = blockIdx.y * S::TI, j0 = blockIdx.x * S::TJ;
+    int i0, ti, j0;
+    {
+        const int unit = blockIdx.x;
+        const bool big = unit < w.U1;
+        const int P = big ? w.P1 : w.P2, v = big ? unit : unit - w.U1;
+        const int r0 = big ? 0 : w.R1, rows = big ? w.R1 : d.NX - w.R1, pc = v % P;
+        i0 = r0 + (int)((int64_t)pc * rows / P);
+        ti = r0 + (int)((int64_t)(pc + 1) * rows / P) - i0;
+        j0 = (v / P) * S::TJ;
+    }
+    // the unit's region sizes (ti <= TI rows)
+    const int nS = (ti + 4) * S::WS, nZ = (ti + 3) * S::WZ, nB = (ti + 2) * S::WB, nC = (ti + 1) * S::WC;
     const int tid = threadIdx.x;
     constexpr unsigned ALL = 0xffffffffu;
 #define IS(li, lj) (((li) + 2) * S::WS + ((lj) + 2))
@@ -191,7 +215,7 @@ evp_f64_kernel(Dims d, int64_t lp, HaloFill h, FastConsts<double> c, F64Scalars 
     auto voc = [&](int li, int lj) { return __ldg(c.vOc + (int64_t)d.wxt(i0 + li) * lp + d.wyt(j0 + lj)); };
 
     // ---- stage u, v and the flags of the tile plus a 2-cell ring
-    for (int idx = tid; idx < S::NS; idx += F64_THREADS) {
+    for (int idx = tid; idx < nS; idx += F64_THREADS) {
         const int li = idx / S::WS - 2, lj = idx % S::WS - 2;
         const int64_t o = (int64_t)d.wxt(i0 + li) * lp + d.wyt(j0 + lj);
         sU[idx] = __ldg(io.u + o);
@@ -201,10 +225,10 @@ evp_f64_kernel(Dims d, int64_t lp, HaloFill h, FastConsts<double> c, F64Scalars 
     __syncthreads();
 
     // ---- A: e12 at Z points [-1, TI+1] x [-1, TJ+1] (veris/dynamics_routines.py:160-175)
-    for (int base = 0; base < S::NZ; base += F64_THREADS) {
+    for (int base = 0; base < nZ; base += F64_THREADS) {
         const int idx = base + tid;
-        const unsigned m = __ballot_sync(ALL, idx < S::NZ);
-        if (idx >= S::NZ) continue;
+        const unsigned m = __ballot_sync(ALL, idx < nZ);
+        if (idx >= nZ) continue;
         const int li = idx / S::WZ - 1, lj = idx % S::WZ - 1;
         const int gi = d.wxt(i0 + li), gj = d.wyt(j0 + lj);
         const uint32_t f0 = sF[IS(li, lj)], fw = sF[IS(li - 1, lj)], fs = sF[IS(li, lj - 1)],
@@ -233,10 +257,10 @@ evp_f64_kernel(Dims d, int64_t lp, HaloFill h, FastConsts<double> c, F64Scalars 
 
     // ---- B: viscosities at C [-1, TI] x [-1, TJ] (veris/dynamics_routines.py:220-268);
     //      stresses, drag and Coriolis terms on [-1, TI) x [-1, TJ) (veris/evp_solver.py:80-145)
-    for (int base = 0; base < S::NB; base += F64_THREADS) {
+    for (int base = 0; base < nB; base += F64_THREADS) {
         const int idx = base + tid;
-        const unsigned m = __ballot_sync(ALL, idx < S::NB);
-        if (idx >= S::NB) continue;
+        const unsigned m = __ballot_sync(ALL, idx < nB);
+        if (idx >= nB) continue;
         const int li = idx / S::WB - 1, lj = idx % S::WB - 1;
         const int gi = d.wxt(i0 + li), gj = d.wyt(j0 + lj);
         const int64_t o = (int64_t)gi * lp + gj;
@@ -258,7 +282,7 @@ evp_f64_kernel(Dims d, int64_t lp, HaloFill h, FastConsts<double> c, F64Scalars 
             zeta = div64(Ph, delta + k.deltaMin, m);
         }
         sZeta[idx] = zeta;
-        const bool in2 = li < S::TI && lj < S::TJ;
+        const bool in2 = li < ti && lj < S::TJ;
         const unsigned m2 = __ballot_sync(m, in2);
         if (in2) {
             const int q = IC(li, lj);
@@ -306,7 +330,7 @@ evp_f64_kernel(Dims d, int64_t lp, HaloFill h, FastConsts<double> c, F64Scalars 
 
     // ---- C: sigma12 at Z [0, TI] x [0, TJ] (veris/evp_solver.py:101-103 with
     //      veris/averaging.py:4-19); sZq is dead: it takes sigma12
-    for (int idx = tid; idx < S::NC; idx += F64_THREADS) {
+    for (int idx = tid; idx < nC; idx += F64_THREADS) {
         const int li = idx / S::WC, lj = idx % S::WC;
         const int gi = d.wxt(i0 + li), gj = d.wyt(j0 + lj);
         const uint32_t n = (sF[IS(li, lj)] & F_MC) + (sF[IS(li - 1, lj)] & F_MC) + (sF[IS(li, lj - 1)] & F_MC) +
@@ -316,16 +340,16 @@ evp_f64_kernel(Dims d, int64_t lp, HaloFill h, FastConsts<double> c, F64Scalars 
                           (sZeta[IB(li, lj - 1)] + sZeta[IB(li - 1, lj - 1)]);
         const double s12 = fma(__ldg(io.s12 + (int64_t)gi * lp + gj), k.am1r, (nh * zs) * sE12[IZ(li, lj)]);
         sS12[idx] = s12;
-        if (li < S::TI && lj < S::TJ && i0 + li < d.NX && j0 + lj < d.NY) io.s12o[(int64_t)gi * io.ldo + gj] = s12;
+        if (li < ti && lj < S::TJ && i0 + li < d.NX && j0 + lj < d.NY) io.s12o[(int64_t)gi * io.ldo + gj] = s12;
     }
     __syncthreads();
 
     // ---- D: u, v at the tile's U and V points (veris/evp_solver.py:105-187)
-    for (int base = 0; base < S::TI * S::TJ; base += F64_THREADS) {
+    for (int base = 0; base < ti * S::TJ; base += F64_THREADS) {
         const int idx = base + tid;
         const int li = idx / S::TJ, lj = idx % S::TJ;
         const int gi = i0 + li, gj = j0 + lj;
-        const bool act = idx < S::TI * S::TJ && gi < d.NX && gj < d.NY;
+        const bool act = idx < ti * S::TJ && gi < d.NX && gj < d.NY;
         const unsigned m = __ballot_sync(ALL, act);
         if (!act) continue;
         const int64_t o = (int64_t)gi * lp + gj;
@@ -392,6 +416,29 @@ evp_f64_kernel(Dims d, int64_t lp, HaloFill h, FastConsts<double> c, F64Scalars 
 #undef IZZ
 }
 
+// The units of a launch: when all full pieces fit the resident CTAs' slots
+// at once, the fewest pieces of at most TI rows; otherwise a last round of
+// about one small piece (TI/3 rows) per slot at the bottom of every strip,
+// the rest in full pieces.  (Equal full tiles left a thin last wave: 12 % of
+// the SM cycles idle on 1440 x 720 with 24-row tiles.)
+static F64Units f64_units(const Dims &d, int TI, int slots) {
+    const int strips = (d.NY + 31) / 32;
+    F64Units w;
+    const int minP = (d.NX + TI - 1) / TI;
+    w.P2 = 0;
+    w.R1 = d.NX;
+    if ((int64_t)strips * minP > slots) {
+        const int small = TI / 3 > 4 ? TI / 3 : 4;
+        w.P2 = (slots + strips - 1) / strips;
+        const int r2 = w.P2 * small;
+        if (r2 < d.NX / 2) w.R1 = d.NX - r2;
+        else w.P2 = 0;
+    }
+    w.P1 = (w.R1 + TI - 1) / TI;
+    w.U1 = strips * w.P1;
+    return w;
+}
+
 template <int TI, bool B, bool R>
 static int launch64(const Dims &d, int64_t lp, const HaloFill &h, const FastConsts<double> &c, const F64Scalars &k,
                     const FastIO<double> &io, cudaStream_t st) {
@@ -400,8 +447,22 @@ static int launch64(const Dims &d, int64_t lp, const HaloFill &h, const FastCons
     const size_t sm = S::bytes(B);
     static std::atomic<bool> configured[MAX_DEVICES];
     if (!smem_configured(configured, kern, (int)sm)) return VERIS_ERR_LAUNCH;
-    dim3 grid((d.NY + S::TJ - 1) / S::TJ, (d.NX + S::TI - 1) / S::TI);
-    kern<<<grid, F64_THREADS, sm, st>>>(d, lp, h, c, k, io);
+    static std::atomic<int> resident[MAX_DEVICES];   // CTAs per SM (0: not queried yet)
+    const int dev = current_device();
+    if (dev < 0) return VERIS_ERR_LAUNCH;
+    int per = resident[dev].load(std::memory_order_acquire);
+    if (per == 0) {
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, F64_THREADS, sm) != cudaSuccess || per < 1) {
+            cudaGetLastError();
+            return VERIS_ERR_LAUNCH;
+        }
+        resident[dev].store(per, std::memory_order_release);
+    }
+    const int sms = sm_count();
+    if (sms <= 0) return VERIS_ERR_LAUNCH;
+    const F64Units w = f64_units(d, TI, per * sms);
+    const int units = w.U1 + ((d.NY + S::TJ - 1) / S::TJ) * w.P2;
+    kern<<<units, F64_THREADS, sm, st>>>(d, lp, h, c, k, io, w);
     return launch_status();
 }
 
@@ -415,9 +476,9 @@ static int launch64_rows(const Dims &d, int64_t lp, const HaloFill &h, const Fas
 
 // rows per tile of later float64 subcycles (0: the default); process-wide
 static std::atomic<int> g_tile_rows{0};
-// measured on GB300 (500-subcycle workloads): 24 rows 209.7 / 1159.7 us per
-// subcycle on 1440x720 / 3600x1800, against 210.0 / 1180.5 (16) and
-// 229.0 / 1229.2 (32)
+// measured on GB300 (ordered units): 24 rows 204.0 / 1153.0 us per subcycle
+// on 1440x720 / 3600x1800, against 202.6 / 1173.3 (16) and 222.7 / 1240.8
+// (32); the bench's tuner picks per workload
 constexpr int F64_DEFAULT_ROWS = 24;
 
 int fast64_subcycle(const Dims &d, const HaloFill &h, const FastConsts<double> &c, const FastScalars<double> &ks,
