@@ -375,10 +375,12 @@ int veris_evp_adjoint_f64(const VerisGrid *g, const VerisParams *p, const VerisF
 
 /*
  * Taping forms for gradients of many steps (float64 fast form): the forward
- * keeps every subcycle's state in a caller buffer of veris_evp_tape_bytes()
- * (slot k = the five state arrays after k subcycles, internal pitch), and the
- * adjoint reads the tape instead of recomputing the subcycles.  Same values
- * as veris_evp_fast_solver_f64 and veris_evp_adjoint_f64.
+ * keeps every subcycle in a caller buffer of veris_evp_tape_bytes() (slot k,
+ * five arrays of internal pitch: uIce and vIce after k subcycles, and the
+ * Delta, zeta and ocean-drag coefficient that subcycle k + 1 computes from
+ * them; the stresses, which the adjoint does not read, are not kept), and
+ * the adjoint reads the tape instead of recomputing the subcycles.  Same
+ * values as veris_evp_fast_solver_f64 and veris_evp_adjoint_f64.
  */
 size_t veris_evp_tape_bytes(const VerisGrid *g, int32_t elem_size, int32_t n_subcycles);
 int veris_evp_fast_tape_f64(const VerisGrid *g, const VerisParams *p, const VerisFieldsF64 *vs,

@@ -21,20 +21,13 @@
 // Non-differentiable points take these subgradients: sqrt at Delta = 0 and at
 // a drag argument of 0 give 0; the ocean-drag floor (cDragMin) and the
 // "denominator = 0 -> 1" guard contribute nothing on their constant branch.
-#include "evp_fast.cuh"
+#include "evp_adjoint.cuh"
 
 namespace veris {
 
 namespace adj {
 
 constexpr int TJ = 32, THREADS = 256;   // tile columns and threads; rows TI per instantiation
-
-template <class T>
-struct Adj {
-    // adjoints of the folded constants (internal pitch), accumulated over subcycles
-    T *Ph, *mfC, *bfac, *mU, *cU, *AW, *uOc, *mV, *cV, *AS, *vOc;
-    double *dragN, *dragS;   // d/d waterIceDrag, d/d waterIceDrag_south
-};
 
 template <class T>
 struct Io {
@@ -605,6 +598,7 @@ struct Plan {
     int *status;
     Adj<T> a;
     T *cp, *seg, *lam[2][5];
+    double *scr[N_SCRATCH64];   // float64: the gather passes' arrays
     size_t field;   // bytes of one internal array
     size_t total;
 };
@@ -626,6 +620,8 @@ static size_t plan(const Dims &d, int n, int K, char *base, Plan<T> *pl, bool ta
     pl->seg = reinterpret_cast<T *>(take(taped ? 0 : (size_t)(K + 1) * 5 * pl->field));
     for (int b = 0; b < 2; ++b)
         for (int q = 0; q < 5; ++q) pl->lam[b][q] = reinterpret_cast<T *>(take(pl->field));
+    for (int q = 0; q < N_SCRATCH64; ++q)
+        pl->scr[q] = sizeof(T) == 8 ? reinterpret_cast<double *>(take(pl->field)) : nullptr;
     pl->total = off;
     return off;
 }
@@ -702,7 +698,14 @@ static int evp_adjoint(const VerisGrid *g, const VerisParams *p, const VerisFiel
             for (int q = 0; q < 5; ++q) segs[q] = slot(pl.seg, pl.field, 0, q);
             T *cps[5];
             for (int q = 0; q < 5; ++q) cps[q] = slot(pl.cp, pl.field, m, q);
-            if ((stt = copy_state<T>(segs, cps, pl.field, st)) != VERIS_OK) return stt;
+            if constexpr (sizeof(T) == 8) {
+                // float64 segment slots hold (u, v, Delta, zeta, cDrag); the
+                // stresses run in the workspace's state buffers
+                T *to[5] = {segs[0], segs[1], pl.st2[0][2], pl.st2[0][3], pl.st2[0][4]};
+                if ((stt = copy_state<T>(to, cps, pl.field, st)) != VERIS_OK) return stt;
+            } else {
+                if ((stt = copy_state<T>(segs, cps, pl.field, st)) != VERIS_OK) return stt;
+            }
         }
         for (int ss = s0; ss < s1 && !taped; ++ss) {
             const T *cur[5];
@@ -712,15 +715,44 @@ static int evp_adjoint(const VerisGrid *g, const VerisParams *p, const VerisFiel
                 dst[q] = slot(pl.seg, pl.field, ss - s0 + 1, q);
             }
             FastIO<T> io{cur[0], cur[1], cur[2], cur[3], cur[4], dst[0], dst[1], dst[2], dst[3], dst[4], lp};
+            if constexpr (sizeof(T) == 8) {
+                T *const *a = pl.st2[(ss - s0) % 2], *const *b = pl.st2[(ss - s0 + 1) % 2];
+                io.s1 = a[2]; io.s2 = a[3]; io.s12 = a[4];
+                io.s1o = b[2]; io.s2o = b[3]; io.s12o = b[4];
+                io.tDel = slot(pl.seg, pl.field, ss - s0, 2);
+                io.tZeta = slot(pl.seg, pl.field, ss - s0, 3);
+                io.tCd = slot(pl.seg, pl.field, ss - s0, 4);
+            }
             if ((stt = fast_subcycle<T>(d, h, pl.c, k, io, basal, turn, st)) != VERIS_OK) return stt;
         }
         for (int ss = s1 - 1; ss >= s0; --ss) {
             const bool first = ss == n - 1;
             T *out[5];
             for (int q = 0; q < 5; ++q) out[q] = pl.lam[first ? 0 : lb ^ 1][q];
+            const int rs = taped ? ss : ss - s0;   // slot of this subcycle's input state
+            if constexpr (sizeof(T) == 8) {
+                // gather passes: every adjoint array written whole, nothing to clear
+                const Tape64 tt{slot(segb, pl.field, rs, 0), slot(segb, pl.field, rs, 1), slot(segb, pl.field, rs, 2),
+                                slot(segb, pl.field, rs, 3), slot(segb, pl.field, rs, 4),
+                                slot(segb, pl.field, rs + 1, 0), slot(segb, pl.field, rs + 1, 1)};
+                Lam64 ll;
+                if (first) {
+                    ll.lu = lout[0]; ll.lv = lout[1]; ll.ls1 = lout[2]; ll.ls2 = lout[3]; ll.ls12 = lout[4];
+                    ll.ldl = d.ld;
+                } else {
+                    ll.lu = pl.lam[lb][0]; ll.lv = pl.lam[lb][1]; ll.ls1 = pl.lam[lb][2];
+                    ll.ls2 = pl.lam[lb][3]; ll.ls12 = pl.lam[lb][4];
+                    ll.ldl = lp;
+                }
+                ll.ou = out[0]; ll.ov = out[1]; ll.os1 = out[2]; ll.os2 = out[3]; ll.os12 = out[4];
+                if ((stt = adjoint64_subcycle(d, lp, h, pl.c, k, p->rhoSea, tt, ll, pl.a, pl.scr, basal, turn, st)) !=
+                    VERIS_OK)
+                    return stt;
+                lb = first ? 0 : lb ^ 1;
+                continue;
+            }
             // the five adjoint arrays of a buffer are contiguous: one memset
             if (cudaMemsetAsync(out[0], 0, 5 * pl.field, st) != cudaSuccess) return VERIS_ERR_LAUNCH;
-            const int rs = taped ? ss : ss - s0;   // slot of this subcycle's input state
             Io<T> io;
             // a float32 tape is written by the register walk in its own
             // layout: (u, v, sigma1, sigma2) per point over the slot's first

@@ -252,8 +252,12 @@ template int fast_subcycle<double>(const Dims &, const HaloFill &, const FastCon
 template <class T>
 static size_t tape_field(const Dims &d) { return rup256((size_t)d.NX * internal_pitch(d.NY) * sizeof(T)); }
 
-// tape != nullptr: every subcycle's state is kept, slot k (5 arrays of
-// tape_field bytes each, pitch lp) holding the state after k subcycles
+// tape != nullptr: every subcycle is kept, slot k (5 arrays of tape_field
+// bytes each, pitch lp) holding the state after k subcycles; in float64
+// slot k holds (u_k, v_k, Delta_k, zeta_k, cDrag_k), the velocities after
+// k subcycles and the viscosity and drag terms subcycle k + 1 computes from
+// them (the adjoint needs no stresses; they run in the workspace's state
+// buffers)
 template <class T>
 static int evp_fast(const VerisGrid *g, const VerisParams *p, const VerisFieldsF64 *vs64, int n, T *uo, T *vo,
                     T *s1o, T *s2o, T *s12o, void *ws, size_t wsb, int allow_tma, veris_stream_t s,
@@ -282,8 +286,10 @@ static int evp_fast(const VerisGrid *g, const VerisParams *p, const VerisFieldsF
     const size_t tf = tape_field<T>(d);
     if (tape) VERIS_REQUIRE(tape_bytes >= (size_t)(n + 1) * 5 * tf, VERIS_ERR_WORKSPACE);
     auto tslot = [&](int sl, int q) { return reinterpret_cast<T *>(reinterpret_cast<char *>(tape) + ((size_t)sl * 5 + q) * tf); };
+    // float64 tapes: the stresses stay in the workspace's state buffers
+    constexpr bool rich = sizeof(T) == 8;
     T *s0[5];
-    for (int q = 0; q < 5; ++q) s0[q] = tape ? tslot(0, q) : state[0][q];
+    for (int q = 0; q < 5; ++q) s0[q] = tape && !(rich && q >= 2) ? tslot(0, q) : state[0][q];
     dim3 g2((d.NY + 31) / 32, (d.NX + 7) / 8);
     if (basal)
         fast_prep_kernel<T, true><<<g2, dim3(32, 8), 0, st>>>(*p, f, d, lp, c, s0[0], s0[1], s0[2], s0[3], s0[4],
@@ -316,6 +322,12 @@ static int evp_fast(const VerisGrid *g, const VerisParams *p, const VerisFieldsF
                 FastIO<T> io{tslot(it, 0), tslot(it, 1), tslot(it, 2), tslot(it, 3), tslot(it, 4),
                              tslot(it + 1, 0), tslot(it + 1, 1), tslot(it + 1, 2), tslot(it + 1, 3), tslot(it + 1, 4),
                              lp};
+                if constexpr (rich) {
+                    T *const *a = state[it % 2], *const *b = state[(it + 1) % 2];
+                    io.s1 = a[2]; io.s2 = a[3]; io.s12 = a[4];
+                    io.s1o = b[2]; io.s2o = b[3]; io.s12o = b[4];
+                    io.tDel = tslot(it, 2); io.tZeta = tslot(it, 3); io.tCd = tslot(it, 4);
+                }
                 if ((stt = fast_subcycle<T>(d, h, c, k, io, basal, turn, st)) != VERIS_OK) return stt;
             }
         }
@@ -325,10 +337,12 @@ static int evp_fast(const VerisGrid *g, const VerisParams *p, const VerisFieldsF
                 return evp_walk_unpack(d, tslot(n, 0), tslot(n, 4), o5, d.ld, st);
             }
         }
-        for (int q = 0; q < 5; ++q)
-            if (cudaMemcpy2DAsync(outs[q], d.ld * sizeof(T), tslot(n, q), lp * sizeof(T), d.NY * sizeof(T), d.NX,
+        for (int q = 0; q < 5; ++q) {
+            const T *from = rich && q >= 2 ? state[n % 2][q] : tslot(n, q);
+            if (cudaMemcpy2DAsync(outs[q], d.ld * sizeof(T), from, lp * sizeof(T), d.NY * sizeof(T), d.NX,
                                   cudaMemcpyDeviceToDevice, st) != cudaSuccess)
                 return VERIS_ERR_LAUNCH;
+        }
         return VERIS_OK;
     }
     if constexpr (sizeof(T) == 4) {

@@ -152,6 +152,10 @@ struct FastIO {
     const T *u, *v, *s1, *s2, *s12;   // state at the start of the subcycle (internal pitch)
     T *uo, *vo, *s1o, *s2o, *s12o;    // state at its end
     int64_t ldo;                      // pitch of the outputs
+    // float64 tapes (pitch ldo, C points; all three or none): Delta and
+    // zeta of the subcycle's viscosities and its ocean-drag coefficient,
+    // which the adjoint reads instead of recomputing
+    T *tDel = nullptr, *tZeta = nullptr, *tCd = nullptr;
 };
 
 int fast_support(const VerisParams &p);

@@ -33,6 +33,7 @@
 //   latency), the launch ending on a round of small units so that the SMs
 //   run out of work together.
 #include "evp_fast.cuh"
+#include "f64math.cuh"
 
 namespace veris {
 
@@ -71,76 +72,6 @@ static F64Scalars f64_scalars(const FastScalars<double> &k) {
     return s;
 }
 
-// --------------------------------------------- division and square root
-__device__ __forceinline__ double rcp_seed(double b) {
-    double r;
-    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(b));
-    return r;
-}
-
-__device__ __forceinline__ double rsqrt_seed(double x) {
-    double r;
-    asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
-    return r;
-}
-
-// positive, normal, and at least 2^64 away from both ends of the exponent
-// range (so neither the seed nor its square flushes or overflows)
-__device__ __forceinline__ bool seed_range(double b) {
-    const int hi = __double2hiint(b);
-    return hi >= (64 << 20) && hi < (1984 << 20);
-}
-
-// the bits of x through a move the compiler cannot fold back into a float
-// comparison (which would run on the float64 pipe)
-__device__ __forceinline__ unsigned long long bits_of(double x) {
-    unsigned long long b;
-    asm("mov.b64 %0, %1;" : "=l"(b) : "d"(x));
-    return b;
-}
-
-__device__ __forceinline__ bool is_zero(double x) { return (bits_of(x) << 1) == 0; }
-
-// a / b for b in seed_range: r0 ~ 1/b, e = 1 - b*r0, 1/b = r0*(1 + e + e^2 + O(e^3))
-__device__ __forceinline__ double div_series(double a, double b) {
-    const double r0 = rcp_seed(b);
-    const double e = fma(-b, r0, 1.0);
-    return a * fma(r0, fma(e, e, e), r0);
-}
-
-// sqrt(x) for x in seed_range: y ~ x^(-1/2), s0 = x*y, r = 1 - s0*y,
-// sqrt(x) = s0*(1 - r)^(-1/2) = s0*(1 + r/2 + 3r^2/8 + O(r^3))
-__device__ __forceinline__ double sqrt_series(double x) {
-    const double y = rsqrt_seed(x);
-    const double s0 = x * y;
-    const double r = fma(-s0, y, 1.0);
-    return fma(s0, r * fma(0.375, r, 0.5), s0);
-}
-
-// a / b on the lanes of `m` (all of which call it); IEEE division for the
-// whole warp when any b leaves the seed range (zero, denormal, negative,
-// huge, NaN)
-__device__ __forceinline__ double div64(double a, double b, unsigned m) {
-    if (__all_sync(m, seed_range(b))) return div_series(a, b);
-    return a / b;
-}
-
-// sqrt(x), x >= 0 or -0, on the lanes of `m`
-__device__ __forceinline__ double sqrt64(double x, unsigned m) {
-    const bool z = is_zero(x);
-    if (__all_sync(m, z || seed_range(x))) {
-        const double s = sqrt_series(z ? 1.0 : x);
-        return z ? 0.0 : s;
-    }
-    return sqrt(x);
-}
-
-// x > y for x, y >= 0 (or -0); false when x is NaN, as the float comparison
-__device__ __forceinline__ bool gt_nonneg(double x, double y) {
-    const long long a = (long long)bits_of(x), b = (long long)bits_of(y);
-    return a > b && a <= 0x7ff0000000000000LL;
-}
-
 // ------------------------------------------------------------------ tile
 constexpr int F64_THREADS = 256;
 
@@ -172,7 +103,7 @@ struct F64Units {
     int P1, R1, P2, U1;
 };
 
-template <int TI, bool BASAL, bool TURN>
+template <int TI, bool BASAL, bool TURN, bool TAPE>
 __global__ void __launch_bounds__(F64_THREADS, f64_min_blocks(TI))
 evp_f64_kernel(Dims d, int64_t lp, HaloFill h, FastConsts<double> c, F64Scalars k, FastIO<double> io,
                F64Units w) {
@@ -273,7 +204,8 @@ evp_f64_kernel(Dims d, int64_t lp, HaloFill h, FastConsts<double> c, F64Scalars 
         const double ep = e11 + e22, em = e11 - e22;
         const double Ph = __ldg(c.Ph + o);
         double zeta = 0.0, delta = 0.0;
-        if (__any_sync(m, !is_zero(Ph))) {
+        // (a taped subcycle keeps Delta where zeta = 0 too: the adjoint needs it)
+        if (TAPE || __any_sync(m, !is_zero(Ph))) {
             const double zs =
                 (sZq[IZ(li, lj)] + sZq[IZ(li + 1, lj)]) + (sZq[IZ(li, lj + 1)] + sZq[IZ(li + 1, lj + 1)]);
             // Delta^2 = ep^2 + (em^2 + 4 * 0.25/rA * sum rAz e12^2) / e^2
@@ -293,7 +225,8 @@ evp_f64_kernel(Dims d, int64_t lp, HaloFill h, FastConsts<double> c, F64Scalars 
             const double s2 = mC ? fma(__ldg(io.s2 + o), k.am1r, zh * em) : 0.0;
             sS11[q] = (s1 + s2) * __ldg(c.dyVh_y + gj);
             sS22[q] = (s1 - s2) * __ldg(c.dxUh_x + gi);
-            if (li >= 0 && lj >= 0 && i0 + li < d.NX && j0 + lj < d.NY) {
+            const bool own = li >= 0 && lj >= 0 && i0 + li < d.NX && j0 + lj < d.NY;
+            if (own) {
                 const int64_t w = (int64_t)gi * io.ldo + gj;
                 io.s1o[w] = s1;
                 io.s2o[w] = s2;
@@ -315,6 +248,12 @@ evp_f64_kernel(Dims d, int64_t lp, HaloFill h, FastConsts<double> c, F64Scalars 
                 if (fast) cd = (south ? k.dchS : k.dchN) * sx;
             }
             sCd[q] = mC ? cd : 0.0;
+            if (TAPE && own) {
+                const int64_t w = (int64_t)gi * io.ldo + gj;
+                io.tDel[w] = delta;
+                io.tZeta[w] = zeta;
+                io.tCd[w] = mC ? cd : 0.0;
+            }
             if (BASAL) {   // veris/dynamics_routines.py:55-96 with the step factor folded by the prep
                 const double a_ = (f0 & F_INU) ? u0 : 0.0, b_ = (fe & F_INU) ? ue : 0.0;
                 const double c_ = (f0 & F_INV) ? v0 : 0.0, e_ = (fn & F_INV) ? vn : 0.0;
@@ -439,11 +378,11 @@ static F64Units f64_units(const Dims &d, int TI, int slots) {
     return w;
 }
 
-template <int TI, bool B, bool R>
+template <int TI, bool B, bool R, bool TP>
 static int launch64(const Dims &d, int64_t lp, const HaloFill &h, const FastConsts<double> &c, const F64Scalars &k,
                     const FastIO<double> &io, cudaStream_t st) {
     using S = Smem64<TI>;
-    auto kern = evp_f64_kernel<TI, B, R>;
+    auto kern = evp_f64_kernel<TI, B, R, TP>;
     const size_t sm = S::bytes(B);
     static std::atomic<bool> configured[MAX_DEVICES];
     if (!smem_configured(configured, kern, (int)sm)) return VERIS_ERR_LAUNCH;
@@ -466,12 +405,21 @@ static int launch64(const Dims &d, int64_t lp, const HaloFill &h, const FastCons
     return launch_status();
 }
 
+// a taped subcycle (io.tDel set) also writes Delta, zeta and cDrag
+template <int TI, bool B, bool R>
+static int launch64_tape(const Dims &d, int64_t lp, const HaloFill &h, const FastConsts<double> &c,
+                         const F64Scalars &k, const FastIO<double> &io, cudaStream_t st) {
+    return io.tDel ? launch64<TI, B, R, true>(d, lp, h, c, k, io, st) : launch64<TI, B, R, false>(d, lp, h, c, k, io, st);
+}
+
 template <int TI>
 static int launch64_rows(const Dims &d, int64_t lp, const HaloFill &h, const FastConsts<double> &c,
                          const F64Scalars &k, const FastIO<double> &io, bool basal, bool turn, cudaStream_t st) {
     if (basal)
-        return turn ? launch64<TI, true, true>(d, lp, h, c, k, io, st) : launch64<TI, true, false>(d, lp, h, c, k, io, st);
-    return turn ? launch64<TI, false, true>(d, lp, h, c, k, io, st) : launch64<TI, false, false>(d, lp, h, c, k, io, st);
+        return turn ? launch64_tape<TI, true, true>(d, lp, h, c, k, io, st)
+                    : launch64_tape<TI, true, false>(d, lp, h, c, k, io, st);
+    return turn ? launch64_tape<TI, false, true>(d, lp, h, c, k, io, st)
+                : launch64_tape<TI, false, false>(d, lp, h, c, k, io, st);
 }
 
 // rows per tile of later float64 subcycles (0: the default); process-wide
