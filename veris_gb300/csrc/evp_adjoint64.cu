@@ -49,11 +49,11 @@ constexpr int BX = 32, BY = 8;   // 32 points along j (contiguous) x 8 rows per 
 struct K64 {
     double bU, bU1;            // beta/dt, (beta + 1)/dt
     double hc, sinH;           // 0.5 cos(turning angle), 0.5 sin(turning angle)
-    double am1, ra;            // (alpha - 1)/alpha, 1/alpha
-    double kp, rsq, dmin;      // press factor, 1/e^2, Delta_min
+    double am1, ra2, rah;      // (alpha - 1)/alpha, 2/alpha, 0.5/alpha
+    double hkp, rsq, dmin;     // half the press factor, 1/e^2, Delta_min
     double nh1, nh2, nh3, nh4; // 0.5/alpha/n: sigma12's average over n wet C points
     double dcq2N, dcq2S, cmin2;   // the drag test (as the float64 forward takes it)
-    double kXN, kXS;           // 0.5 (0.5 rhoSea drag)^2: d cDrag/dX = kX / cDrag
+    double kXN, kXS;           // (rhoSea drag)^2 / 4: 2 d cDrag/dX = kX / cDrag
     double wN, wS;             // rhoSea / (rhoSea drag): d cDrag / d drag = cDrag * w
     double U02;                // basal U0^2
 };
@@ -65,8 +65,9 @@ K64 k64(const FastScalars<double> &k, double rhoSea) {
     s.hc = k.halfCos;
     s.sinH = 0.5 * k.sinW;
     s.am1 = k.alpha_m1 * k.ralpha;
-    s.ra = k.ralpha;
-    s.kp = k.kp;
+    s.ra2 = 2.0 * k.ralpha;
+    s.rah = 0.5 * k.ralpha;
+    s.hkp = 0.5 * k.kp;
     s.rsq = k.rsq;
     s.dmin = k.deltaMin;
     s.nh1 = 0.5 * k.ralpha;
@@ -76,8 +77,8 @@ K64 k64(const FastScalars<double> &k, double rhoSea) {
     s.dcq2N = 0.25 * k.dN2;
     s.dcq2S = 0.25 * k.dS2;
     s.cmin2 = k.cmin2;
-    s.kXN = 0.5 * (0.25 * k.dN2);
-    s.kXS = 0.5 * (0.25 * k.dS2);
+    s.kXN = 0.25 * k.dN2;
+    s.kXS = 0.25 * k.dS2;
     s.wN = k.dN != 0.0 ? rhoSea / k.dN : 0.0;
     s.wS = k.dS != 0.0 ? rhoSea / k.dS : 0.0;
     s.U02 = k.U02;
@@ -95,11 +96,11 @@ struct Scr {
     double *q0V, *qsV;     // the same for v: (i, j),(i+1, j) and (i, j-1),(i+1, j-1)
     double *tZ;            // a Z point's share in the adjoint of each neighbouring zeta
     double *le12;          // e12's adjoint through sigma12
-    double *e2;            // 2 rAz e12
+    double *e2;            // rAz e12
     double *uA, *uB;       // a C point's share in d/du of U(i, j) and U(i+1, j)
     double *vA, *vB;       // the same for V(i, j) and V(i, j+1)
     double *ldu, *ldv;     // ocean-drag shares in d/du, d/dv (masked by the U/V point)
-    double *wC;            // 4 rsq qrA dL/d(Delta^2): e12^2's adjoint
+    double *wC;            // recip_rA/e^2 dL/dDelta / Delta: twice the adjoint of rAz e12^2
     double *lsb;           // basal shares, times u or v at the U/V point
     double *cb;            // the basal coefficient (recomputed once per subcycle)
 };
@@ -190,26 +191,33 @@ __global__ void __launch_bounds__(BX * BY) uv_reverse_kernel(Dims d, int64_t lp,
     }
     double sg = 0.0;
     if (TURN) sg = (f0 & F_SPOS) ? 1.0 : ((f0 & F_SNEG) ? -1.0 : 0.0);
-    {   // U point
-        const double AW = c.AW[o], MU = c.mU[o], uo = c.uOc[o], u0 = t.u[o];
-        const double S = cd0 + cdw, hA = k.hc * AW, kU = hA * S;
-        double den = fma(MU, k.bU1, kU);
-        if (BASAL) den = fma(0.5 * AW, cb0 + cbw, den);
+    if (!__any_sync(m, f0 & F_MU)) {   // a warp of dry U points: no momentum adjoint, nothing to add
+        l.ou[o] = 0.0;
+        s.gU[o] = 0.0;
+        s.rU[o] = 0.0;
+        s.wU0[o] = 0.0;
+        if (TURN) s.wU1[o] = s.q0U[o] = s.qwU[o] = 0.0;
+        if (BASAL) s.bU[o] = 0.0;
+    } else {   // U point (hAW = cos/2 AW, mUb = mU beta/dt, mUb1 = mU (beta+1)/dt folded by the prep)
+        const double hA = c.hAW[o], uo = c.uOc[o], u0 = t.u[o];
+        const double S = cd0 + cdw, kU = hA * S;
+        double den = c.mUb1[o] + kU;
+        if (BASAL) den = fma(0.5 * c.AW[o], cb0 + cbw, den);
         const bool guard = is_zero(den);
         const double r = rcp64(guard ? 1.0 : den, m);
         const double g = sel(f0 & F_MU, LU * r);
         const double lden = guard ? 0.0 : -t.un[o] * g;
         const double Y = fma(uo, g, lden);   // d/dkU
         const double W = hA * Y;
-        l.ou[o] = (MU * k.bU) * g;
-        a.mU[o] += fma(k.bU * u0, g, k.bU1 * lden);
+        l.ou[o] = c.mUb[o] * g;
+        a.mU[o] = fma(k.bU * u0, g, fma(k.bU1, lden, a.mU[o]));
         a.cU[o] += g;
-        double lAW = k.hc * S * Y;
+        double lAW = fma(k.hc * S, Y, a.AW[o]);
         if (BASAL) {
             lAW = fma(0.5 * (cb0 + cbw), lden, lAW);
-            s.bU[o] = 0.5 * AW * lden;
+            s.bU[o] = 0.5 * c.AW[o] * lden;
         }
-        a.uOc[o] += kU * g;
+        a.uOc[o] = fma(kU, g, a.uOc[o]);
         s.gU[o] = g;
         s.rU[o] = c.rrAu[o] * g;
         if (TURN) {
@@ -220,7 +228,7 @@ __global__ void __launch_bounds__(BX * BY) uv_reverse_kernel(Dims d, int64_t lp,
             const double pn = 0.5 * ((uo - u0) + (c.uOc[on] - t.u[on]));
             const double pw = 0.5 * ((c.uOc[ow] - t.u[ow]) + (c.uOc[own_] - t.u[own_]));
             lAW = fma(tu * fma(cd0, pn, cdw * pw), g, lAW);
-            const double tg = tu * AW * g;
+            const double tg = tu * c.AW[o] * g;
             s.wU0[o] = fma(tg, pn, W);
             s.wU1[o] = fma(tg, pw, W);
             s.q0U[o] = 0.5 * tg * cd0;
@@ -228,28 +236,35 @@ __global__ void __launch_bounds__(BX * BY) uv_reverse_kernel(Dims d, int64_t lp,
         } else {
             s.wU0[o] = W;
         }
-        a.AW[o] += lAW;
+        a.AW[o] = lAW;
     }
-    {   // V point
-        const double AS = c.AS[o], MV = c.mV[o], vo = c.vOc[o], v0 = t.v[o];
-        const double S = cd0 + cds, hA = k.hc * AS, kV = hA * S;
-        double den = fma(MV, k.bU1, kV);
-        if (BASAL) den = fma(0.5 * AS, cb0 + cbs, den);
+    if (!__any_sync(m, f0 & F_MV)) {
+        l.ov[o] = 0.0;
+        s.gV[o] = 0.0;
+        s.rV[o] = 0.0;
+        s.wV0[o] = 0.0;
+        if (TURN) s.wV1[o] = s.q0V[o] = s.qsV[o] = 0.0;
+        if (BASAL) s.bV[o] = 0.0;
+    } else {   // V point
+        const double hA = c.hAS[o], vo = c.vOc[o], v0 = t.v[o];
+        const double S = cd0 + cds, kV = hA * S;
+        double den = c.mVb1[o] + kV;
+        if (BASAL) den = fma(0.5 * c.AS[o], cb0 + cbs, den);
         const bool guard = is_zero(den);
         const double r = rcp64(guard ? 1.0 : den, m);
         const double g = sel(f0 & F_MV, LV * r);
         const double lden = guard ? 0.0 : -t.vn[o] * g;
         const double Y = fma(vo, g, lden);
         const double W = hA * Y;
-        l.ov[o] = (MV * k.bU) * g;
-        a.mV[o] += fma(k.bU * v0, g, k.bU1 * lden);
+        l.ov[o] = c.mVb[o] * g;
+        a.mV[o] = fma(k.bU * v0, g, fma(k.bU1, lden, a.mV[o]));
         a.cV[o] += g;
-        double lAS = k.hc * S * Y;
+        double lAS = fma(k.hc * S, Y, a.AS[o]);
         if (BASAL) {
             lAS = fma(0.5 * (cb0 + cbs), lden, lAS);
-            s.bV[o] = 0.5 * AS * lden;
+            s.bV[o] = 0.5 * c.AS[o] * lden;
         }
-        a.vOc[o] += kV * g;
+        a.vOc[o] = fma(kV, g, a.vOc[o]);
         s.gV[o] = g;
         s.rV[o] = c.rrAv[o] * g;
         if (TURN) {
@@ -260,7 +275,7 @@ __global__ void __launch_bounds__(BX * BY) uv_reverse_kernel(Dims d, int64_t lp,
             const double pe = 0.5 * ((vo - v0) + (c.vOc[oe] - t.v[oe]));
             const double ps = 0.5 * ((c.vOc[os] - t.v[os]) + (c.vOc[ose] - t.v[ose]));
             lAS = fma(tv * fma(cd0, pe, cds * ps), g, lAS);
-            const double tg = tv * AS * g;
+            const double tg = tv * c.AS[o] * g;
             s.wV0[o] = fma(tg, pe, W);
             s.wV1[o] = fma(tg, ps, W);
             s.q0V[o] = 0.5 * tg * cd0;
@@ -268,7 +283,7 @@ __global__ void __launch_bounds__(BX * BY) uv_reverse_kernel(Dims d, int64_t lp,
         } else {
             s.wV0[o] = W;
         }
-        a.AS[o] += lAS;
+        a.AS[o] = lAS;
     }
 }
 
@@ -317,7 +332,7 @@ __global__ void __launch_bounds__(BX * BY) z_reverse_kernel(Dims d, int64_t lp, 
     const double cz = nh * L;
     s.tZ[o] = cz * e;
     s.le12[o] = cz * zs;
-    s.e2[o] = 2.0 * c.rAz[o] * e;
+    s.e2[o] = c.rAz[o] * e;
 }
 
 // ------------------------------------------------------------------ P3
@@ -339,50 +354,57 @@ __global__ void __launch_bounds__(BX * BY) c_reverse_kernel(Dims d, int64_t lp, 
         const uint32_t f0 = c.flags[o], fe = c.flags[oe], fn = c.flags[on];
         const bool mC = f0 & F_MC, inC = f0 & F_INC;
         // shares gathered from U(i, j), U(i+1, j), V(i, j), V(i, j+1)
-        const double gU0 = s.gU[o], gUe = s.gU[oe], gV0 = s.gV[o], gVn = s.gV[on];
+        const double sU = s.gU[o] + s.gU[oe], sV = s.gV[o] + s.gV[on];
         const double lcd = (s.wU0[o] + (TURN ? s.wU1[oe] : s.wU0[oe])) + (s.wV0[o] + (TURN ? s.wV1[on] : s.wV0[on]));
-        const double ls11 = c.dyV_y[j] * (s.rU[o] - s.rU[oe]);
-        const double ls22 = c.dxU_x[i] * (s.rV[o] - s.rV[on]);
-        const double L1 = fma(0.5, ls11 + ls22, l.ls1[(int64_t)i * l.ldl + j]);
-        const double L2 = fma(0.5, ls11 - ls22, l.ls2[(int64_t)i * l.ldl + j]);
+        // sig11 = (sigma1' + sigma2')/2 enters U(i, j) (+) and U(i+1, j) (-) as rrAu dyV,
+        // sig22 = (sigma1' - sigma2')/2 V(i, j) (+) and V(i, j+1) (-) as rrAv dxU
+        const double h11 = c.dyVh_y[j] * (s.rU[o] - s.rU[oe]);
+        const double h22 = c.dxUh_x[i] * (s.rV[o] - s.rV[on]);
+        const double L1 = l.ls1[(int64_t)i * l.ldl + j] + (h11 + h22);
+        const double L2 = l.ls2[(int64_t)i * l.ldl + j] + (h11 - h22);
         l.os1[o] = sel(mC, k.am1 * L1);
         l.os2[o] = sel(mC, k.am1 * L2);
-        const double g1 = sel(mC, k.ra * L1), g2 = sel(mC, k.ra * L2);
-        // strain rates (forward recomputed from the tape's velocities)
+        // sigma1' = mC ((alpha-1)/alpha sigma1 + zeta (2 ep - kp Delta)/alpha),
+        // sigma2' = mC ((alpha-1)/alpha sigma2 + zeta em/(2 alpha)): h1 = 2 d/dsigma1'/alpha, h2 = d/dsigma2'/(2 alpha)
+        const double h1 = sel(mC, k.ra2 * L1), h2 = sel(mC, k.rah * L2);
+        // strain rates (recomputed from the tape's velocities)
         const double u0 = t.u[o], ue = t.u[oe], v0 = t.v[o], vn = t.v[on];
         const double rdx = c.rdxU_x[i], rdy = c.rdyV_y[j];
         const double e11 = inC ? (ue - u0) * rdx : 0.0;
         const double e22 = inC ? (vn - v0) * rdy : 0.0;
         const double ep = e11 + e22, em = e11 - e22;
         const double del = t.del[o], zeta = t.zeta[o];
-        // sigma1' = mC ((alpha-1)/alpha sigma1 + zeta (2 ep - kp Delta)/alpha),
-        // sigma2' = mC ((alpha-1)/alpha sigma2 + zeta em/(2 alpha))
         const double tz = (s.tZ[o] + s.tZ[oe]) + (s.tZ[on] + s.tZ[oen]);
-        const double lz = fma(fma(2.0, ep, -k.kp * del), g1, fma(0.5 * em, g2, tz));
-        double lep = 2.0 * zeta * g1, lem = 0.5 * zeta * g2;
+        const double lz = fma(fma(-k.hkp, del, ep), h1, fma(em, h2, tz));
         // zeta = Ph/(Delta + Delta_min)
         const double rz = rcp64(del + k.dmin, m);
-        a.Ph[o] += lz * rz;
-        const double ldel = fma(-zeta * rz, lz, -k.kp * zeta * g1);
-        // Delta = sqrt(ep^2 + rsq em^2 + (recip_rA/e^2) sum rAz e12^2); 0 at Delta = 0
-        const bool dz = is_zero(del);
-        const double rdel = rcp64(dz ? 1.0 : del, m);
-        const double ld2 = dz ? 0.0 : 0.5 * ldel * rdel;
-        lep = fma(2.0 * ep, ld2, lep);
-        lem = fma(2.0 * k.rsq * em, ld2, lem);
-        s.wC[o] = c.rsqrA[o] * ld2;
-        const double le11 = inC ? (lep + lem) * rdx : 0.0;
-        const double le22 = inC ? (lep - lem) * rdy : 0.0;
-        // Coriolis: Fv = mfC (v + v_n) enters U(i, j), U(i+1, j) with 1/2; Fu = mfC (u + u_e) V(i, j), V(i, j+1) with -1/2
-        const double lFv = 0.5 * (gU0 + gUe), lFu = -0.5 * (gV0 + gVn);
-        const double mf = c.mfC[o];
-        a.mfC[o] += fma(v0 + vn, lFv, (u0 + ue) * lFu);
-        const double fu = mf * lFu, fv = mf * lFv;
+        a.Ph[o] = fma(lz, rz, a.Ph[o]);
+        // where the ice strength is 0, zeta = 0 and nothing flows back through Delta
+        double q = 0.0, le11 = 0.0, le22 = 0.0;
+        if (__any_sync(m, !is_zero(zeta))) {
+            double lep = zeta * h1, lem = zeta * h2;
+            const double ldel = fma(-zeta * rz, lz, -k.hkp * lep);
+            // Delta = sqrt(ep^2 + rsq em^2 + (recip_rA/e^2) sum rAz e12^2); 0 at Delta = 0.  q = 2 dL/dDelta^2
+            const bool dz = is_zero(del);
+            const double rdel = rcp64(dz ? 1.0 : del, m);
+            q = dz ? 0.0 : ldel * rdel;
+            lep = fma(ep, q, lep);
+            lem = fma(k.rsq * em, q, lem);
+            le11 = inC ? (lep + lem) * rdx : 0.0;
+            le22 = inC ? (lep - lem) * rdy : 0.0;
+        }
+        s.wC[o] = c.rsqrA[o] * q;
+        // Coriolis: Fv = mfC (v + v_n) enters U(i, j), U(i+1, j) with 1/2, Fu = mfC (u + u_e)
+        // V(i, j), V(i, j+1) with -1/2 (mf4 = mfC/2)
+        const double mf = c.mf4[o];
+        a.mfC[o] = fma(0.5, fma(v0 + vn, sU, -((u0 + ue) * sV)), a.mfC[o]);
+        const double fv = mf * sU, fu = -mf * sV;
         s.uA[o] = fu - le11;
         s.uB[o] = fu + le11;
         s.vA[o] = fv - le22;
         s.vB[o] = fv + le22;
         // ocean drag: cd = 0.5 rhoSea drag sqrt(X), X = (du + du_e)^2 + (dv + dv_n)^2, above its floor
+        // (the branch taken exactly as the forward takes it)
         const double du0 = (f0 & F_INU) ? u0 - c.uOc[o] : 0.0;
         const double du1 = (fe & F_INU) ? ue - c.uOc[oe] : 0.0;
         const double dv0 = (f0 & F_INV) ? v0 - c.vOc[o] : 0.0;
@@ -391,18 +413,17 @@ __global__ void __launch_bounds__(BX * BY) c_reverse_kernel(Dims d, int64_t lp, 
         const double X = fma(B, B, A * A);
         const bool south = f0 & F_SOUTH;
         const bool fast = mC && gt_nonneg((south ? k.dcq2S : k.dcq2N) * X, k.cmin2);
-        const double cd = t.cd[o];
-        double lX = 0.0;
+        double lX2 = 0.0;   // 2 dL/dX
         if (__any_sync(m, fast)) {
+            const double cd = t.cd[o];
             const double rc = rcp64(fast ? cd : 1.0, m);
             if (fast) {
-                lX = lcd * (south ? k.kXS : k.kXN) * rc;
-                const double lw = lcd * cd * (south ? k.wS : k.wN);
-                if (south) dragS = lw; else dragN = lw;
+                lX2 = lcd * (south ? k.kXS : k.kXN) * rc;
+                if (south) dragS = lcd * cd; else dragN = lcd * cd;
             }
         }
-        s.ldu[o] = 2.0 * A * lX;
-        s.ldv[o] = 2.0 * B * lX;
+        s.ldu[o] = A * lX2;
+        s.ldv[o] = B * lX2;
         if (BASAL) {
             // cb = bfac / sqrt(0.25 (a^2 + b^2 + c^2 + e^2) + U0^2), a = inU u, b = inU_e u_e, c = inV v, e = inV_n v_n
             const double lcb = (s.bU[o] + s.bU[oe]) + (s.bV[o] + s.bV[on]);
@@ -421,9 +442,9 @@ __global__ void __launch_bounds__(BX * BY) c_reverse_kernel(Dims d, int64_t lp, 
         dragN += __shfl_down_sync(ALL, dragN, off);
         dragS += __shfl_down_sync(ALL, dragS, off);
     }
-    if ((threadIdx.x & 31) == 0) {
-        if (dragN != 0.0) atomicAdd(a.dragN, dragN);
-        if (dragS != 0.0) atomicAdd(a.dragS, dragS);
+    if ((threadIdx.x & 31) == 0) {   // d cDrag / d drag = cDrag rhoSea / (rhoSea drag)
+        if (dragN != 0.0) atomicAdd(a.dragN, dragN * k.wN);
+        if (dragS != 0.0) atomicAdd(a.dragS, dragS * k.wS);
     }
 }
 
@@ -434,10 +455,13 @@ __device__ __forceinline__ double le12_at(const Scr &s, int64_t o, int64_t ow, i
     return fma(s.e2[o], (s.wC[o] + s.wC[ow]) + (s.wC[os] + s.wC[ows]), s.le12[o]);
 }
 
-// d e12(Z) / d u at the Z point's own U point (sign +1) and at its southern
-// one (sign -1), in units of 0.5 rdyU: 2 hU + (sign) mz
+// d e12(Z) / d u (or v) in units of 0.5 rdyU (0.5 rdxV): 2 h + sign mz at
+// the Z point's own U (V) point (sign +1) and at its southern (western) one
+// (sign -1), h = iceMaskU - its southern neighbour (iceMaskV - its western
+// one); a small integer, selected rather than converted
 __device__ __forceinline__ double e12_coef(bool mz, int h, int sign) {
-    return (double)(2 * h + (mz ? sign : 0));
+    const int v = 2 * h + (mz ? sign : 0);
+    return v == 0 ? 0.0 : v == 1 ? 1.0 : v == -1 ? -1.0 : v == 2 ? 2.0 : v == -2 ? -2.0 : v == 3 ? 3.0 : -3.0;
 }
 
 // ------------------------------------------------------------------ P4
@@ -449,6 +473,7 @@ __global__ void __launch_bounds__(BX * BY) uv_gather_kernel(Dims d, int64_t lp, 
                                                              Lam64 l, Adj<double> a, Scr s) {
     const int j = blockIdx.x * BX + threadIdx.x, i = blockIdx.y * BY + threadIdx.y;
     const bool act = i < d.NX && j < d.NY;
+    const unsigned m = __ballot_sync(ALL, act);
     if (!act) return;
     const int iw = wxp(d, i - 1), ie = wxp(d, i + 1), js = wyp(d, j - 1), jn = wyp(d, j + 1);
     const int64_t o = (int64_t)i * lp + j, ow = (int64_t)iw * lp + j, oe = (int64_t)ie * lp + j,
@@ -466,8 +491,16 @@ __global__ void __launch_bounds__(BX * BY) uv_gather_kernel(Dims d, int64_t lp, 
     const int hV0 = (int)((f0 & F_MV) != 0) - (int)((fw & F_MV) != 0);
     const int hVe = (int)((fe & F_MV) != 0) - (int)((f0 & F_MV) != 0);
     const bool mz0 = z_wet(f0, fw, fs, fws), mzn = z_wet(fn, fwn, f0, fw), mze = z_wet(fe, f0, fes, fs);
-    double lu = fma(z0 * c.rdyUh_y[j], e12_coef(mz0, hU0, 1), zn * c.rdyUh_y[jn] * e12_coef(mzn, hUn, -1));
-    double lv = fma(z0 * c.rdxVh_x[i], e12_coef(mz0, hV0, 1), ze * c.rdxVh_x[ie] * e12_coef(mze, hVe, -1));
+    const double ru0 = z0 * c.rdyUh_y[j], run = zn * c.rdyUh_y[jn];
+    const double rv0 = z0 * c.rdxVh_x[i], rve = ze * c.rdxVh_x[ie];
+    double lu, lv;
+    if (__any_sync(m, (hU0 | hUn | hV0 | hVe) != 0)) {   // no-slip boundary terms in this warp
+        lu = fma(ru0, e12_coef(mz0, hU0, 1), run * e12_coef(mzn, hUn, -1));
+        lv = fma(rv0, e12_coef(mz0, hV0, 1), rve * e12_coef(mze, hVe, -1));
+    } else {
+        lu = sel(mz0, ru0) - sel(mzn, run);
+        lv = sel(mz0, rv0) - sel(mze, rve);
+    }
     // strain rates and Coriolis (C(i, j) and C(i-1, j) for u; C(i, j), C(i, j-1) for v)
     lu += s.uA[o] + s.uB[ow];
     lv += s.vA[o] + s.vB[os];

@@ -205,13 +205,14 @@ evp_f64_kernel(Dims d, int64_t lp, HaloFill h, FastConsts<double> c, F64Scalars 
         const double Ph = __ldg(c.Ph + o);
         double zeta = 0.0, delta = 0.0;
         // (a taped subcycle keeps Delta where zeta = 0 too: the adjoint needs it)
-        if (TAPE || __any_sync(m, !is_zero(Ph))) {
+        const bool strong = __any_sync(m, !is_zero(Ph));
+        if (TAPE || strong) {
             const double zs =
                 (sZq[IZ(li, lj)] + sZq[IZ(li + 1, lj)]) + (sZq[IZ(li, lj + 1)] + sZq[IZ(li + 1, lj + 1)]);
             // Delta^2 = ep^2 + (em^2 + 4 * 0.25/rA * sum rAz e12^2) / e^2
             const double d2 = fma(__ldg(c.rsqrA + o), zs, fma(k.rsq * em, em, ep * ep));
             delta = sqrt64(d2, m);
-            zeta = div64(Ph, delta + k.deltaMin, m);
+            if (strong) zeta = div64(Ph, delta + k.deltaMin, m);
         }
         sZeta[idx] = zeta;
         const bool in2 = li < ti && lj < S::TJ;
