@@ -84,6 +84,8 @@ def parse():
                     help="float32 EVP kernel: register-walking warps or TMA-staged tiles")
     ap.add_argument("--walk-rows", type=int, default=0, help="rows per walk (0: from the grid and the SM count)")
     ap.add_argument("--walk-variant", type=int, default=-1, help="-1: tuned on the workload")
+    ap.add_argument("--walk-persistent", type=int, default=-1, choices=(-1, 0, 1),
+                    help="float32 walk subcycles per launch: 0 one, 1 all but the last (-1: tuned)")
     ap.add_argument("--f64-tile-rows", type=int, default=-1, choices=(-1, 0, 16, 24, 32),
                     help="rows per tile of the float64 subcycle kernel (0: the library's default; "
                          "-1: tuned on the workload)")
@@ -401,10 +403,13 @@ def make_engine(arrays, sett, dev, precision, args, walk_variant=None, budgets=F
     eng = SeaIceStep(state, precision=precision, evp=args.evp, f32_kernel=args.f32_kernel,
                      walk_rows=args.walk_rows, walk_variant=wv, budgets=budgets)
     tuning = None
-    if (precision == "f32" and eng.f32_kernel == "walk" and eng.evp_form == "fast" and walk_variant is None
-            and args.walk_variant < 0):
-        from veris_gb300.autotune import tune_walk
-        tuning = tune_walk(eng)
+    persist = (0, 1) if args.walk_persistent < 0 else (args.walk_persistent,)
+    if precision == "f32" and eng.f32_kernel == "walk" and eng.evp_form == "fast":
+        if walk_variant is None and args.walk_variant < 0:
+            from veris_gb300.autotune import tune_walk
+            tuning = tune_walk(eng, persistent=persist)
+        elif args.walk_persistent >= 0:
+            eng.lib.veris_evp_walk_persistent(args.walk_persistent)
     if precision == "f64" and eng.evp_form == "fast" and args.f64_tile_rows < 0 and tune:
         from veris_gb300.autotune import tune_f64_tile
         tuning = tune_f64_tile(eng)
@@ -612,7 +617,9 @@ def fp32_block(arrays, sett, dev, args, flush, ws, workload, cells, n_sub):
            "gpu_launches": eng.launches_per_step * args.steps,
            "roofline": roofline_hbm(evp_kernel_name(eng), workload, cells, us, "f32"),
            "evp_form": eng.evp_form, "f32_kernel": eng.f32_kernel,
-           "walk": {"rows": eng.walk_rows or "auto", "variant": eng.walk_variant, "tuning": tuning}}
+           "walk": {"rows": eng.walk_rows or "auto", "variant": eng.walk_variant,
+                    "persistent": bool(tuning["persistent"]) if tuning else args.walk_persistent == 1,
+                    "tuning": tuning}}
     if not args.no_e2e:
         out["e2e"] = e2e_of(eng, args, ws, cells, n_sub)
     wv = eng.walk_variant

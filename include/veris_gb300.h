@@ -310,13 +310,27 @@ int veris_evp_walk_solver_f32(const VerisGrid *g, const VerisParams *p, const Ve
                               int32_t n_subcycles, int32_t rows, int32_t variant, float *uIce,
                               float *vIce, float *sigma1, float *sigma2, float *sigma12,
                               void *workspace, size_t workspace_bytes, veris_stream_t s);
+/*
+ * Subcycles per launch of the register-walking float32 kernel (every float32
+ * walk solve with at least 3 subcycles): 0 = one launch per subcycle, 1 =
+ * all but the last subcycle in one persistent cooperative launch, each walk
+ * waiting only for the walks whose rows or columns its stencil shares
+ * (per-walk progress counters; a wait that gives up after about half a
+ * second sets status bit 1 and ends the launch), then the last subcycle as
+ * usual.  Falls back to one launch per subcycle when the walks cannot all
+ * be resident at once.  Process-wide, for every later launch; same values.
+ * VERIS_ERR_ARG for other values.  A tuning knob with no counterpart in the
+ * reference.
+ */
+int veris_evp_walk_persistent(int32_t on);
 int veris_evp_smem_solver_f32(const VerisGrid *g, const VerisParams *p, const VerisFieldsF64 *vs,
                               int32_t n_subcycles, float *uIce, float *vIce, float *sigma1,
                               float *sigma2, float *sigma12, void *workspace,
                               size_t workspace_bytes, veris_stream_t s);
 /*
  * Device status word of the last fast solve on this workspace (0 = clean;
- * bit 0: a bounded TMA wait gave up and the affected tiles were skipped).
+ * bit 0: a bounded TMA wait gave up and the affected tiles were skipped;
+ * bit 1: a persistent walk's bounded wait gave up and the launch ended).
  * Synchronises the stream.
  */
 int veris_evp_fast_status(const void *workspace, int32_t *status_host, veris_stream_t s);

@@ -427,3 +427,29 @@ def test_float64_tile_heights_give_the_same_values_and_the_tuner_picks_one():
         assert torch.equal(before, eng.state.variables.uIce)
     finally:
         lib.veris_evp_f64_tile_rows(0)
+
+
+@pytest.mark.parametrize("nx,ny,fill,n", ((300, 150, True, 25), (61, 33, True, 9), (120, 90, False, 14),
+                                          (1440, 720, True, 40)))
+def test_persistent_walk_gives_the_same_values(nx, ny, fill, n):
+    """Several float32 subcycles per persistent launch (each walk waiting on
+    its neighbours' progress counters) against one launch per subcycle: bit
+    for bit, for several walk lengths and compiled forms, with the cyclic
+    x-halo images (veros_fill) and with both halos refreshed."""
+    from veris_gb300 import _abi
+    from veris_gb300.evp_solver import evp_solver_fast
+    lib = _abi.load()
+    st = _prepared(nx, ny, nx + 7, veros_fill=fill)
+    try:
+        for rows, variant in ((0, 2), (16, 0), (0, 3)):
+            assert lib.veris_evp_walk_persistent(0) == 0
+            one = evp_solver_fast(st, "f32", "walk", n_subcycles=n, rows=rows, variant=variant)
+            assert lib.veris_evp_walk_persistent(1) == 0
+            many, status = evp_solver_fast(st, "f32", "walk", n_subcycles=n, rows=rows, variant=variant,
+                                           return_status=True)
+            assert status == 0, status
+            for k in range(5):
+                assert torch.equal(one[k], many[k]), (rows, variant, k)
+    finally:
+        lib.veris_evp_walk_persistent(0)
+    assert lib.veris_evp_walk_persistent(2) != 0

@@ -88,36 +88,45 @@ def tune(ens, candidates=DEFAULT_CANDIDATES, subcycles=10, repeats=3, use_cache=
     return dict(choice, trials=trials, cached=False)
 
 
-def tune_walk(eng, variants=(0, 1, 2, 3), subcycles=10, repeats=3):
-    """Pick the walking kernel's compiled register budget (variant) for a
-    float32 ``SeaIceStep`` by timing each on ``subcycles`` subcycles of the
-    engine's state (outputs go to scratch: the state is not advanced).  More
-    resident warps hide more latency but force shorter walks (all walks stay
-    in one wave), so the best budget depends on the grid."""
-    import ctypes
+def tune_walk(eng, variants=(0, 1, 2, 3), persistent=(0, 1), subcycles=10, repeats=3):
+    """Pick the walking kernel's compiled register budget (variant) and its
+    subcycles per launch (one, or all but the last in one persistent launch)
+    for a float32 ``SeaIceStep`` by timing each pair on ``subcycles``
+    subcycles of the engine's state (outputs go to scratch: the state is not
+    advanced).  More resident warps hide more latency but force shorter
+    walks (all walks stay in one wave), so the best budget depends on the
+    grid.  Sets the subcycles per launch process-wide
+    (veris_evp_walk_persistent) and drops the engine's captured graph."""
     from ._abi import check
     outs = [torch.empty(eng.shape, dtype=torch.float32, device=eng.device) for _ in range(5)]
     ptrs = [t.data_ptr() for t in outs]
     ws = (eng.ws_evp.data_ptr(), eng.ws_evp.numel(), eng.stream)
     r64 = eng._refs(eng.f64)
     trials = []
-    for v in variants:
-        run = lambda n: check("evp_walk_f32", eng.lib.veris_evp_walk_solver_f32(*r64, n, eng.walk_rows, v, *ptrs, *ws))
-        run(2)
-        times = []
-        for _ in range(repeats):
-            a = torch.cuda.Event(enable_timing=True)
-            b = torch.cuda.Event(enable_timing=True)
-            a.record()
-            run(subcycles)
-            b.record()
-            b.synchronize()
-            times.append(a.elapsed_time(b) / subcycles)
-        trials.append({"variant": v, "ms_per_subcycle": sorted(times)[len(times) // 2]})
+    try:
+        for p in persistent:
+            check("evp_walk_persistent", eng.lib.veris_evp_walk_persistent(p))
+            for v in variants:
+                run = lambda n: check("evp_walk_f32", eng.lib.veris_evp_walk_solver_f32(*r64, n, eng.walk_rows, v,
+                                                                                       *ptrs, *ws))
+                run(3)
+                times = []
+                for _ in range(repeats):
+                    a = torch.cuda.Event(enable_timing=True)
+                    b = torch.cuda.Event(enable_timing=True)
+                    a.record()
+                    run(subcycles)
+                    b.record()
+                    b.synchronize()
+                    times.append(a.elapsed_time(b) / subcycles)
+                trials.append({"variant": v, "persistent": bool(p), "ms_per_subcycle": sorted(times)[len(times) // 2]})
+    finally:
+        check("evp_walk_persistent", eng.lib.veris_evp_walk_persistent(0))
     best = min(trials, key=lambda t: t["ms_per_subcycle"])
     eng.walk_variant = best["variant"]
+    check("evp_walk_persistent", eng.lib.veris_evp_walk_persistent(int(best["persistent"])))
     eng.graph = None
-    return {"variant": best["variant"], "trials": trials}
+    return {"variant": best["variant"], "persistent": best["persistent"], "trials": trials}
 
 
 F64_TILE_ROWS = (16, 24, 32)

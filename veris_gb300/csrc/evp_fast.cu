@@ -348,8 +348,7 @@ static int evp_fast(const VerisGrid *g, const VerisParams *p, const VerisFieldsF
     if constexpr (sizeof(T) == 4) {
         if (allow_tma >= 4 || allow_tma < 0)   // register-walking kernel, allow_tma rows per walk (< 0: auto)
             return evp_walk_subcycles(adapt, paired, d, h, c, k, state, outs, d.ld, n, basal, turn,
-                                      allow_tma < 0 ? 0 : allow_tma,
-                                      walk_variant, st);
+                                      allow_tma < 0 ? 0 : allow_tma, walk_variant, st, false, status);
         if (allow_tma) {
             stt = evp_tma_subcycles(d, h, c, k, state, outs, d.ld, n, status, basal, turn, st);
             if (stt != VERIS_ERR_UNSUPPORTED) return stt;

@@ -33,7 +33,7 @@ enum : int {
 };
 
 // device status word bits (first word of the fast workspace)
-enum : int { S_TMA_TIMEOUT = 1 };
+enum : int { S_TMA_TIMEOUT = 1, S_WALK_TIMEOUT = 2 };
 
 template <class T>
 struct FastConsts {
@@ -58,6 +58,7 @@ struct FastConsts {
     T *qrA_y, *rAz_y, *rrAu_y, *rrAv_y;   // the register walk's cell areas (0.25/rA, rAz, 1/rAu, 1/rAv), along j
     T *pMUV;   // (mU, mV) pairs, pitch lp: the register walk's U/V masses when its areas are 1-D
     uint16_t *flags16;   // the flag word's 11 bits, pitch lp: the register walk's copy
+    int *wprog;          // the persistent walk's progress counters, one per walk (MAX_WALKS)
     // float64 only (evp_fast64.cu): products the float64 subcycle would
     // otherwise form on every subcycle, folded once per step
     T *rsqrA;        // recip_rA / e^2 (C points)
@@ -69,6 +70,7 @@ struct FastConsts {
     T *rdyUh_y, *dyVh_y;   // 0.5 * recip_dyU, 0.5 * dyV (along j)
 };
 constexpr int N_FAST_2D = 16;
+constexpr int MAX_WALKS = 16384;   // walks of one persistent float32 launch (resident warps bound it)
 constexpr int N_F64_2D = 8;
 
 __host__ __device__ inline int64_t internal_pitch(int NY) { return ((int64_t)NY + 7) / 8 * 8; }
@@ -98,6 +100,7 @@ size_t fast_layout(const Dims &d, char *base, FastConsts<T> *c, T *state[2][5], 
     c->pQrRz = reinterpret_cast<T *>(take(2 * f2));
     c->pMUV = reinterpret_cast<T *>(take(2 * f2));
     c->flags16 = reinterpret_cast<uint16_t *>(take(rup256((size_t)d.NX * lp * sizeof(uint16_t))));
+    c->wprog = reinterpret_cast<int *>(take(rup256((size_t)MAX_WALKS * sizeof(int))));
     for (int q = 0; q < 8; ++q) *ys[q] = reinterpret_cast<T *>(take(fy));
     // the float64 subcycle's folded products (no space for float32)
     const bool f64 = sizeof(T) == 8;
@@ -195,7 +198,7 @@ constexpr int N_WALK_VARIANTS = 4;
 int evp_walk_subcycles(bool adapt, bool paired, const Dims &d, const HaloFill &h, const FastConsts<float> &c,
                        const FastScalars<float> &k,
                        float *const state[2][5], float *const outs[5], int64_t ldo, int n, bool basal, bool turn,
-                       int rows, int variant, cudaStream_t st, bool paired_outs = false);
+                       int rows, int variant, cudaStream_t st, bool paired_outs = false, int *status = nullptr);
 // the walk's layout (its first four fields at `quad`, sigma12 at `s12`, pitch
 // lp) -> five planar arrays of pitch ldo
 int evp_walk_unpack(const Dims &d, const float *quad, const float *s12, float *const outs[5], int64_t ldo,

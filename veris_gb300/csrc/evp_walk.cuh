@@ -52,23 +52,31 @@ struct Row {
 
 // PIN: the state is the walk's four-value layout, io.u holding (u, v, sigma1, sigma2)
 // A1D: the cell areas vary along j only (per-lane constants): qr, rz are not loaded
-template <bool BASAL, bool ADAPT = false, bool PIN = false, bool A1D = false>
+// COH: the state was written by other warps of the same launch (the
+// persistent walk): load it through L2, not the read-only path
+template <bool COH, class T>
+__device__ __forceinline__ T state_ld(const T *p) {
+    if constexpr (COH) return __ldcg(p);
+    else return __ldg(p);
+}
+
+template <bool BASAL, bool ADAPT = false, bool PIN = false, bool A1D = false, bool COH = false>
 __device__ __forceinline__ void load_row(Row &r, const FastConsts<float> &c, const FastIO<float> &io, int64_t lp,
                                          int gi, int gj) {
     const int64_t o = (int64_t)gi * lp + gj;
     if (PIN) {
-        const float4 q = __ldg(reinterpret_cast<const float4 *>(io.u) + o);
+        const float4 q = state_ld<COH>(reinterpret_cast<const float4 *>(io.u) + o);
         r.u = q.x;
         r.v = q.y;
         r.s1 = q.z;
         r.s2 = q.w;
     } else {
-        r.u = __ldg(io.u + o);
-        r.v = __ldg(io.v + o);
-        r.s1 = __ldg(io.s1 + o);
-        r.s2 = __ldg(io.s2 + o);
+        r.u = state_ld<COH>(io.u + o);
+        r.v = state_ld<COH>(io.v + o);
+        r.s1 = state_ld<COH>(io.s1 + o);
+        r.s2 = state_ld<COH>(io.s2 + o);
     }
-    r.s12 = __ldg(io.s12 + o);
+    r.s12 = state_ld<COH>(io.s12 + o);
     const float4 om = __ldg(reinterpret_cast<const float4 *>(c.q4O) + o);
     const float2 qz = A1D ? make_float2(0.f, 0.f) : __ldg(reinterpret_cast<const float2 *>(c.pQrRz) + o);
     r.uo = om.x;
@@ -99,7 +107,7 @@ __device__ __forceinline__ void load_row(Row &r, const FastConsts<float> &c, con
 // velocities.  A1D: the cell areas (0.25/rA, rAz, 1/rAu, 1/rAv) vary along j
 // only and live in registers for the whole walk.
 template <bool BASAL, bool TURN, int UNROLL, bool PRE = false, bool ADAPT = false, bool PIN = false,
-          bool POUT = false, bool A1D = false>
+          bool POUT = false, bool A1D = false, bool COH = false>
 __device__ __forceinline__ void walk_strip(const Dims &d, int64_t lp, const HaloFill &h, const FastConsts<float> &c,
                                            const FastScalars<float> &k, const FastIO<float> &io, int i0, int j0,
                                            int H, int lane) {
@@ -132,7 +140,7 @@ __device__ __forceinline__ void walk_strip(const Dims &d, int64_t lp, const Halo
     // row indices advance by one per step: wrapped incrementally (any walk length)
     int gnext = d.wxa(i0 - 2);   // row of the next prefetch
     int gown = d.wxa(i0 - 4);    // row of this step's own-point constants (row t-2)
-    load_row<BASAL, ADAPT, PIN, A1D>(Pf, c, io, lp, gnext, gj);
+    load_row<BASAL, ADAPT, PIN, A1D, COH>(Pf, c, io, lp, gnext, gj);
     const int T = H + 4;   // rows i0-2 .. i0+H+1
     // UNROLL = 4 (the rotation period) would rename the row ages instead of
     // copying them; measured slower (register pressure), the kernels use 1
@@ -140,7 +148,7 @@ __device__ __forceinline__ void walk_strip(const Dims &d, int64_t lp, const Halo
     for (int t = 0; t < T; ++t) {
         N = Pf;
         gnext = gnext + 1 == d.NX ? 0 : gnext + 1;
-        if (t + 1 < T) load_row<BASAL, ADAPT, PIN, A1D>(Pf, c, io, lp, gnext, gj);
+        if (t + 1 < T) load_row<BASAL, ADAPT, PIN, A1D, COH>(Pf, c, io, lp, gnext, gj);
         // own-point constants of row t-2 (stage D)
         float cU = 0.f, cV = 0.f, AW = 0.f, AS = 0.f, mU = 0.f, mV = 0.f, rrAu = 0.f, rrAv = 0.f;
         if (PRE) {
