@@ -428,6 +428,14 @@ int veris_evp_adjoint_f32(const VerisGrid *g, const VerisParams *p, const VerisF
                           float *l_sigma120, const VerisFieldsF64 *lfields, double *lscalars,
                           void *workspace, size_t workspace_bytes, veris_stream_t s);
 size_t veris_evp_adjoint_taped_workspace_bytes_f32(const VerisGrid *g, int32_t n_subcycles);
+/*
+ * Form of the float32 EVP adjoint subcycle: 0 by grid size (the gather
+ * passes from 2^19 padded cells up, where they are memory-bound; below, one
+ * tile kernel per subcycle, which beats six latency-bound launches), 1 the
+ * tile kernel, 2 the gather passes.  Process-wide, for every later call;
+ * the two agree to float32 rounding.  VERIS_ERR_ARG for other values.
+ */
+int veris_evp_adjoint_f32_form(int32_t form);
 int veris_evp_adjoint_taped_f32(const VerisGrid *g, const VerisParams *p, const VerisFieldsF64 *vs,
                                 int32_t n_subcycles, const float *tape, size_t tape_bytes,
                                 const float *l_uIce, const float *l_vIce, const float *l_sigma1,

@@ -74,3 +74,40 @@ def test_adjoint_is_the_transpose_of_the_tangent(case, golden):
     mag = sum(float(np.abs(t).sum()) for t in lhs_terms + rhs_terms)
     assert mag > 0
     assert abs(lhs - rhs) <= TOL * mag, f"{case}/{golden}: <J dx, w> {lhs:.12e} <dx, J^T w> {rhs:.12e}"
+
+
+@pytest.mark.parametrize("golden", ["moving", "c1"])
+@pytest.mark.parametrize("form", [1, 2])
+def test_float32_evp_adjoint_is_the_transpose_to_float32_rounding(golden, form):
+    """The float32 EVP adjoint (form 1: the tile kernel; 2: the gather passes,
+    which recompute Delta, zeta and cDrag in float32) against the float64
+    oracle's exact tangent: <J dx, w> = <dx, J^T w> to float32 rounding of
+    the state, the linearisation and the adjoint sweep (bar 1e-4 of the
+    magnitude of the terms)."""
+    from veris_gb300 import _abi
+    from veris_gb300 import adjoint as A
+    from veris_gb300.state import VerisState
+    lib = _abi.load()
+    rng = np.random.default_rng(5)
+    st = jitter(golden_state("evp", golden), rng)
+    _routine, ins, outs, _f = CASES["evp"]
+    dx = directions(st, ins, rng)
+    jd = tangent("evp", st, dx)
+    w = {k: rng.standard_normal(jd[k].shape) for k in outs}
+    lhs_terms = [w[k] * jd[k] for k in outs]
+    lhs = sum(float(t.sum()) for t in lhs_terms)
+    gst = VerisState.from_numpy(vars(st.variables), st.settings)
+    lam = {k: torch.as_tensor(w[k], device="cuda") for k in outs}
+    try:
+        assert lib.veris_evp_adjoint_f32_form(form) == 0
+        state, fields, _drag = A.evp_adjoint(gst, lam, n_subcycles=3, precision="f32")
+    finally:
+        lib.veris_evp_adjoint_f32_form(0)
+    adj = dict(state, **fields)
+    torch.cuda.synchronize()
+    rhs_terms = [dx[k] * adj[k].cpu().numpy() for k in ins]
+    rhs = sum(float(t.sum()) for t in rhs_terms)
+    mag = sum(float(np.abs(t).sum()) for t in lhs_terms + rhs_terms)
+    assert mag > 0
+    assert abs(lhs - rhs) <= 1e-4 * mag, f"evp f32 form {form}/{golden}: {lhs:.9e} vs {rhs:.9e} ({abs(lhs - rhs) / mag:.2e})"
+    assert lib.veris_evp_adjoint_f32_form(3) != 0

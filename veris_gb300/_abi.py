@@ -157,6 +157,7 @@ SIGNATURES = {
     "veris_evp_fast_solver_f64": ([_G, _Pa, _F, ctypes.c_int32, _P, _P, _P, _P, _P, _P, _S, _P], _I),
     "veris_evp_f64_tile_rows": ([ctypes.c_int32], _I),
     "veris_evp_walk_persistent": ([ctypes.c_int32], _I),
+    "veris_evp_adjoint_f32_form": ([ctypes.c_int32], _I),
     "veris_evp_walk_solver_f32": ([_G, _Pa, _F, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, _P, _P, _P, _P, _P,
                                    _P, _S, _P], _I),
     "veris_evp_smem_solver_f32": ([_G, _Pa, _F, ctypes.c_int32, _P, _P, _P, _P, _P, _P, _S, _P], _I),

@@ -21,29 +21,34 @@ EVP_FIELDS = ("SeaIceStrength", "SeaIceMassC", "SeaIceMassU", "SeaIceMassV", "Wi
               "AreaW", "AreaS", "uOcean", "vOcean", "hIceMean", "Area")
 
 
-def evp_adjoint(state, lam_out, n_subcycles=None, checkpoint_every=0):
+def evp_adjoint(state, lam_out, n_subcycles=None, checkpoint_every=0, precision="f64"):
     """Reverse-mode derivative of ``n_subcycles`` EVP subcycles.
 
     ``lam_out``: {name: float64 CUDA tensor} adjoints of uIce, vIce, sigma1,
     sigma2, sigma12 after the loop (missing names count as zero).  Returns
     (adjoints of the initial state {name: tensor}, adjoints of the constant
     fields {name: tensor}, {"waterIceDrag": float tensor, "waterIceDrag_south": ...}).
+    ``precision`` "f32": the float32 loop (its forward recomputed in float32,
+    the state adjoints float32, returned as float64 tensors).
     """
     s = state.settings
     n = int(s.nEVPsteps if n_subcycles is None else n_subcycles)
     c = Call(state)
-    zeros = lambda: torch.zeros(c.shape, dtype=torch.float64, device=c.device)
-    lo = [c.arg(lam_out[k], "lam_" + k) if k in lam_out else c.arg(zeros()) for k in EVP_STATE]
-    li = c.empty(5)
+    f32 = precision == "f32"
+    dt = torch.float32 if f32 else torch.float64
+    zeros = lambda d=torch.float64: torch.zeros(c.shape, dtype=d, device=c.device)
+    lam = [lam_out[k].to(dt).contiguous() if k in lam_out else zeros(dt) for k in EVP_STATE]
+    lo = [t.data_ptr() if f32 else c.arg(t, "lam_" + k) for k, t in zip(EVP_STATE, lam)]
+    li = [zeros(dt) for _ in EVP_STATE]
     lf = {k: zeros() for k in EVP_FIELDS}
     table = VerisFields(**{k: t.data_ptr() for k, t in lf.items()})
     scal = torch.zeros(2, dtype=torch.float64, device=c.device)
-    wsb = c.lib.veris_evp_adjoint_workspace_bytes(c.refs()[0], 8, n, int(checkpoint_every))
+    wsb = c.lib.veris_evp_adjoint_workspace_bytes(c.refs()[0], 4 if f32 else 8, n, int(checkpoint_every))
     ws, wsb = c.workspace(wsb)
-    check("evp_adjoint", c.lib.veris_evp_adjoint_f64(
-        *c.refs(), n, int(checkpoint_every), *lo, *[t.data_ptr() for t in li], ctypes.byref(table),
-        scal.data_ptr(), ws, wsb, c.stream))
-    return (dict(zip(EVP_STATE, li)), lf,
+    fn = c.lib.veris_evp_adjoint_f32 if f32 else c.lib.veris_evp_adjoint_f64
+    check("evp_adjoint", fn(*c.refs(), n, int(checkpoint_every), *lo, *[t.data_ptr() for t in li],
+                            ctypes.byref(table), scal.data_ptr(), ws, wsb, c.stream))
+    return (dict(zip(EVP_STATE, [t.double() for t in li])), lf,
             {"waterIceDrag": scal[0], "waterIceDrag_south": scal[1]})
 
 

@@ -21,6 +21,8 @@
 // Non-differentiable points take these subgradients: sqrt at Delta = 0 and at
 // a drag argument of 0 give 0; the ocean-drag floor (cDragMin) and the
 // "denominator = 0 -> 1" guard contribute nothing on their constant branch.
+#include <atomic>
+
 #include "evp_adjoint.cuh"
 
 namespace veris {
@@ -598,7 +600,7 @@ struct Plan {
     int *status;
     Adj<T> a;
     T *cp, *seg, *lam[2][5];
-    double *scr[N_SCRATCH64];   // float64: the gather passes' arrays
+    T *scr[N_SCRATCH];   // the gather passes' arrays
     size_t field;   // bytes of one internal array
     size_t total;
 };
@@ -615,13 +617,14 @@ static size_t plan(const Dims &d, int n, int K, char *base, Plan<T> *pl, bool ta
     double *sc = reinterpret_cast<double *>(take(256));
     pl->a.dragN = sc;
     pl->a.dragS = sc ? sc + 1 : nullptr;
+    // float64 gather passes: per-cell water-drag sums, reduced after the sweep
+    pl->a.dragC = reinterpret_cast<double *>(take(sizeof(T) == 8 ? rup256((size_t)d.NX * lp * sizeof(double)) : 0));
     const int ncp = taped ? 0 : (n + K - 1) / K;
     pl->cp = reinterpret_cast<T *>(take((size_t)ncp * 5 * pl->field));
     pl->seg = reinterpret_cast<T *>(take(taped ? 0 : (size_t)(K + 1) * 5 * pl->field));
     for (int b = 0; b < 2; ++b)
         for (int q = 0; q < 5; ++q) pl->lam[b][q] = reinterpret_cast<T *>(take(pl->field));
-    for (int q = 0; q < N_SCRATCH64; ++q)
-        pl->scr[q] = sizeof(T) == 8 ? reinterpret_cast<double *>(take(pl->field)) : nullptr;
+    for (int q = 0; q < N_SCRATCH; ++q) pl->scr[q] = reinterpret_cast<T *>(take(pl->field));
     pl->total = off;
     return off;
 }
@@ -638,6 +641,12 @@ static int copy_state(T *const dst[5], T *const src[5], size_t bytes, cudaStream
     return VERIS_OK;
 }
 
+// the float32 adjoint's form: 0 by grid size, 1 the tile kernel, 2 the gather passes
+static std::atomic<int> g_f32_form{0};
+// padded cells from which the float32 adjoint takes the gather passes (measured: 360 x 180
+// faster with the tile kernel, 3600 x 1800 with the passes)
+constexpr int64_t F32_GATHER_CELLS = 1 << 19;
+
 // tape != nullptr: the forward's subcycle states (slot k = after k
 // subcycles, 5 arrays per slot, plan field bytes each) replace the
 // checkpoints and the recomputation
@@ -652,6 +661,11 @@ static int evp_adjoint(const VerisGrid *g, const VerisParams *p, const VerisFiel
     if (fast_support(*p)) return VERIS_ERR_UNSUPPORTED;
     if (K <= 0 || K > n || tape) K = n;
     const bool taped = tape != nullptr;
+    // float64: the gather passes; float32: the passes on large grids (memory-bound there), the
+    // tile kernel on small ones (its one launch per subcycle beats six latency-bound ones)
+    const int f32_form = g_f32_form.load(std::memory_order_relaxed);
+    const bool gather = sizeof(T) == 8 || f32_form == 2 ||
+                        (f32_form == 0 && (int64_t)d.NX * d.NY >= F32_GATHER_CELLS);
     Plan<T> pl;
     VERIS_REQUIRE(ws && wsb >= plan<T>(d, n, K, nullptr, &pl, taped), VERIS_ERR_WORKSPACE);
     plan<T>(d, n, K, static_cast<char *>(ws), &pl, taped);
@@ -669,6 +683,9 @@ static int evp_adjoint(const VerisGrid *g, const VerisParams *p, const VerisFiel
     for (int q = 0; q < 11; ++q)
         if (cudaMemsetAsync(zero_list[q], 0, pl.field, st) != cudaSuccess) return VERIS_ERR_LAUNCH;
     if (cudaMemsetAsync(pl.a.dragN, 0, 2 * sizeof(double), st) != cudaSuccess) return VERIS_ERR_LAUNCH;
+    if (sizeof(T) == 8 &&
+        cudaMemsetAsync(pl.a.dragC, 0, (size_t)d.NX * lp * sizeof(double), st) != cudaSuccess)
+        return VERIS_ERR_LAUNCH;
 
     // forward sweep: state 0 from the prep, checkpoints every K subcycles
     T *cp0[5];
@@ -730,12 +747,23 @@ static int evp_adjoint(const VerisGrid *g, const VerisParams *p, const VerisFiel
             T *out[5];
             for (int q = 0; q < 5; ++q) out[q] = pl.lam[first ? 0 : lb ^ 1][q];
             const int rs = taped ? ss : ss - s0;   // slot of this subcycle's input state
-            if constexpr (sizeof(T) == 8) {
-                // gather passes: every adjoint array written whole, nothing to clear
-                const Tape64 tt{slot(segb, pl.field, rs, 0), slot(segb, pl.field, rs, 1), slot(segb, pl.field, rs, 2),
-                                slot(segb, pl.field, rs, 3), slot(segb, pl.field, rs, 4),
-                                slot(segb, pl.field, rs + 1, 0), slot(segb, pl.field, rs + 1, 1)};
-                Lam64 ll;
+            if (gather) {
+                // gather passes: every adjoint array written whole, nothing to clear.  A float64
+                // slot holds (u, v, Delta, zeta, cDrag); a float32 tape the walk's (u, v, sigma1,
+                // sigma2) layout, a float32 segment five planar state arrays: the passes recompute
+                // Delta, zeta and cDrag
+                const bool quad = taped && sizeof(T) == 4;
+                TapeG<T> tt;
+                tt.u = slot(segb, pl.field, rs, 0);
+                tt.v = quad ? tt.u + 1 : slot(segb, pl.field, rs, 1);
+                tt.un = slot(segb, pl.field, rs + 1, 0);
+                tt.vn = quad ? tt.un + 1 : slot(segb, pl.field, rs + 1, 1);
+                tt.sst = quad ? 4 : 1;
+                const bool rich = sizeof(T) == 8;
+                tt.del = rich ? slot(segb, pl.field, rs, 2) : nullptr;
+                tt.zeta = rich ? slot(segb, pl.field, rs, 3) : nullptr;
+                tt.cd = rich ? slot(segb, pl.field, rs, 4) : nullptr;
+                LamG<T> ll;
                 if (first) {
                     ll.lu = lout[0]; ll.lv = lout[1]; ll.ls1 = lout[2]; ll.ls2 = lout[3]; ll.ls12 = lout[4];
                     ll.ldl = d.ld;
@@ -745,8 +773,8 @@ static int evp_adjoint(const VerisGrid *g, const VerisParams *p, const VerisFiel
                     ll.ldl = lp;
                 }
                 ll.ou = out[0]; ll.ov = out[1]; ll.os1 = out[2]; ll.os2 = out[3]; ll.os12 = out[4];
-                if ((stt = adjoint64_subcycle(d, lp, h, pl.c, k, p->rhoSea, tt, ll, pl.a, pl.scr, basal, turn, st)) !=
-                    VERIS_OK)
+                if ((stt = adjoint_gather_subcycle<T>(d, lp, h, pl.c, k, p->rhoSea, tt, ll, pl.a, pl.scr, basal, turn,
+                                                      st)) != VERIS_OK)
                     return stt;
                 lb = first ? 0 : lb ^ 1;
                 continue;
@@ -786,6 +814,11 @@ static int evp_adjoint(const VerisGrid *g, const VerisParams *p, const VerisFiel
             if (stt != VERIS_OK) return stt;
             lb = first ? 0 : lb ^ 1;
         }
+    }
+    if (sizeof(T) == 8) {   // the water-drag gradients of the gather passes
+        const double wN = k.dN != 0 ? p->rhoSea / (double)k.dN : 0.0, wS = k.dS != 0 ? p->rhoSea / (double)k.dS : 0.0;
+        if ((stt = reduce_drag(d, lp, pl.c.flags, pl.a.dragC, wN, wS, pl.a.dragN, pl.a.dragS, st)) != VERIS_OK)
+            return stt;
     }
     // fold the constant adjoints back onto the fields; initial-state adjoints
     dim3 g2((d.NY + 31) / 32, (d.NX + 7) / 8);
@@ -884,6 +917,12 @@ int veris_evp_adjoint_f64(const VerisGrid *g, const VerisParams *p, const VerisF
     const double *lout[5] = {lu, lv, ls1, ls2, ls12};
     double *lin[5] = {lu0, lv0, ls10, ls20, ls120};
     return adj::evp_adjoint<double>(g, p, vs, n, K, lout, lin, lfields, lscalars, ws, wsb, s);
+}
+
+int veris_evp_adjoint_f32_form(int32_t form) {
+    VERIS_REQUIRE(form >= 0 && form <= 2, VERIS_ERR_ARG);
+    adj::g_f32_form.store(form, std::memory_order_relaxed);
+    return VERIS_OK;
 }
 
 }  // extern "C"

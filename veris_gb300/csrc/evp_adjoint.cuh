@@ -1,4 +1,4 @@
-// Shared declarations of the EVP adjoint (evp_adjoint.cu, evp_adjoint64.cu).
+// Shared declarations of the EVP adjoint (evp_adjoint.cu, evp_adjoint_gather.cu).
 #pragma once
 #include "evp_fast.cuh"
 
@@ -11,31 +11,48 @@ struct Adj {
     // adjoints of the folded constants (internal pitch), accumulated over subcycles
     T *Ph, *mfC, *bfac, *mU, *cU, *AW, *uOc, *mV, *cV, *AS, *vOc;
     double *dragN, *dragS;   // d/d waterIceDrag, d/d waterIceDrag_south
+    double *dragC;           // float64 gather passes: per-cell sum over subcycles of dL/dcDrag cDrag
 };
 
-// One float64 subcycle of the adjoint sweep in gather passes
-// (evp_adjoint64.cu).  The subcycle's tape entries: the velocities before
-// and after it, and the Delta, zeta and ocean-drag coefficient it computed.
-struct Tape64 {
-    const double *u, *v, *del, *zeta, *cd;   // slot k (pitch lp)
-    const double *un, *vn;                   // u, v of slot k + 1
+// dragN, dragS += the per-cell sums dragC times rhoSea / (rhoSea drag) of
+// each hemisphere (the float64 gather passes' water-drag gradients)
+int reduce_drag(const Dims &d, int64_t lp, const uint32_t *flags, const double *dragC, double wN, double wS,
+                double *dragN, double *dragS, cudaStream_t st);
+
+// One subcycle of the adjoint sweep in gather passes (evp_adjoint_gather.cu).
+// Its tape entries: the velocities before and after it (element stride sst:
+// 1 planar, 4 in the float32 register walk's (u, v, sigma1, sigma2) layout)
+// and the Delta, zeta and ocean-drag coefficient it computed (a float64 tape
+// holds them; for a float32 tape the adjoint recomputes them first: NULL).
+template <class T>
+struct TapeG {
+    const T *u, *v;          // slot k (pitch lp)
+    const T *un, *vn;        // slot k + 1
+    int64_t sst;
+    const T *del, *zeta, *cd;
+    __device__ __forceinline__ T U(int64_t o) const { return u[o * sst]; }
+    __device__ __forceinline__ T V(int64_t o) const { return v[o * sst]; }
+    __device__ __forceinline__ T UN(int64_t o) const { return un[o * sst]; }
+    __device__ __forceinline__ T VN(int64_t o) const { return vn[o * sst]; }
 };
 
 // adjoints of the subcycle's outputs (pitch ldl; the image points of a
 // filled halo included) and of its inputs (pitch lp, overwritten)
-struct Lam64 {
-    const double *lu, *lv, *ls1, *ls2, *ls12;
+template <class T>
+struct LamG {
+    const T *lu, *lv, *ls1, *ls2, *ls12;
     int64_t ldl;
-    double *ou, *ov, *os1, *os2, *os12;
+    T *ou, *ov, *os1, *os2, *os12;
 };
 
-// the passes' intermediate arrays, one internal field each
-constexpr int N_SCRATCH64 = 26;
+// the passes' intermediate arrays, one internal field each (the last four:
+// e12, Delta, zeta and cDrag recomputed for a tape that lacks them)
+constexpr int N_SCRATCH = 30;
 
-int adjoint64_subcycle(const Dims &d, int64_t lp, const HaloFill &h, const FastConsts<double> &c,
-                       const FastScalars<double> &k, double rhoSea, const Tape64 &t, const Lam64 &l,
-                       const Adj<double> &a, double *const scratch[N_SCRATCH64], bool basal, bool turn,
-                       cudaStream_t st);
+template <class T>
+int adjoint_gather_subcycle(const Dims &d, int64_t lp, const HaloFill &h, const FastConsts<T> &c,
+                            const FastScalars<T> &k, double rhoSea, const TapeG<T> &t, const LamG<T> &l,
+                            const Adj<T> &a, T *const scratch[N_SCRATCH], bool basal, bool turn, cudaStream_t st);
 
 }  // namespace adj
 
