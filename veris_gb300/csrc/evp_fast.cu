@@ -112,6 +112,7 @@ __global__ void fast_prep_kernel(VerisParams p, Fields<double> f, Dims d, int64_
         c.mVb[q] = bU * mV;
         c.hAW[q] = 0.5 * p.cosWat * f.AreaW[o];
         c.hAS[q] = 0.5 * p.cosWat * f.AreaS[o];
+        c.Phh[q] = c.Ph[q] * (0.5 / p.evpAlpha);
         if (j == 0) {
             c.rdxVh_x[i] = 0.5 * f.recip_dxV[o];
             c.dxUh_x[i] = 0.5 * f.dxU[o];

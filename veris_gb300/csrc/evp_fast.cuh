@@ -66,12 +66,13 @@ struct FastConsts {
     T *mUb1, *mVb1;  // mass * (beta + 1) / dt (U, V points)
     T *mUb, *mVb;    // mass * beta / dt
     T *hAW, *hAS;    // 0.5 * cos(water turning angle) * AreaW, AreaS
+    T *Phh;          // Ph / (2 alpha): its division by Delta + Delta_min gives zeta / (2 alpha)
     T *rdxVh_x, *dxUh_x;   // 0.5 * recip_dxV, 0.5 * dxU (along i)
     T *rdyUh_y, *dyVh_y;   // 0.5 * recip_dyU, 0.5 * dyV (along j)
 };
 constexpr int N_FAST_2D = 16;
 constexpr int MAX_WALKS = 16384;   // walks of one persistent float32 launch (resident warps bound it)
-constexpr int N_F64_2D = 8;
+constexpr int N_F64_2D = 9;
 
 __host__ __device__ inline int64_t internal_pitch(int NY) { return ((int64_t)NY + 7) / 8 * 8; }
 
@@ -104,7 +105,7 @@ size_t fast_layout(const Dims &d, char *base, FastConsts<T> *c, T *state[2][5], 
     for (int q = 0; q < 8; ++q) *ys[q] = reinterpret_cast<T *>(take(fy));
     // the float64 subcycle's folded products (no space for float32)
     const bool f64 = sizeof(T) == 8;
-    T **f64s[N_F64_2D] = {&c->rsqrA, &c->mf4, &c->mUb1, &c->mVb1, &c->mUb, &c->mVb, &c->hAW, &c->hAS};
+    T **f64s[N_F64_2D] = {&c->rsqrA, &c->mf4, &c->mUb1, &c->mVb1, &c->mUb, &c->mVb, &c->hAW, &c->hAS, &c->Phh};
     for (int q = 0; q < N_F64_2D; ++q) *f64s[q] = reinterpret_cast<T *>(take(f64 ? f2 : 0));
     c->rdxVh_x = reinterpret_cast<T *>(take(f64 ? fx : 0));
     c->dxUh_x = reinterpret_cast<T *>(take(f64 ? fx : 0));

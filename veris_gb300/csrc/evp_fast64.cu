@@ -13,8 +13,11 @@
 //   precomputed coefficient;
 // * products of step constants are folded once per step by the prep
 //   (recip_rA/e^2, mass*(beta+1)/dt, mass*beta/dt, 0.5*cos*Area, 0.25*m*f,
-//   halved grid lengths) and the relaxation 1/alpha into the stress
-//   coefficients, one multiplication fewer per use;
+//   halved grid lengths, and 1/(2 alpha) into the ice strength factor, so
+//   that its division by Delta + Delta_min gives zeta/(2 alpha), the stress
+//   update's coefficient), one multiplication fewer per use; the drag
+//   coefficient is the square root of the product the drag floor's test
+//   forms;
 // * divisions and square roots start from the hardware's approximate
 //   reciprocal and reciprocal square root (rcp/rsqrt.approx.ftz.f64) and
 //   add the first terms of the series of the exact correction: with
@@ -39,36 +42,33 @@ namespace veris {
 
 struct F64Scalars {
     double am1r;             // (alpha - 1) / alpha
-    double hralpha;          // 0.5 / alpha
     double kp2;              // 2 * (press factor 2(1 - tsf)/(1 + tsf))
     double rsq, deltaMin;    // 1/e^2, Delta_min
     double dcq2N, dcq2S;     // 0.25 * (rhoSea * waterIceDrag)^2, north and south
-    double dchN, dchS;       // 0.5 * rhoSea * waterIceDrag
     double cmin, cmin2;      // cDragMin, its square
     double U02;              // basal drag U0^2
     double sinW;             // sin(water turning angle)
-    double nh1, nh2, nh3, nh4;   // 0.5 / alpha / n: the sigma12 average over n wet C points
+    double nh1, nh2, nh3, nh4;   // 1 / n: the sigma12 average over n wet C points (of zeta / (2 alpha))
+    double twoAlpha;             // 2 alpha: zeta from zeta / (2 alpha), for the tape
 };
 
 static F64Scalars f64_scalars(const FastScalars<double> &k) {
     F64Scalars s;
     s.am1r = k.alpha_m1 * k.ralpha;
-    s.hralpha = 0.5 * k.ralpha;
     s.kp2 = 2.0 * k.kp;
     s.rsq = k.rsq;
     s.deltaMin = k.deltaMin;
     s.dcq2N = 0.25 * k.dN2;
     s.dcq2S = 0.25 * k.dS2;
-    s.dchN = 0.5 * k.dN;
-    s.dchS = 0.5 * k.dS;
     s.cmin = k.cmin;
     s.cmin2 = k.cmin2;
     s.U02 = k.U02;
     s.sinW = k.sinW;
-    s.nh1 = 0.5 * k.ralpha;
-    s.nh2 = 0.5 * k.ralpha * 0.5;
-    s.nh3 = 0.5 * k.ralpha * (1.0 / 3.0);
-    s.nh4 = 0.5 * k.ralpha * 0.25;
+    s.nh1 = 1.0;
+    s.nh2 = 0.5;
+    s.nh3 = 1.0 / 3.0;
+    s.nh4 = 0.25;
+    s.twoAlpha = 2.0 / k.ralpha;
     return s;
 }
 
@@ -202,7 +202,7 @@ evp_f64_kernel(Dims d, int64_t lp, HaloFill h, FastConsts<double> c, F64Scalars 
         const double e11 = inC ? (ue - u0) * __ldg(c.rdxU_x + gi) : 0.0;
         const double e22 = inC ? (vn - v0) * __ldg(c.rdyV_y + gj) : 0.0;
         const double ep = e11 + e22, em = e11 - e22;
-        const double Ph = __ldg(c.Ph + o);
+        const double Ph = __ldg(c.Phh + o);   // Ph / (2 alpha): zeta below is zeta / (2 alpha)
         double zeta = 0.0, delta = 0.0;
         // (a taped subcycle keeps Delta where zeta = 0 too: the adjoint needs it)
         const bool strong = __any_sync(m, !is_zero(Ph));
@@ -221,7 +221,7 @@ evp_f64_kernel(Dims d, int64_t lp, HaloFill h, FastConsts<double> c, F64Scalars 
             const int q = IC(li, lj);
             const bool mC = f0 & F_MC;
             // sigma_k = sigma_k (alpha-1)/alpha + zeta/(2 alpha) * (4 ep - 2 kp Delta | em)
-            const double zh = zeta * k.hralpha;
+            const double zh = zeta;
             const double s1 = mC ? fma(__ldg(io.s1 + o), k.am1r, zh * fma(4.0, ep, -(k.kp2 * delta))) : 0.0;
             const double s2 = mC ? fma(__ldg(io.s2 + o), k.am1r, zh * em) : 0.0;
             sS11[q] = (s1 + s2) * __ldg(c.dyVh_y + gj);
@@ -232,8 +232,8 @@ evp_f64_kernel(Dims d, int64_t lp, HaloFill h, FastConsts<double> c, F64Scalars 
                 io.s1o[w] = s1;
                 io.s2o[w] = s2;
             }
-            // ocean drag at C (veris/dynamics_routines.py:21-52): with X = 4 t,
-            // dc^2 t > cmin^2 <=> (dc^2/4) X > cmin^2 and dc sqrt(t) = (dc/2) sqrt(X)
+            // ocean drag at C (veris/dynamics_routines.py:21-52): with X = 4 t and
+            // Y = (dc^2/4) X, dc^2 t > cmin^2 <=> Y > cmin^2 and dc sqrt(t) = sqrt(Y)
             const uint32_t fe = sF[IS(li + 1, lj)], fn = sF[IS(li, lj + 1)];
             const double du0 = (f0 & F_INU) ? u0 - __ldg(c.uOc + o) : 0.0;
             const double du1 = (fe & F_INU) ? ue - uoc(li + 1, lj) : 0.0;
@@ -242,17 +242,18 @@ evp_f64_kernel(Dims d, int64_t lp, HaloFill h, FastConsts<double> c, F64Scalars 
             const double a = du0 + du1, b = dv0 + dv1;
             const double X = fma(b, b, a * a);
             const bool south = f0 & F_SOUTH;
-            const bool fast = gt_nonneg((south ? k.dcq2S : k.dcq2N) * X, k.cmin2);
+            const double Y = (south ? k.dcq2S : k.dcq2N) * X;
+            const bool fast = gt_nonneg(Y, k.cmin2);
             double cd = k.cmin;
             if (__any_sync(m2, fast)) {
-                const double sx = sqrt64(X, m2);
-                if (fast) cd = (south ? k.dchS : k.dchN) * sx;
+                const double sy = sqrt64(Y, m2);
+                if (fast) cd = sy;
             }
             sCd[q] = mC ? cd : 0.0;
             if (TAPE && own) {
                 const int64_t w = (int64_t)gi * io.ldo + gj;
                 io.tDel[w] = delta;
-                io.tZeta[w] = zeta;
+                io.tZeta[w] = zeta * k.twoAlpha;
                 io.tCd[w] = mC ? cd : 0.0;
             }
             if (BASAL) {   // veris/dynamics_routines.py:55-96 with the step factor folded by the prep
