@@ -237,10 +237,12 @@ def fp64_peak(sm_count):
     return FP64_LANES_PER_SM_CYCLE * sm_count * float(mhz) * 1e6 / 1e9, float(mhz)
 
 
-def recorded(kernel, workload, what="traffic"):
+def recorded(kernel, workload, what="traffic", form=None):
     """A per-launch figure of ``kernel`` on ``workload`` from an ncu capture
     (profiles/roofline_traffic.json): DRAM bytes ("traffic") or float64-pipe
-    lane operations ("fp64_lane_ops"); None when not recorded."""
+    lane operations ("fp64_lane_ops"), of the kernel's ``form`` (e.g. the
+    float64 subcycle's unit height "rows16") where one is recorded; None
+    when not recorded."""
     path = os.path.join(ROOT, "profiles", "roofline_traffic.json")
     try:
         with open(path) as f:
@@ -248,7 +250,17 @@ def recorded(kernel, workload, what="traffic"):
     except (OSError, ValueError):
         return None
     key = f"{kernel}/{workload}" + ("" if what == "traffic" else f":{what}")
+    if form is not None and f"{key}@{form}" in rec:
+        return rec[f"{key}@{form}"]
     return rec.get(key)
+
+
+def f64_rows(tuning, args):
+    """The float64 subcycle's unit height in use: the tuner's choice, the
+    one asked for, or the library default (24)."""
+    if isinstance(tuning, dict) and "rows" in tuning:
+        return int(tuning["rows"])
+    return args.f64_tile_rows if args.f64_tile_rows > 0 else 24
 
 
 # ----------------------------------------------------------------- CPU legs
@@ -464,30 +476,31 @@ def evp_launch_us(eng, n_sub, flush):
     return float(np.median(ms)) * 1e3 / n_sub
 
 
-def roofline_hbm(kernel, workload, cells, us, precision):
+def roofline_hbm(kernel, workload, cells, us, precision, form=None):
     peak, kind = hbm_peak()
     algo = BYTES_PER_CELL_SUBCYCLE[precision] * cells
     achieved = algo / (us * 1e-6) / 1e9
     return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "traffic": recorded(kernel, workload), "kernel": kernel, "algorithmic_bytes_per_launch": algo,
+            "traffic": recorded(kernel, workload, form=form), "kernel": kernel, "algorithmic_bytes_per_launch": algo,
             "avg_launch_us": us, "peak_source": f"{kind} HBM copy bandwidth"}
 
 
-def roofline_fp64(kernel, workload, cells, us, sm_count):
+def roofline_fp64(kernel, workload, cells, us, sm_count, rows=None):
     """The float64 subcycle's roofline: GB300's float64 pipe (its bound),
     with the HBM fraction of the algorithmic bytes beside it.  ``achieved``
     = the kernel's float64-pipe lane operations per launch (ncu, recorded in
     profiles/roofline_traffic.json) over the live launch duration."""
     peak, mhz = fp64_peak(sm_count)
-    ops = recorded(kernel, workload, "fp64_lane_ops")
+    form = f"rows{rows}" if rows else None
+    ops = recorded(kernel, workload, "fp64_lane_ops", form)
     achieved = ops / (us * 1e-6) / 1e9 if ops else None
     return {"bound": "fp64_pipe", "achieved": achieved, "peak": peak, "unit": "Gop/s",
-            "frac": achieved / peak if achieved else None, "traffic": recorded(kernel, workload),
-            "kernel": kernel, "avg_launch_us": us, "fp64_lane_ops_per_launch": ops,
+            "frac": achieved / peak if achieved else None, "traffic": recorded(kernel, workload, form=form),
+            "kernel": kernel, "unit_rows": rows, "avg_launch_us": us, "fp64_lane_ops_per_launch": ops,
             "fp64_lane_ops_per_cell": ops / cells if ops else None,
             "peak_source": f"{FP64_LANES_PER_SM_CYCLE} float64 lanes per SM and cycle x {sm_count} SMs x "
                            f"{mhz:g} MHz (the measured maximum SM clock)",
-            "hbm": roofline_hbm(kernel, workload, cells, us, "f64")}
+            "hbm": roofline_hbm(kernel, workload, cells, us, "f64", form)}
 
 
 def e2e_of(eng, args, ws, cells, n_sub):
@@ -649,7 +662,8 @@ def c5_block(args, dev, flush):
     ms64, _, _ = time_steps(e64, 2, 1, flush, 1, dev)
     us64 = evp_launch_us(e64, n_sub, flush)
     out["fp64"] = {"value": cells * n_sub * 2 / (ms64 / 1e3) / 1e9, "ms_per_step": ms64 / 2, "steps": 2,
-                   "roofline": roofline_fp64(evp_kernel_name(e64), name, cells, us64, sms), "f64_tile": tuning64}
+                   "roofline": roofline_fp64(evp_kernel_name(e64), name, cells, us64, sms, f64_rows(tuning64, args)),
+                   "f64_tile": tuning64}
     del e64
     e32, tuning = make_engine(arrays, sett, dev, "f32", args)
     ms32, _, _ = time_steps(e32, 5, 2, flush, 1, dev)
@@ -719,7 +733,7 @@ def run_ours(args):
     us = evp_launch_us(eng, n_sub, flush)
     phases = eng.phase_times()
     kernel = evp_kernel_name(eng)
-    roof = (roofline_fp64(kernel, args.config, cells, us, sms) if args.precision == "f64"
+    roof = (roofline_fp64(kernel, args.config, cells, us, sms, f64_rows(tuning, args)) if args.precision == "f64"
             else roofline_hbm(kernel, args.config, cells, us, "f32"))
     line = {"metric": METRIC, "value": value, "unit": "Gcell-subcycles/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
