@@ -55,11 +55,14 @@ def _direction(st, name, rng):
 # c1 starts from rest, where Delta = 0 and zeta = P/deltaMin: a finite
 # difference of any affordable size then measures a secant of zeta(Delta),
 # not its derivative, so c1 is checked from the start of its second step.
-@pytest.mark.parametrize("case,call", (("c1", 1), ("moving", 0), ("moving", 1)))
-def test_evp_adjoint_matches_finite_differences(case, call):
+@pytest.mark.parametrize("case,call,fill", (("c1", 1, True), ("moving", 0, True), ("moving", 1, True),
+                                            ("c1", 1, False)))
+def test_evp_adjoint_matches_finite_differences(case, call, fill):
+    """fill False: both halos refreshed after every subcycle (veros_fill off),
+    so the adjoint also moves the y-halo images' adjoints to their sources."""
     from veris_gb300.adjoint import evp_adjoint
     rng = np.random.default_rng(5)
-    st = _state(case, call)
+    st = _state(case, call, veros_fill=fill)
     shape = tuple(st.variables.iceMask.shape)
     W = [torch.as_tensor(rng.standard_normal(shape), device="cuda") for _ in range(5)]
     lam_in, lam_f, scal = evp_adjoint(st, dict(zip(("uIce", "vIce", "sigma1", "sigma2", "sigma12"), W)),

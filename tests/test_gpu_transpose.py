@@ -111,3 +111,27 @@ def test_float32_evp_adjoint_is_the_transpose_to_float32_rounding(golden, form):
     assert mag > 0
     assert abs(lhs - rhs) <= 1e-4 * mag, f"evp f32 form {form}/{golden}: {lhs:.9e} vs {rhs:.9e} ({abs(lhs - rhs) / mag:.2e})"
     assert lib.veris_evp_adjoint_f32_form(3) != 0
+
+
+def test_evp_adjoint_is_the_transpose_with_both_halos_refreshed():
+    """The float64 EVP adjoint with veros_fill off (the x and the y halo
+    refreshed after every subcycle): the adjoints of both halos' images go
+    back to their sources; against the oracle's exact tangent to 1e-10."""
+    from veris_gb300.state import VerisState
+    rng = np.random.default_rng(7)
+    st = jitter(golden_state("evp", "c1"), rng)
+    st.settings.veros_fill = False
+    _routine, ins, outs, _f = CASES["evp"]
+    dx = directions(st, ins, rng)
+    jd = tangent("evp", st, dx)
+    w = {k: rng.standard_normal(jd[k].shape) for k in outs}
+    lhs_terms = [w[k] * jd[k] for k in outs]
+    lhs = sum(float(t.sum()) for t in lhs_terms)
+    gst = VerisState.from_numpy(vars(st.variables), st.settings)
+    lam = {k: torch.as_tensor(w[k], device="cuda") for k in outs}
+    adj = _adjoint("evp", gst, lam)
+    torch.cuda.synchronize()
+    rhs_terms = [dx[k] * adj[k].cpu().numpy() for k in ins]
+    rhs = sum(float(t.sum()) for t in rhs_terms)
+    mag = sum(float(np.abs(t).sum()) for t in lhs_terms + rhs_terms)
+    assert abs(lhs - rhs) <= TOL * mag, f"{lhs:.12e} vs {rhs:.12e}"
