@@ -583,9 +583,9 @@ int veris_prep_adjoint_f64(const VerisGrid *g, const VerisParams *p, const Veris
  *                               first re-forms the momentum constant from
  *                               the current velocities (a new step).  shape
  *                               picks the tile (0: 32x32, 1: 16x32, 2: 32x16,
- *                               3: 16x16 shared-memory tiles; 4, 5, 6: register
- *                               walks of 8, 16, 32 rows over 28 columns, one
- *                               ticket per warp), blocks_per_sm the persistent
+ *                               3: 16x16 shared-memory tiles; 4-8: register
+ *                               walks of 8, 16, 32, 64, 128 rows over 28
+ *                               columns, one ticket per warp), blocks_per_sm the persistent
  *                               grid (0: 2 per SM, 4 for walks).  A memset and kernel launches
  *                               only: capturable in a CUDA graph.
  *   veris_batch_copy_state_f32  member m's five state arrays (buffer buf) into

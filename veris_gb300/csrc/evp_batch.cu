@@ -21,9 +21,10 @@
 namespace veris {
 namespace batch {
 
-// shapes 0-3: shared-memory tiles (rows x columns); 4-6: register walks of
-// 8, 16 or 32 rows over 28-column strips (one warp each)
-constexpr int N_SHAPES = 7;
+// shapes 0-3: shared-memory tiles (rows x columns); 4-8: register walks of
+// 8, 16, 32, 64 or 128 rows over 28-column strips (one warp each; longer
+// walks recompute fewer ring rows, shorter ones balance better)
+constexpr int N_SHAPES = 9;
 constexpr int FIRST_WALK = 4;
 template <int S>
 struct ShapeOf;
@@ -37,7 +38,8 @@ template <>
 struct ShapeOf<3> { static constexpr int TI = 16, TJ = 16, MINB = 4; };
 
 inline void shape_dims(int s, int *ti, int *tj) {
-    static const int T[N_SHAPES][2] = {{32, 32}, {16, 32}, {32, 16}, {16, 16}, {8, 28}, {16, 28}, {32, 28}};
+    static const int T[N_SHAPES][2] = {{32, 32}, {16, 32}, {32, 16}, {16, 16}, {8, 28}, {16, 28}, {32, 28},
+                                       {64, 28}, {128, 28}};
     *ti = T[s][0];
     *tj = T[s][1];
 }

@@ -37,7 +37,8 @@ from .state import VerisState
 
 EVP_STATE = ("uIce", "vIce", "sigma1", "sigma2", "sigma12")
 # 0-3: shared-memory tiles (rows, columns); 4-6: register walks (rows, 28 columns)
-SHAPES = {0: (32, 32), 1: (16, 32), 2: (32, 16), 3: (16, 16), 4: (8, 28), 5: (16, 28), 6: (32, 28)}
+SHAPES = {0: (32, 32), 1: (16, 32), 2: (32, 16), 3: (16, 16), 4: (8, 28), 5: (16, 28), 6: (32, 28), 7: (64, 28),
+          8: (128, 28)}
 
 
 def prepare_dynamics(lib, grid, params, fields, v, stream):
