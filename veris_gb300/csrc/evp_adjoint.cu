@@ -8,7 +8,13 @@
 // u/dt + wind forcing, ocean velocities, basal factor) and of the two water
 // drag coefficients.
 //
-// One CTA per TI x TJ tile.  The CTA recomputes the forward intermediates it
+// This file holds the driver of the sweep (checkpoints, segment recompute,
+// tapes, the reverse loop, the fold back onto the fields) and the float32
+// tile kernel below, which the sweep uses on float32 grids under 2^19
+// padded cells; float64 and larger float32 grids take the gather passes of
+// evp_adjoint_gather.cu.
+//
+// The tile kernel: one CTA per TI x TJ tile.  The CTA recomputes the forward intermediates it
 // needs on the tile plus its ring (strain rates, e12, Delta, zeta, drag
 // coefficients) from the subcycle's input state; it takes the output u', v'
 // from the next state of the sweep.  It then propagates the adjoints of its
@@ -779,40 +785,42 @@ static int evp_adjoint(const VerisGrid *g, const VerisParams *p, const VerisFiel
                 lb = first ? 0 : lb ^ 1;
                 continue;
             }
-            // the five adjoint arrays of a buffer are contiguous: one memset
-            if (cudaMemsetAsync(out[0], 0, 5 * pl.field, st) != cudaSuccess) return VERIS_ERR_LAUNCH;
-            Io<T> io;
-            // a float32 tape is written by the register walk in its own
-            // layout: (u, v, sigma1, sigma2) per point over the slot's first
-            // four fields
-            const bool quad = taped && sizeof(T) == 4;
-            io.u = slot(segb, pl.field, rs, 0);
-            io.v = quad ? io.u + 1 : slot(segb, pl.field, rs, 1);
-            io.s1 = slot(segb, pl.field, rs, 2);
-            io.s2 = slot(segb, pl.field, rs, 3);
-            io.s12 = slot(segb, pl.field, rs, 4);
-            io.un = slot(segb, pl.field, rs + 1, 0);
-            io.vn = quad ? io.un + 1 : slot(segb, pl.field, rs + 1, 1);
-            io.sst = quad ? 4 : 1;
-            io.ldn = lp;
-            if (first) {
-                io.lu = lout[0]; io.lv = lout[1]; io.ls1 = lout[2]; io.ls2 = lout[3]; io.ls12 = lout[4];
-                io.ldl = d.ld;
-            } else {
-                io.lu = pl.lam[lb][0]; io.lv = pl.lam[lb][1]; io.ls1 = pl.lam[lb][2];
-                io.ls2 = pl.lam[lb][3]; io.ls12 = pl.lam[lb][4];
-                io.ldl = lp;
+            if constexpr (sizeof(T) == 4) {   // the float32 tile kernel (float64 always gathers)
+                // the five adjoint arrays of a buffer are contiguous: one memset
+                if (cudaMemsetAsync(out[0], 0, 5 * pl.field, st) != cudaSuccess) return VERIS_ERR_LAUNCH;
+                Io<T> io;
+                // a float32 tape is written by the register walk in its own
+                // layout: (u, v, sigma1, sigma2) per point over the slot's first
+                // four fields
+                const bool quad = taped && sizeof(T) == 4;
+                io.u = slot(segb, pl.field, rs, 0);
+                io.v = quad ? io.u + 1 : slot(segb, pl.field, rs, 1);
+                io.s1 = slot(segb, pl.field, rs, 2);
+                io.s2 = slot(segb, pl.field, rs, 3);
+                io.s12 = slot(segb, pl.field, rs, 4);
+                io.un = slot(segb, pl.field, rs + 1, 0);
+                io.vn = quad ? io.un + 1 : slot(segb, pl.field, rs + 1, 1);
+                io.sst = quad ? 4 : 1;
+                io.ldn = lp;
+                if (first) {
+                    io.lu = lout[0]; io.lv = lout[1]; io.ls1 = lout[2]; io.ls2 = lout[3]; io.ls12 = lout[4];
+                    io.ldl = d.ld;
+                } else {
+                    io.lu = pl.lam[lb][0]; io.lv = pl.lam[lb][1]; io.ls1 = pl.lam[lb][2];
+                    io.ls2 = pl.lam[lb][3]; io.ls12 = pl.lam[lb][4];
+                    io.ldl = lp;
+                }
+                io.ou = out[0]; io.ov = out[1]; io.os1 = out[2]; io.os2 = out[3]; io.os12 = out[4];
+                const T rho = (T)p->rhoSea;
+                if (basal)
+                    stt = turn ? launch_adj<T, true, true>(d, lp, h, pl.c, k, io, pl.a, rho, st)
+                               : launch_adj<T, true, false>(d, lp, h, pl.c, k, io, pl.a, rho, st);
+                else
+                    stt = turn ? launch_adj<T, false, true>(d, lp, h, pl.c, k, io, pl.a, rho, st)
+                               : launch_adj<T, false, false>(d, lp, h, pl.c, k, io, pl.a, rho, st);
+                if (stt != VERIS_OK) return stt;
+                lb = first ? 0 : lb ^ 1;
             }
-            io.ou = out[0]; io.ov = out[1]; io.os1 = out[2]; io.os2 = out[3]; io.os12 = out[4];
-            const T rho = (T)p->rhoSea;
-            if (basal)
-                stt = turn ? launch_adj<T, true, true>(d, lp, h, pl.c, k, io, pl.a, rho, st)
-                           : launch_adj<T, true, false>(d, lp, h, pl.c, k, io, pl.a, rho, st);
-            else
-                stt = turn ? launch_adj<T, false, true>(d, lp, h, pl.c, k, io, pl.a, rho, st)
-                           : launch_adj<T, false, false>(d, lp, h, pl.c, k, io, pl.a, rho, st);
-            if (stt != VERIS_OK) return stt;
-            lb = first ? 0 : lb ^ 1;
         }
     }
     if (sizeof(T) == 8) {   // the water-drag gradients of the gather passes
