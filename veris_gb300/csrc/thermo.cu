@@ -165,6 +165,62 @@ __device__ void solve4temp_multi(const VerisParams &p, const S4TIn &x, const S &
         lwabs[l] = -lw - absSW;
         T[l] = Tin;
     }
+    if constexpr (!std::is_same<S, double>::value) {
+        // Derivatives (dual numbers): implicit differentiation at the root.
+        // The values come from the float64 solve itself (so every later
+        // branch is taken as in the forward); at its root T* of
+        // R(T) = Fc(T) - Fia(T), dT* = -R_theta / R_T with R_theta the
+        // residual's derivative at fixed T (through the conductivity and
+        // the absorbed radiation) and R_T = -(k + dFia/dT), the Newton
+        // iteration's own denominator; a root held by the melt or the
+        // minimum-temperature clamp has dT* = 0.  The converged Newton
+        // iterates have this derivative (the Newton map's derivative in T
+        // vanishes at the root), without iterating the dual numbers.
+        double hIv[NC], hSv[NC], Tv[NC], Fiov[NC], Fiav[NC], Penv[NC];
+#pragma unroll
+        for (int l = 0; l < NC; ++l) {
+            hIv[l] = val(hI[l]);
+            hSv[l] = val(hS[l]);
+        }
+        solve4temp_multi<NC, double>(p, x, val(Tin), hIv, hSv, Tv, Fiov, Fiav, Penv);
+        const double aa1l2 = aa1 * 3.32192809488736234787;
+        const double qnum = bb1 * cc0, qsub = one_m_bb1 * cc0;
+#pragma unroll
+        for (int l = 0; l < NC; ++l) {
+            if (!ice[l]) {
+                oT[l] = Tin;
+                oFio[l] = S(0.0);
+                oFia[l] = S(0.0);
+                continue;
+            }
+            const double t = Tv[l], t3 = t * t * t;
+            const double rt = 1.0 / t, c3 = ::exp2(aa1l2 * rt);
+            const double qs = qnum / (c3 * Pa - qsub), den = cc2 - c3 * Pa;
+            const double dqs = cc1 * c3 * (rt * rt) / (den * den);
+            const double FiaT = 4 * d3[l] * t3 + d1ug + d1iug * dqs;
+            const S Fc = k[l] * (x.TempFrz - t);
+            const S Fia = lwabs[l] + (t3 * t * d3[l] + d1ug * (t - Ta) + d1iug * (qs - x.aqh));
+            const bool held = t >= Tmelt || t <= Tmin;
+            S dT = Fc - Fia;   // its derivative part: R_theta
+            const double scale = held ? 0.0 : 1.0 / (val(k[l]) + FiaT);
+            S T = Tin, Fo = Fc, Fa = Fia;
+            T.v = t;
+#pragma unroll
+            for (int q = 0; q < (int)(sizeof(S::d) / sizeof(double)); ++q) {
+                const double dTq = dT.d[q] * scale;
+                T.d[q] = dTq;
+                Fo.d[q] = Fc.d[q] - val(k[l]) * dTq;
+                Fa.d[q] = Fia.d[q] + FiaT * dTq;
+            }
+            const bool up = Fiov[l] > 0;
+            Fo.v = Fiov[l];
+            Fa.v = Fiav[l];
+            oT[l] = T;
+            oFio[l] = up ? Fo : S(0.0);
+            oFia[l] = up ? S(0.0) : Fa;
+        }
+        return;
+    }
     S Fc[NC], Fia[NC];
     bool moving[NC];
 #pragma unroll
