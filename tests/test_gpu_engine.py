@@ -429,17 +429,23 @@ def test_float64_tile_heights_give_the_same_values_and_the_tuner_picks_one():
         lib.veris_evp_f64_tile_rows(0)
 
 
-@pytest.mark.parametrize("nx,ny,fill,n", ((300, 150, True, 25), (61, 33, True, 9), (120, 90, False, 14),
-                                          (1440, 720, True, 40)))
-def test_persistent_walk_gives_the_same_values(nx, ny, fill, n):
+_TURN = dict(waterTurnAngle=15.0, sinWat=float(np.sin(np.radians(15.0))), cosWat=float(np.cos(np.radians(15.0))))
+
+
+@pytest.mark.parametrize("nx,ny,fill,n,extra", ((300, 150, True, 25, {}), (61, 33, True, 9, {}),
+                                                (120, 90, False, 14, {}), (1440, 720, True, 40, {}),
+                                                (200, 120, True, 12, {"useAdaptiveEVP": True}),
+                                                (200, 120, False, 12, dict(_TURN, basalDragK2=15.0))))
+def test_persistent_walk_gives_the_same_values(nx, ny, fill, n, extra):
     """Several float32 subcycles per persistent launch (each walk waiting on
     its neighbours' progress counters) against one launch per subcycle: bit
     for bit, for several walk lengths and compiled forms, with the cyclic
-    x-halo images (veros_fill) and with both halos refreshed."""
+    x-halo images (veros_fill) and with both halos refreshed, and with the
+    adaptive EVP, basal drag and turning angles."""
     from veris_gb300 import _abi
     from veris_gb300.evp_solver import evp_solver_fast
     lib = _abi.load()
-    st = _prepared(nx, ny, nx + 7, veros_fill=fill)
+    st = _prepared(nx, ny, nx + 7, veros_fill=fill, **extra)
     try:
         for rows, variant in ((0, 2), (16, 0), (0, 3)):
             assert lib.veris_evp_walk_persistent(0) == 0
