@@ -359,9 +359,11 @@ evp_f64_kernel(Dims d, int64_t lp, HaloFill h, FastConsts<double> c, F64Scalars 
 
 // The units of a launch: when all full pieces fit the resident CTAs' slots
 // at once, the fewest pieces of at most TI rows; otherwise a last round of
-// about one small piece (TI/3 rows) per slot at the bottom of every strip,
+// about one small piece (TI/4 rows) per slot at the bottom of every strip,
 // the rest in full pieces.  (Equal full tiles left a thin last wave: 12 % of
-// the SM cycles idle on 1440 x 720 with 24-row tiles.)
+// the SM cycles idle on 1440 x 720 with 24-row tiles; third-height last
+// pieces took 197.2 us a launch there, quarter-height 193.0, fifth- and
+// sixth-height 193.8.)
 static F64Units f64_units(const Dims &d, int TI, int slots) {
     const int strips = (d.NY + 31) / 32;
     F64Units w;
@@ -369,7 +371,7 @@ static F64Units f64_units(const Dims &d, int TI, int slots) {
     w.P2 = 0;
     w.R1 = d.NX;
     if ((int64_t)strips * minP > slots) {
-        const int small = TI / 3 > 4 ? TI / 3 : 4;
+        const int small = TI / 4 > 4 ? TI / 4 : 4;
         w.P2 = (slots + strips - 1) / strips;
         const int r2 = w.P2 * small;
         if (r2 < d.NX / 2) w.R1 = d.NX - r2;
