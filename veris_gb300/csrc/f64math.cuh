@@ -113,4 +113,17 @@ __device__ __forceinline__ double rsqrt64(double x, unsigned m) {
     return 1.0 / sqrt(x);
 }
 
+// The same per lane, for code where the lanes that reach the call are not
+// known (data-dependent branches): the series where the operand is in the
+// seed range, IEEE otherwise (a warp whose lanes disagree runs both).
+__device__ __forceinline__ double div_lane(double a, double b) {
+    return seed_range(b) ? div_series(a, b) : a / b;
+}
+__device__ __forceinline__ double rcp_lane(double b) { return seed_range(b) ? rcp_series(b) : 1.0 / b; }
+__device__ __forceinline__ double sqrt_lane(double x) {
+    if (is_zero(x)) return x;
+    return seed_range(x) ? sqrt_series(x) : sqrt(x);
+}
+__device__ __forceinline__ double rsqrt_lane(double x) { return seed_range(x) ? rsqrt_series(x) : 1.0 / sqrt(x); }
+
 }  // namespace veris

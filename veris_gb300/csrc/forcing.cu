@@ -27,11 +27,37 @@
 // are multiplied by exactly zero, so they are skipped there.  A NULL output
 // pointer skips that output's store (the reference's own caller discards the
 // last three, seaice_global_4deg.py:761).
+//
+// Both routines are bound by GB300's float64 pipe in float64 (2 lanes per SM
+// and cycle): their divisions, reciprocals and square roots take the
+// series-refined hardware approximations of f64math.cuh (per lane, IEEE
+// where an operand leaves the safe range); float32 keeps IEEE-rounded
+// float32 arithmetic.
 #include <cmath>
 
 #include "common.cuh"
+#include "f64math.cuh"
 
 namespace veris {
+
+// division, reciprocal and square roots of each precision
+template <class T>
+struct Fm;
+template <>
+struct Fm<double> {
+    static __device__ __forceinline__ double root(double x) { return sqrt_lane(x); }
+    static __device__ __forceinline__ double rcp(double x) { return rcp_lane(x); }
+    static __device__ __forceinline__ double div(double a, double b) { return div_lane(a, b); }
+    // 1 / (a sqrt(x)) for a > 0, x > 0
+    static __device__ __forceinline__ double rnorm(double a, double x) { return rcp_lane(a) * rsqrt_lane(x); }
+};
+template <>
+struct Fm<float> {
+    static __device__ __forceinline__ float root(float x) { return sqrtf(x); }
+    static __device__ __forceinline__ float rcp(float x) { return 1.f / x; }
+    static __device__ __forceinline__ float div(float a, float b) { return a / b; }
+    static __device__ __forceinline__ float rnorm(float a, float x) { return 1.f / (a * sqrtf(x)); }
+};
 
 // rows per walk: float64 is bound by its arithmetic and walks long (fewer
 // C points solved twice); float32 is bound by memory latency and walks short,
@@ -55,21 +81,21 @@ __device__ __forceinline__ void fd_center(const FdArgs<T> &a, T tauX, T tauY, T 
     const T rhsX = -tauX - mIceCor * vOc;
     const T rhsY = -tauY + mIceCor * uOc;
     const T n2 = rhsX * rhsX + rhsY * rhsY;
-    const T rhsN = n2 > T(0) ? sqrt(n2) : T(0);
+    const T rhsN = n2 > T(0) ? Fm<T>::root(n2) : T(0);
     const bool south = f < T(0);
     const T t1 = south ? a.t1s : a.t1n;
     const T t1sq = t1 * t1;
     const T t2 = t1sq * (mIceCor * mIceCor);
     const T t3 = t1sq * (rhsN * rhsN);
     const T t4 = t2 * t2 + T(4) * t3;
-    const T solN = t3 > T(0) ? sqrt(T(0.5) * (sqrt(t4) - t2)) : T(0);
+    const T solN = t3 > T(0) ? Fm<T>::root(T(0.5) * (Fm<T>::root(t4) - t2)) : T(0);
     uC = uOc;
     vC = vOc;
     if (solN > T(0)) {
         // solN > 0 implies rhsN > 0 and p2 > 0: both angles are defined
         const T p2 = (south ? a.t1s_inv : a.t1n_inv) * (solN * solN);
         const T p3 = mIceCor * solN;
-        const T r = T(1) / (rhsN * sqrt(p2 * p2 + p3 * p3));
+        const T r = Fm<T>::rnorm(rhsN, p2 * p2 + p3 * p3);
         const T cosA = (rhsX * p2 + rhsY * p3) * r;
         const T sinA = (rhsY * p2 - rhsX * p3) * r;
         uC = uOc - solN * cosA;
@@ -133,7 +159,7 @@ struct BulkArgs {
     T *flwupa, *flha, *fsha, *df0dT, *ust, *vst, *evp, *ssq, *dEvdT;
     int64_t n;
     T zvir, cpdair, karman, latvap, emis, gamma_blk, rhoAir, stefBoltz, czol, aln, rdn;
-    T g, rlatvap;   // rdn / karman, 1 / latvap
+    T g, rlatvap, rzvir;   // rdn / karman, 1 / latvap, 1 / zvir
 };
 
 template <class T>
@@ -144,23 +170,23 @@ __global__ void __launch_bounds__(256) bulkf_kernel(BulkArgs<T> a) {
         const T uw = __ldg(a.uw + k), vw = __ldg(a.vw + k);
         const T ta = __ldg(a.ta + k), qa = __ldg(a.qa + k), tsf = __ldg(a.tsf + k);
         const T lath = a.latvap;
-        const T us = sqrt(uw * uw + vw * vw);
+        const T us = Fm<T>::root(uw * uw + vw * vw);
         const T usm = us > T(1) ? us : T(1);
         const T t0 = ta * (T(1) + a.zvir * qa);
-        const T rtsf = T(1) / tsf;
+        const T rtsf = Fm<T>::rcp(tsf);
         const T ssq = T(3.797915) * exp(lath * (T(7.93252e-6) - T(2.166847e-3) * rtsf)) * T(1.0 / 1013.0);
         const T deltap = ta - tsf + a.gamma_blk * ht;
         const T delq = qa - ssq;
-        const T qden = T(1) / a.zvir + qa;
+        const T qden = a.rzvir + qa;
         // With rd = rdn / Dm and rh = re = rdn / Dh (Dm = Dh = 1 before the
         // first iteration), ustar = rd usm, tstar = rh deltap, qstar = rh delq:
         //   huol = czol / ustar^2 (tstar / t0 + qstar / qden) = K Dm^2 / Dh,
         //   K = czol (deltap qden + delq t0) / (t0 qden usm^2 rdn)
         // one division per iteration instead of seven; rounding differs only.
-        const T K = a.czol * (deltap * qden + delq * t0) / (t0 * qden * (usm * usm) * a.rdn);
+        const T K = Fm<T>::div(a.czol * (deltap * qden + delq * t0), t0 * qden * (usm * usm) * a.rdn);
         T Dm = T(1), Dh = T(1);
         for (int it = 0; it < 5; ++it) {
-            T huol = it == 0 ? K : K * (Dm * Dm) / Dh;
+            T huol = it == 0 ? K : Fm<T>::div(K * (Dm * Dm), Dh);
             const T ah = fabs(huol);
             huol = (ah < T(10) ? ah : T(10)) * bk_sign(huol);
             T psimh, psixh;
@@ -168,9 +194,9 @@ __global__ void __launch_bounds__(256) bulkf_kernel(BulkArgs<T> a) {
                 psimh = psixh = T(-5) * huol;       // stable: the unstable terms carry a factor 0
             } else {
                 const T stable = T(0.5) + T(0.5) * bk_sign(huol);
-                const T sq = sqrt(fabs(T(1) - T(16) * huol));
+                const T sq = Fm<T>::root(fabs(T(1) - T(16) * huol));
                 const T xsq = sq > T(1) ? sq : T(1);
-                const T x = sqrt(xsq);
+                const T x = Fm<T>::root(xsq);
                 const T l2 = T(2) * log(T(0.5) * (T(1) + xsq));
                 psimh = T(-5) * huol * stable +
                         (T(1) - stable) * (T(2) * log(T(0.5) * (T(1) + x)) + l2 - T(2) * atan(x) + pi * T(0.5));
@@ -179,7 +205,7 @@ __global__ void __launch_bounds__(256) bulkf_kernel(BulkArgs<T> a) {
             Dm = T(1) + a.g * (a.aln - psimh);
             Dh = T(1) + a.g * (a.aln - psixh);
         }
-        const T rhrd = a.rdn * a.rdn / (Dm * Dh);   // rh rd (= re rd)
+        const T rhrd = Fm<T>::div(a.rdn * a.rdn, Dm * Dh);   // rh rd (= re rd)
         const T csha = a.rhoAir * a.cpdair * us * rhrd;
         const T clha = a.rhoAir * lath * us * rhrd;
         const T flha = clha * delq;
@@ -192,7 +218,7 @@ __global__ void __launch_bounds__(256) bulkf_kernel(BulkArgs<T> a) {
         if (a.df0dT) a.df0dT[k] = -(T(4) * a.emis * a.stefBoltz * t3) + (-csha) + (-lath * devdt);
         if (a.dEvdT) a.dEvdT[k] = devdt;
         if (a.ssq) a.ssq[k] = ssq;
-        const T cdn = T(2.7e-3) / usm + T(0.142e-3) + T(0.0764e-3) * usm;
+        const T cdn = Fm<T>::div(T(2.7e-3), usm) + T(0.142e-3) + T(0.0764e-3) * usm;
         const T ws = a.rhoAir * cdn * us;
         if (a.ust) a.ust[k] = ws * uw;
         if (a.vst) a.vst[k] = ws * vw;
@@ -252,6 +278,7 @@ static int bulkf(const VerisParams *p, int64_t n, const T *uw, const T *vw, cons
     a.rdn = T(p->karman / std::log(10.0 / 0.0005));
     a.g = T(p->karman / std::log(10.0 / 0.0005) / p->karman);
     a.rlatvap = T(1.0 / p->latvap);
+    a.rzvir = T(1) / a.zvir;
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
