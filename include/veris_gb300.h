@@ -647,6 +647,21 @@ int veris_check_finite_f32(const VerisGrid *g, const float *const *arrays, int32
 /* elementwise precision conversion of n values */
 int veris_convert_f64_to_f32(const double *src, float *dst, int64_t n, veris_stream_t s);
 int veris_convert_f32_to_f64(const float *src, double *dst, int64_t n, veris_stream_t s);
+/*
+ * No counterpart in the reference: a self-check of the float64 division,
+ * reciprocal and square roots that the float64 kernels take from the
+ * hardware's approximate reciprocal and reciprocal square root refined by
+ * the series of the exact correction (instead of IEEE division and square
+ * root).  For n operand pairs (a, b) in device memory it writes 8 planar
+ * arrays of n values to out: a/b, a/b, 1/b, 1/b, sqrt(b), sqrt(b),
+ * 1/sqrt(b), 1/sqrt(b), each pair in the warp-uniform form (a warp with any
+ * operand outside the safe range takes IEEE for all its lanes) and in the
+ * per-lane form.  Results are within one unit in the last place of the
+ * correctly rounded value (measured over 2^20 operands spanning 2^+-900);
+ * zeros, denormals, negatives, infinities and NaN give the IEEE results
+ * (sqrt of -0 in the warp form: +0 when the warp takes the series).
+ */
+int veris_f64_math_check(const double *a, const double *b, int64_t n, double *out, veris_stream_t s);
 
 #ifdef __cplusplus
 }

@@ -210,6 +210,7 @@ SIGNATURES = {
     "veris_check_finite_f32": ([_G, _P, ctypes.c_int32, ctypes.c_int32, _P, _P], _I),
     "veris_convert_f64_to_f32": ([_P, _P, _L, _P], _I),
     "veris_convert_f32_to_f64": ([_P, _P, _L, _P], _I),
+    "veris_f64_math_check": ([_P, _P, _L, _P, _P], _I),
 }
 
 _lib = None
