@@ -98,8 +98,9 @@ def parse():
     ap.add_argument("--evp-checkpoint-every", type=int, default=None,
                     help="EVP subcycle checkpoint interval inside a step's adjoint "
                          "(0: keep all; default: keep all when it fits in device memory)")
-    ap.add_argument("--tape", default="auto", choices=("auto", "on", "off"),
-                    help="keep every EVP subcycle state during the forward")
+    ap.add_argument("--tape", default="auto", choices=("auto", "on", "off", "step"),
+                    help="keep every EVP subcycle state during the forward (step: float32, one step's "
+                         "tape written during the reverse)")
     ap.add_argument("--adjoint-repeats", type=int, default=2)
     ap.add_argument("--no-fd", action="store_true", help="skip the centred-difference check of dL/dP*")
     ap.add_argument("--evp-alpha-beta", type=float, default=None,
@@ -912,7 +913,7 @@ def run_adjoint(args):
         sett.evpAlpha = sett.evpBeta = float(args.evp_alpha_beta)
     st = VerisState.from_numpy(arrays, sett)
     v = st.variables
-    tape = {"auto": "auto", "on": True, "off": False}[args.tape]
+    tape = {"auto": "auto", "on": True, "off": False, "step": "step"}[args.tape]
     torch.cuda.reset_peak_memory_stats()
     tr = Trajectory(st, n_steps, snapshots=args.snapshots, evp_checkpoint_every=args.evp_checkpoint_every,
                     tape=tape, precision=args.adjoint_precision)
@@ -988,7 +989,7 @@ def run_adjoint(args):
             "unit": "x", "higher_is_better": False, "dtype": args.adjoint_precision, "data": "synthetic",
             "config": {"workload": name, "nx": c["nx"], "ny": c["ny"], "steps": n_steps,
                        "subcycles": int(sett.nEVPsteps), "dt_s": c["dt"],
-                       "snapshots": tr.snaps, "evp_checkpoint_every": tr.K, "evp_tape": tr.tapes is not None,
+                       "snapshots": tr.snaps, "evp_checkpoint_every": tr.K, "evp_tape": tr.tape_mode,
                        "evpAlpha": float(sett.evpAlpha), "evpBeta": float(sett.evpBeta),
                        "target": "P* x 1.2 and seed+1 winds", "loss": "interior sum (u-u*)^2+(v-v*)^2+(A-A*)^2"},
             "forward_ms": t_fwd, "forward_with_snapshots_ms": t_f2, "adjoint_ms": t_adj,

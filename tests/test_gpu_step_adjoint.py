@@ -339,6 +339,74 @@ def test_trajectory_autograd_function():
     assert G.rel_err(A0.grad.cpu().numpy(), g["Area"].cpu().numpy()) <= 1e-12
 
 
+@pytest.mark.parametrize("rows,variant", ((0, 0), (16, 1), (32, 2), (8, 3)))
+def test_float32_tape_is_the_walks_trajectory(rows, variant):
+    """The float32 tape (veris_evp_fast_tape_f32, automatic walk length,
+    variant 0) holds the states the engine's tuned walk computes: its final
+    state equals the walk solver's bit for bit for any walk length and
+    register variant, so a tape written during the reverse sweep linearises
+    the forward's own trajectory."""
+    import ctypes
+    from veris_gb300.evp_solver import evp_solver_fast
+    from veris_gb300.state import Call
+    from veris_gb300._abi import check
+    st = _trajectory_state()
+    want = evp_solver_fast(st, "f32", form="walk", n_subcycles=N_SUB, rows=rows, variant=variant)
+    c = Call(st)
+    g = c.refs()[0]
+    tape = torch.empty(int(c.lib.veris_evp_tape_bytes(g, 4, N_SUB)) // 4, dtype=torch.float32, device=c.device)
+    out = [torch.empty(c.shape, dtype=torch.float32, device=c.device) for _ in range(5)]
+    ws, wsb = c.workspace(c.lib.veris_evp_fast_workspace_bytes(g, 4))
+    check("evp_tape_f32", c.lib.veris_evp_fast_tape_f32(*c.refs(), N_SUB, *[t.data_ptr() for t in out],
+                                                         tape.data_ptr(), tape.numel() * 4, ws, wsb, c.stream))
+    torch.cuda.synchronize()
+    for a, b in zip(out, want):
+        assert torch.equal(a, b)
+
+
+def test_float32_step_tape_gives_the_all_steps_gradients():
+    """tape="step" (one step's tape written by the walk during the reverse)
+    against the tapes of all steps written during the forward: the same
+    state gradients bit for bit and the same coefficient gradients up to the
+    order of the per-warp drag sums' atomics, with the gather passes (the
+    tile kernel this small grid would take sums with shared-memory atomics,
+    so no two of its runs agree bit for bit); the shared-memory recompute
+    (tape off) within float32 rounding of them."""
+    from veris_gb300 import _abi
+    from veris_gb300.trajectory import Trajectory, tracking_loss_adjoint
+    lib = _abi.load()
+    assert lib.veris_evp_adjoint_f32_form(2) == 0
+    try:
+        _step_tape_case()
+    finally:
+        lib.veris_evp_adjoint_f32_form(0)
+
+
+def _step_tape_case():
+    from veris_gb300.trajectory import Trajectory, tracking_loss_adjoint
+    rng = np.random.default_rng(11)
+    st = _trajectory_state()
+    v = st.variables
+    names = ("uIce", "vIce", "sigma1", "sigma2", "sigma12", "hIceMean", "hSnowMean", "Area", "TSurf")
+    x0 = {k: getattr(v, k).clone() for k in names}
+    target = {k: (getattr(v, k) + 0.01 * _rand(rng, v.iceMask) * v.iceMask).clone() for k in ("uIce", "vIce", "Area")}
+    res = {}
+    for tape in (True, "step", False):
+        for k, t in x0.items():
+            getattr(v, k).copy_(t)
+        tr = Trajectory(st, N_STEPS, n_subcycles=N_SUB, precision="f32", tape=tape)
+        assert tr.tape_mode == {True: "all", "step": "step", False: "off"}[tape]
+        tr.forward()
+        L, lam = tracking_loss_adjoint(st, target)
+        res[tape] = tr.backward(lam)
+    (ga, ca, _), (gs, cs, _), (go, co, _) = res[True], res["step"], res[False]
+    for k in ga:
+        assert torch.equal(ga[k], gs[k]), k
+    for k in ca:
+        assert abs(float(cs[k]) - float(ca[k])) <= 1e-12 * max(abs(float(ca[k])), 1e-30), (k, cs[k], ca[k])
+        assert abs(float(co[k]) - float(ca[k])) <= 5e-3 * max(abs(float(ca[k])), 1e-30), (k, co[k], ca[k])
+
+
 @pytest.mark.parametrize("tape", (True, False))
 def test_float32_trajectory_gradients(tape):
     """The float32 trajectory (float32 EVP and advection forward, float32 EVP

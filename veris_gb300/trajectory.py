@@ -78,7 +78,12 @@ class Trajectory:
         keep every EVP subcycle state of every step during the forward, so
         the adjoint recomputes no subcycle ("auto": when every step is
         snapshotted and the tapes fit in ``tape_memory_fraction`` of the free
-        device memory).  ``precision`` "f32": the forward is the engine's
+        device memory).  ``tape="step"`` (float32 only): the reverse sweep
+        writes the tape of one step at a time with the float32 register
+        walk, just before that step's EVP adjoint, instead of the adjoint
+        recomputing the subcycles in the shared-memory float32 form (3.7x
+        slower per subcycle on 3600 x 1800); "auto" takes it for float32
+        when the tapes of all steps do not fit and one does.  ``precision`` "f32": the forward is the engine's
         float32 step (float32 EVP and advection, float64 thermodynamics) and
         the EVP adjoint runs in float32; the other adjoints stay float64.
         ``evp_checkpoint_every``: without tapes, the EVP adjoint of a step
@@ -145,12 +150,28 @@ class Trajectory:
         f32 = precision == "f32"
         esize = 4 if f32 else 8
         tape_bytes = int(self.lib.veris_evp_tape_bytes(g, esize, self.eng.n_sub))
+        taped_ws = int(self.lib.veris_evp_adjoint_taped_workspace_bytes_f32(g, self.eng.n_sub) if f32 else
+                       self.lib.veris_evp_adjoint_taped_workspace_bytes(g, self.eng.n_sub))
         if tape == "auto":
             free = torch.cuda.mem_get_info(dev)[0]
-            tape = self.snaps == self.n - 1 and (self.n + 1) * tape_bytes <= tape_memory_fraction * free
+            if self.snaps == self.n - 1 and (self.n + 1) * tape_bytes <= tape_memory_fraction * free:
+                tape = True
+            elif f32 and tape_bytes + taped_ws <= tape_memory_fraction * free:
+                tape = "step"
+            else:
+                tape = False
+        elif tape == "step":
+            if not f32:
+                raise ValueError("tape='step' is a float32 form (the float64 adjoint's one-segment recompute "
+                                 "already runs the forward's own kernel)")
         elif tape and self.snaps != self.n - 1:
             raise ValueError("taping needs every step snapshotted (snapshots=None)")
+        self.tape_mode = "step" if tape == "step" else ("all" if tape else "off")
         tdt = torch.float32 if f32 else torch.float64
+        # one tape, rewritten by every step's reverse
+        self.step_tape = torch.empty(tape_bytes // esize, dtype=tdt, device=dev) if tape == "step" else None
+        if tape == "step":
+            tape = False
         self.tapes = ([torch.empty(tape_bytes // esize, dtype=tdt, device=dev) for _ in range(self.n)]
                       if tape else None)
         # the taped step is one CUDA graph writing this staging tape, copied
@@ -158,9 +179,8 @@ class Trajectory:
         # addresses; the copy costs less than launching the step eagerly)
         self.tape_stage = torch.empty_like(self.tapes[0]) if tape else None
         self._tape_graph = None
-        if tape:
-            wsb = (self.lib.veris_evp_adjoint_taped_workspace_bytes_f32(g, self.eng.n_sub) if f32 else
-                   self.lib.veris_evp_adjoint_taped_workspace_bytes(g, self.eng.n_sub))
+        if tape or self.step_tape is not None:
+            wsb = taped_ws
         else:
             if self._auto_K:
                 self.K = self._fitting_checkpoint_spacing(g, esize, tape_memory_fraction)
@@ -386,8 +406,14 @@ class Trajectory:
                                                               lo32[q].numel(), st))
             lo_ptrs = [t.data_ptr() for t in lo32]
             li_ptrs = [t.data_ptr() for t in li32]
-            if self.tapes is not None:
-                tape = self.tapes[step]
+            tape = self.tapes[step] if self.tapes is not None else self.step_tape
+            if tape is self.step_tape and tape is not None:
+                # this step's subcycles from its start state, as the forward ran them (the register
+                # walk; the final state lands in the adjoint's input buffers, which it overwrites)
+                check("evp_tape_f32", lib.veris_evp_fast_tape_f32(
+                    *base, eng.n_sub, *li_ptrs, tape.data_ptr(), tape.numel() * 4, eng.ws_evp.data_ptr(),
+                    eng.ws_evp.numel(), st))
+            if tape is not None:
                 check("evp_adjoint_taped_f32", lib.veris_evp_adjoint_taped_f32(
                     *base, eng.n_sub, tape.data_ptr(), tape.numel() * 4, *lo_ptrs, *li_ptrs,
                     ctypes.byref(self.t_lf), self.evp_scal.data_ptr(), self.ws_evp.data_ptr(), self.ws_evp.numel(),
