@@ -429,6 +429,38 @@ def test_float64_tile_heights_give_the_same_values_and_the_tuner_picks_one():
         lib.veris_evp_f64_tile_rows(0)
 
 
+@pytest.mark.parametrize("nx,ny", ((1203, 611), (4001, 97)))
+def test_f64_units_on_large_odd_grids(nx, ny):
+    """Grids where every unit height leaves a last round of small pieces at
+    the bottom of each strip (more full pieces than resident CTA slots):
+    16-, 24- and 32-row units give the same values bit for bit, and those
+    match the plain float64 loop to 1e-10."""
+    from veris_gb300 import _abi
+    from veris_gb300.evp_solver import evp_solver
+    from veris_gb300.state import Call
+    st = _prepared(nx, ny, nx + ny)
+    lib = _abi.load()
+    c = Call(st)
+    ws, wsb = c.workspace(lib.veris_evp_fast_workspace_bytes(c.refs()[0], 8))
+    n = 6
+    res = []
+    try:
+        for rows in (16, 24, 32):
+            assert lib.veris_evp_f64_tile_rows(rows) == 0
+            out = c.empty(5)
+            assert lib.veris_evp_fast_solver_f64(*c.refs(), n, *[t.data_ptr() for t in out], ws, wsb, c.stream) == 0
+            res.append(out)
+    finally:
+        lib.veris_evp_f64_tile_rows(0)
+    for out in res[1:]:
+        for a, b in zip(out, res[0]):
+            assert torch.equal(a, b)
+    ref = evp_solver(st, n)
+    for k in range(5):
+        e = G.rel_err(res[0][k].cpu().numpy(), ref[k].cpu().numpy())
+        assert e <= 1e-10, (k, e)
+
+
 _TURN = dict(waterTurnAngle=15.0, sinWat=float(np.sin(np.radians(15.0))), cosWat=float(np.cos(np.radians(15.0))))
 
 
