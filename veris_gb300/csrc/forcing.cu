@@ -31,8 +31,12 @@
 // Both routines are bound by GB300's float64 pipe in float64 (2 lanes per SM
 // and cycle): their divisions, reciprocals and square roots take the
 // series-refined hardware approximations of f64math.cuh (per lane, IEEE
-// where an operand leaves the safe range); float32 keeps IEEE-rounded
-// float32 arithmetic.
+// where an operand leaves the safe range).  In float32 the bulk formula is
+// bound by instruction issue: its divisions, logarithms, exponential and the
+// square roots of the psi functions use the hardware approximations
+// (__fdividef, __logf, __expf, rsqrtf: a few units in
+// the last place, inside the float32 forms' 1e-4 bound against the
+// reference); the free drift keeps IEEE-rounded float32 arithmetic.
 #include <cmath>
 
 #include "common.cuh"
@@ -45,7 +49,11 @@ template <class T>
 struct Fm;
 template <>
 struct Fm<double> {
+    static __device__ __forceinline__ double log(double x) { return ::log(x); }
+    static __device__ __forceinline__ double exp(double x) { return ::exp(x); }
+    static __device__ __forceinline__ double fdiv(double a, double b) { return div_lane(a, b); }
     static __device__ __forceinline__ double root(double x) { return sqrt_lane(x); }
+    static __device__ __forceinline__ double root_ge1(double x) { return sqrt_lane(x); }
     static __device__ __forceinline__ double rcp(double x) { return rcp_lane(x); }
     static __device__ __forceinline__ double div(double a, double b) { return div_lane(a, b); }
     // 1 / (a sqrt(x)) for a > 0, x > 0
@@ -53,7 +61,12 @@ struct Fm<double> {
 };
 template <>
 struct Fm<float> {
+    static __device__ __forceinline__ float log(float x) { return __logf(x); }
+    static __device__ __forceinline__ float exp(float x) { return __expf(x); }
+    static __device__ __forceinline__ float fdiv(float a, float b) { return __fdividef(a, b); }
     static __device__ __forceinline__ float root(float x) { return sqrtf(x); }
+    // x >= 1: the approximate reciprocal square root times x (a few ulps)
+    static __device__ __forceinline__ float root_ge1(float x) { return x * rsqrtf(x); }
     static __device__ __forceinline__ float rcp(float x) { return 1.f / x; }
     static __device__ __forceinline__ float div(float a, float b) { return a / b; }
     static __device__ __forceinline__ float rnorm(float a, float x) { return 1.f / (a * sqrtf(x)); }
@@ -173,8 +186,8 @@ __global__ void __launch_bounds__(256) bulkf_kernel(BulkArgs<T> a) {
         const T us = Fm<T>::root(uw * uw + vw * vw);
         const T usm = us > T(1) ? us : T(1);
         const T t0 = ta * (T(1) + a.zvir * qa);
-        const T rtsf = Fm<T>::rcp(tsf);
-        const T ssq = T(3.797915) * exp(lath * (T(7.93252e-6) - T(2.166847e-3) * rtsf)) * T(1.0 / 1013.0);
+        const T rtsf = Fm<T>::fdiv(T(1), tsf);
+        const T ssq = T(3.797915) * Fm<T>::exp(lath * (T(7.93252e-6) - T(2.166847e-3) * rtsf)) * T(1.0 / 1013.0);
         const T deltap = ta - tsf + a.gamma_blk * ht;
         const T delq = qa - ssq;
         const T qden = a.rzvir + qa;
@@ -183,10 +196,10 @@ __global__ void __launch_bounds__(256) bulkf_kernel(BulkArgs<T> a) {
         //   huol = czol / ustar^2 (tstar / t0 + qstar / qden) = K Dm^2 / Dh,
         //   K = czol (deltap qden + delq t0) / (t0 qden usm^2 rdn)
         // one division per iteration instead of seven; rounding differs only.
-        const T K = Fm<T>::div(a.czol * (deltap * qden + delq * t0), t0 * qden * (usm * usm) * a.rdn);
+        const T K = Fm<T>::fdiv(a.czol * (deltap * qden + delq * t0), t0 * qden * (usm * usm) * a.rdn);
         T Dm = T(1), Dh = T(1);
         for (int it = 0; it < 5; ++it) {
-            T huol = it == 0 ? K : Fm<T>::div(K * (Dm * Dm), Dh);
+            T huol = it == 0 ? K : Fm<T>::fdiv(K * (Dm * Dm), Dh);
             const T ah = fabs(huol);
             huol = (ah < T(10) ? ah : T(10)) * bk_sign(huol);
             T psimh, psixh;
@@ -194,18 +207,18 @@ __global__ void __launch_bounds__(256) bulkf_kernel(BulkArgs<T> a) {
                 psimh = psixh = T(-5) * huol;       // stable: the unstable terms carry a factor 0
             } else {
                 const T stable = T(0.5) + T(0.5) * bk_sign(huol);
-                const T sq = Fm<T>::root(fabs(T(1) - T(16) * huol));
+                const T sq = Fm<T>::root_ge1(fabs(T(1) - T(16) * huol));   // huol <= 0: at least 1
                 const T xsq = sq > T(1) ? sq : T(1);
-                const T x = Fm<T>::root(xsq);
-                const T l2 = T(2) * log(T(0.5) * (T(1) + xsq));
+                const T x = Fm<T>::root_ge1(xsq);
+                const T l2 = T(2) * Fm<T>::log(T(0.5) * (T(1) + xsq));
                 psimh = T(-5) * huol * stable +
-                        (T(1) - stable) * (T(2) * log(T(0.5) * (T(1) + x)) + l2 - T(2) * atan(x) + pi * T(0.5));
+                        (T(1) - stable) * (T(2) * Fm<T>::log(T(0.5) * (T(1) + x)) + l2 - T(2) * atan(x) + pi * T(0.5));
                 psixh = T(-5) * huol * stable + (T(1) - stable) * l2;
             }
             Dm = T(1) + a.g * (a.aln - psimh);
             Dh = T(1) + a.g * (a.aln - psixh);
         }
-        const T rhrd = Fm<T>::div(a.rdn * a.rdn, Dm * Dh);   // rh rd (= re rd)
+        const T rhrd = Fm<T>::fdiv(a.rdn * a.rdn, Dm * Dh);   // rh rd (= re rd)
         const T csha = a.rhoAir * a.cpdair * us * rhrd;
         const T clha = a.rhoAir * lath * us * rhrd;
         const T flha = clha * delq;
@@ -218,7 +231,7 @@ __global__ void __launch_bounds__(256) bulkf_kernel(BulkArgs<T> a) {
         if (a.df0dT) a.df0dT[k] = -(T(4) * a.emis * a.stefBoltz * t3) + (-csha) + (-lath * devdt);
         if (a.dEvdT) a.dEvdT[k] = devdt;
         if (a.ssq) a.ssq[k] = ssq;
-        const T cdn = Fm<T>::div(T(2.7e-3), usm) + T(0.142e-3) + T(0.0764e-3) * usm;
+        const T cdn = Fm<T>::fdiv(T(2.7e-3), usm) + T(0.142e-3) + T(0.0764e-3) * usm;
         const T ws = a.rhoAir * cdn * us;
         if (a.ust) a.ust[k] = ws * uw;
         if (a.vst) a.vst[k] = ws * vw;
