@@ -412,10 +412,14 @@ int veris_evp_adjoint_taped_f64(const VerisGrid *g, const VerisParams *p, const 
 
 /*
  * Float32 forms of the same: the tape holds float32 states written by the
- * register-walking float32 kernel (the engine's float32 forward); the
- * adjoint kernel linearises the fast form with exact square root and
- * division at those states.  The adjoints of the five states are float32,
- * those of the constants and the drag coefficients float64.
+ * register-walking float32 kernel (the engine's float32 forward), eight
+ * arrays per slot: the walk's (uIce, vIce, sigma1, sigma2) per point over
+ * four arrays and sigma12 after k subcycles, then the Delta, zeta and
+ * ocean-drag coefficient the walk computed in subcycle k + 1 (constant
+ * alpha; the walk's own values, which the adjoint's gather passes read
+ * instead of recomputing them).  The adjoint linearises the fast form at
+ * those states.  The adjoints of the five states are float32, those of the
+ * constants and the drag coefficients float64.
  */
 int veris_evp_fast_tape_f32(const VerisGrid *g, const VerisParams *p, const VerisFieldsF64 *vs,
                             int32_t n_subcycles, float *uIce, float *vIce, float *sigma1,

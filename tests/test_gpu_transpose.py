@@ -77,13 +77,14 @@ def test_adjoint_is_the_transpose_of_the_tangent(case, golden):
 
 
 @pytest.mark.parametrize("golden", ["moving", "c1"])
-@pytest.mark.parametrize("form", [1, 2])
-def test_float32_evp_adjoint_is_the_transpose_to_float32_rounding(golden, form):
+@pytest.mark.parametrize("form,tape", [(1, False), (2, False), (2, True)])
+def test_float32_evp_adjoint_is_the_transpose_to_float32_rounding(golden, form, tape):
     """The float32 EVP adjoint (form 1: the tile kernel; 2: the gather passes,
-    which recompute Delta, zeta and cDrag in float32) against the float64
-    oracle's exact tangent: <J dx, w> = <dx, J^T w> to float32 rounding of
-    the state, the linearisation and the adjoint sweep (bar 1e-4 of the
-    magnitude of the terms)."""
+    which recompute Delta, zeta and cDrag in float32, or with ``tape`` read
+    the register walk's own from its tape) against the float64 oracle's exact
+    tangent: <J dx, w> = <dx, J^T w> to float32 rounding of the state, the
+    linearisation and the adjoint sweep (bar 1e-4 of the magnitude of the
+    terms)."""
     from veris_gb300 import _abi
     from veris_gb300 import adjoint as A
     from veris_gb300.state import VerisState
@@ -100,7 +101,7 @@ def test_float32_evp_adjoint_is_the_transpose_to_float32_rounding(golden, form):
     lam = {k: torch.as_tensor(w[k], device="cuda") for k in outs}
     try:
         assert lib.veris_evp_adjoint_f32_form(form) == 0
-        state, fields, _drag = A.evp_adjoint(gst, lam, n_subcycles=3, precision="f32")
+        state, fields, _drag = A.evp_adjoint(gst, lam, n_subcycles=3, precision="f32", tape=tape)
     finally:
         lib.veris_evp_adjoint_f32_form(0)
     adj = dict(state, **fields)
@@ -109,7 +110,8 @@ def test_float32_evp_adjoint_is_the_transpose_to_float32_rounding(golden, form):
     rhs = sum(float(t.sum()) for t in rhs_terms)
     mag = sum(float(np.abs(t).sum()) for t in lhs_terms + rhs_terms)
     assert mag > 0
-    assert abs(lhs - rhs) <= 1e-4 * mag, f"evp f32 form {form}/{golden}: {lhs:.9e} vs {rhs:.9e} ({abs(lhs - rhs) / mag:.2e})"
+    assert abs(lhs - rhs) <= 1e-4 * mag, \
+        f"evp f32 form {form} tape {tape}/{golden}: {lhs:.9e} vs {rhs:.9e} ({abs(lhs - rhs) / mag:.2e})"
     assert lib.veris_evp_adjoint_f32_form(3) != 0
 
 

@@ -21,7 +21,7 @@ EVP_FIELDS = ("SeaIceStrength", "SeaIceMassC", "SeaIceMassU", "SeaIceMassV", "Wi
               "AreaW", "AreaS", "uOcean", "vOcean", "hIceMean", "Area")
 
 
-def evp_adjoint(state, lam_out, n_subcycles=None, checkpoint_every=0, precision="f64"):
+def evp_adjoint(state, lam_out, n_subcycles=None, checkpoint_every=0, precision="f64", tape=False):
     """Reverse-mode derivative of ``n_subcycles`` EVP subcycles.
 
     ``lam_out``: {name: float64 CUDA tensor} adjoints of uIce, vIce, sigma1,
@@ -29,7 +29,9 @@ def evp_adjoint(state, lam_out, n_subcycles=None, checkpoint_every=0, precision=
     (adjoints of the initial state {name: tensor}, adjoints of the constant
     fields {name: tensor}, {"waterIceDrag": float tensor, "waterIceDrag_south": ...}).
     ``precision`` "f32": the float32 loop (its forward recomputed in float32,
-    the state adjoints float32, returned as float64 tensors).
+    the state adjoints float32, returned as float64 tensors).  ``tape``: run
+    the fast forward with its tape first (the float32 one is the register
+    walk: cell areas varying along j only) and the adjoint on that tape.
     """
     s = state.settings
     n = int(s.nEVPsteps if n_subcycles is None else n_subcycles)
@@ -43,11 +45,26 @@ def evp_adjoint(state, lam_out, n_subcycles=None, checkpoint_every=0, precision=
     lf = {k: zeros() for k in EVP_FIELDS}
     table = VerisFields(**{k: t.data_ptr() for k, t in lf.items()})
     scal = torch.zeros(2, dtype=torch.float64, device=c.device)
-    wsb = c.lib.veris_evp_adjoint_workspace_bytes(c.refs()[0], 4 if f32 else 8, n, int(checkpoint_every))
-    ws, wsb = c.workspace(wsb)
-    fn = c.lib.veris_evp_adjoint_f32 if f32 else c.lib.veris_evp_adjoint_f64
-    check("evp_adjoint", fn(*c.refs(), n, int(checkpoint_every), *lo, *[t.data_ptr() for t in li],
-                            ctypes.byref(table), scal.data_ptr(), ws, wsb, c.stream))
+    esize = 4 if f32 else 8
+    if tape:
+        g = c.refs()[0]
+        tb = int(c.lib.veris_evp_tape_bytes(g, esize, n))
+        tp = torch.empty(tb // esize, dtype=dt, device=c.device)
+        outs = [torch.empty(c.shape, dtype=dt, device=c.device) for _ in EVP_STATE]
+        fws, fwsb = c.workspace(c.lib.veris_evp_fast_workspace_bytes(g, esize))
+        fwd = c.lib.veris_evp_fast_tape_f32 if f32 else c.lib.veris_evp_fast_tape_f64
+        check("evp_tape", fwd(*c.refs(), n, *[t.data_ptr() for t in outs], tp.data_ptr(), tb, fws, fwsb, c.stream))
+        ws, wsb = c.workspace(c.lib.veris_evp_adjoint_taped_workspace_bytes_f32(g, n) if f32 else
+                              c.lib.veris_evp_adjoint_taped_workspace_bytes(g, n))
+        fn = c.lib.veris_evp_adjoint_taped_f32 if f32 else c.lib.veris_evp_adjoint_taped_f64
+        check("evp_adjoint_taped", fn(*c.refs(), n, tp.data_ptr(), tb, *lo, *[t.data_ptr() for t in li],
+                                      ctypes.byref(table), scal.data_ptr(), ws, wsb, c.stream))
+    else:
+        wsb = c.lib.veris_evp_adjoint_workspace_bytes(c.refs()[0], esize, n, int(checkpoint_every))
+        ws, wsb = c.workspace(wsb)
+        fn = c.lib.veris_evp_adjoint_f32 if f32 else c.lib.veris_evp_adjoint_f64
+        check("evp_adjoint", fn(*c.refs(), n, int(checkpoint_every), *lo, *[t.data_ptr() for t in li],
+                                ctypes.byref(table), scal.data_ptr(), ws, wsb, c.stream))
     return (dict(zip(EVP_STATE, [t.double() for t in li])), lf,
             {"waterIceDrag": scal[0], "waterIceDrag_south": scal[1]})
 

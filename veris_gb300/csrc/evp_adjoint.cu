@@ -635,9 +635,11 @@ static size_t plan(const Dims &d, int n, int K, char *base, Plan<T> *pl, bool ta
     return off;
 }
 
+// field q of slot s: the checkpoints and segments hold 5 fields per slot, a
+// forward's tape tape_slot_fields
 template <class T>
-static T *slot(T *base, size_t field, int s, int q) {
-    return reinterpret_cast<T *>(reinterpret_cast<char *>(base) + ((size_t)s * 5 + q) * field);
+static T *slot(T *base, size_t field, int s, int q, int width = 5) {
+    return reinterpret_cast<T *>(reinterpret_cast<char *>(base) + ((size_t)s * width + q) * field);
 }
 
 template <class T>
@@ -675,7 +677,9 @@ static int evp_adjoint(const VerisGrid *g, const VerisParams *p, const VerisFiel
     Plan<T> pl;
     VERIS_REQUIRE(ws && wsb >= plan<T>(d, n, K, nullptr, &pl, taped), VERIS_ERR_WORKSPACE);
     plan<T>(d, n, K, static_cast<char *>(ws), &pl, taped);
-    if (taped) VERIS_REQUIRE(tape_bytes >= (size_t)(n + 1) * 5 * pl.field, VERIS_ERR_WORKSPACE);
+    // slot width of the states the sweep reads: a tape's, or the segment's
+    const int W = taped ? tape_slot_fields<T>() : 5;
+    if (taped) VERIS_REQUIRE(tape_bytes >= (size_t)(n + 1) * W * pl.field, VERIS_ERR_WORKSPACE);
     cudaStream_t st = (cudaStream_t)s;
     const int64_t lp = internal_pitch(d.NY);
     const Fields<double> &f = *reinterpret_cast<const Fields<double> *>(vs);
@@ -760,15 +764,18 @@ static int evp_adjoint(const VerisGrid *g, const VerisParams *p, const VerisFiel
                 // Delta, zeta and cDrag
                 const bool quad = taped && sizeof(T) == 4;
                 TapeG<T> tt;
-                tt.u = slot(segb, pl.field, rs, 0);
-                tt.v = quad ? tt.u + 1 : slot(segb, pl.field, rs, 1);
-                tt.un = slot(segb, pl.field, rs + 1, 0);
-                tt.vn = quad ? tt.un + 1 : slot(segb, pl.field, rs + 1, 1);
+                tt.u = slot(segb, pl.field, rs, 0, W);
+                tt.v = quad ? tt.u + 1 : slot(segb, pl.field, rs, 1, W);
+                tt.un = slot(segb, pl.field, rs + 1, 0, W);
+                tt.vn = quad ? tt.un + 1 : slot(segb, pl.field, rs + 1, 1, W);
                 tt.sst = quad ? 4 : 1;
-                const bool rich = sizeof(T) == 8;
-                tt.del = rich ? slot(segb, pl.field, rs, 2) : nullptr;
-                tt.zeta = rich ? slot(segb, pl.field, rs, 3) : nullptr;
-                tt.cd = rich ? slot(segb, pl.field, rs, 4) : nullptr;
+                // Delta, zeta, cDrag: a float64 slot's fields 2-4, a float32 tape's 5-7 (the walk's
+                // own values); a float32 segment has none and the passes recompute them
+                const int qd = sizeof(T) == 8 ? 2 : 5;
+                const bool rich = sizeof(T) == 8 || quad;
+                tt.del = rich ? slot(segb, pl.field, rs, qd, W) : nullptr;
+                tt.zeta = rich ? slot(segb, pl.field, rs, qd + 1, W) : nullptr;
+                tt.cd = rich ? slot(segb, pl.field, rs, qd + 2, W) : nullptr;
                 LamG<T> ll;
                 if (first) {
                     ll.lu = lout[0]; ll.lv = lout[1]; ll.ls1 = lout[2]; ll.ls2 = lout[3]; ll.ls12 = lout[4];
@@ -793,13 +800,13 @@ static int evp_adjoint(const VerisGrid *g, const VerisParams *p, const VerisFiel
                 // layout: (u, v, sigma1, sigma2) per point over the slot's first
                 // four fields
                 const bool quad = taped && sizeof(T) == 4;
-                io.u = slot(segb, pl.field, rs, 0);
-                io.v = quad ? io.u + 1 : slot(segb, pl.field, rs, 1);
-                io.s1 = slot(segb, pl.field, rs, 2);
-                io.s2 = slot(segb, pl.field, rs, 3);
-                io.s12 = slot(segb, pl.field, rs, 4);
-                io.un = slot(segb, pl.field, rs + 1, 0);
-                io.vn = quad ? io.un + 1 : slot(segb, pl.field, rs + 1, 1);
+                io.u = slot(segb, pl.field, rs, 0, W);
+                io.v = quad ? io.u + 1 : slot(segb, pl.field, rs, 1, W);
+                io.s1 = slot(segb, pl.field, rs, 2, W);
+                io.s2 = slot(segb, pl.field, rs, 3, W);
+                io.s12 = slot(segb, pl.field, rs, 4, W);
+                io.un = slot(segb, pl.field, rs + 1, 0, W);
+                io.vn = quad ? io.un + 1 : slot(segb, pl.field, rs + 1, 1, W);
                 io.sst = quad ? 4 : 1;
                 io.ldn = lp;
                 if (first) {

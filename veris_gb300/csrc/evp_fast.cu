@@ -253,12 +253,13 @@ template int fast_subcycle<double>(const Dims &, const HaloFill &, const FastCon
 template <class T>
 static size_t tape_field(const Dims &d) { return rup256((size_t)d.NX * internal_pitch(d.NY) * sizeof(T)); }
 
-// tape != nullptr: every subcycle is kept, slot k (5 arrays of tape_field
-// bytes each, pitch lp) holding the state after k subcycles; in float64
-// slot k holds (u_k, v_k, Delta_k, zeta_k, cDrag_k), the velocities after
-// k subcycles and the viscosity and drag terms subcycle k + 1 computes from
-// them (the adjoint needs no stresses; they run in the workspace's state
-// buffers)
+// tape != nullptr: every subcycle is kept, slot k (tape_slot_fields arrays
+// of tape_field bytes each, pitch lp) holding the state after k subcycles;
+// in float64 slot k holds (u_k, v_k, Delta_k, zeta_k, cDrag_k), the
+// velocities after k subcycles and the viscosity and drag terms subcycle
+// k + 1 computes from them (the adjoint needs no stresses; they run in the
+// workspace's state buffers); in float32 the register walk's state after k
+// subcycles, then Delta_k, zeta_k, cDrag_k (constant alpha)
 template <class T>
 static int evp_fast(const VerisGrid *g, const VerisParams *p, const VerisFieldsF64 *vs64, int n, T *uo, T *vo,
                     T *s1o, T *s2o, T *s12o, void *ws, size_t wsb, int allow_tma, veris_stream_t s,
@@ -285,8 +286,9 @@ static int evp_fast(const VerisGrid *g, const VerisParams *p, const VerisFieldsF
     const Fields<double> &f = *reinterpret_cast<const Fields<double> *>(vs64);
     const bool basal = p->basalDragK2 != 0.0, turn = p->sinWat != 0.0;
     const size_t tf = tape_field<T>(d);
-    if (tape) VERIS_REQUIRE(tape_bytes >= (size_t)(n + 1) * 5 * tf, VERIS_ERR_WORKSPACE);
-    auto tslot = [&](int sl, int q) { return reinterpret_cast<T *>(reinterpret_cast<char *>(tape) + ((size_t)sl * 5 + q) * tf); };
+    constexpr int W = tape_slot_fields<T>();
+    if (tape) VERIS_REQUIRE(tape_bytes >= (size_t)(n + 1) * W * tf, VERIS_ERR_WORKSPACE);
+    auto tslot = [&](int sl, int q) { return reinterpret_cast<T *>(reinterpret_cast<char *>(tape) + ((size_t)sl * W + q) * tf); };
     // float64 tapes: the stresses stay in the workspace's state buffers
     constexpr bool rich = sizeof(T) == 8;
     T *s0[5];
@@ -312,9 +314,10 @@ static int evp_fast(const VerisGrid *g, const VerisParams *p, const VerisFieldsF
                                                {nullptr, nullptr, nullptr, nullptr, nullptr}};
                     float *const to[5] = {tslot(it + 1, 0), tslot(it + 1, 1), tslot(it + 1, 2), tslot(it + 1, 3),
                                           tslot(it + 1, 4)};
+                    float *const rich[3] = {tslot(it, 5), tslot(it, 6), tslot(it, 7)};
                     if ((stt = evp_walk_subcycles(adapt, true, d, h, c, k, from, to, lp, 1, basal, turn,
-                                                  allow_tma < 0 ? 0 : allow_tma, walk_variant, st, true)) !=
-                        VERIS_OK)
+                                                  allow_tma < 0 ? 0 : allow_tma, walk_variant, st, true, nullptr,
+                                                  adapt ? nullptr : rich)) != VERIS_OK)
                         return stt;
                     done = true;
                 }
@@ -440,8 +443,8 @@ int veris_evp_fast_solver_f64(const VerisGrid *g, const VerisParams *p, const Ve
 size_t veris_evp_tape_bytes(const VerisGrid *g, int32_t elem_size, int32_t n) {
     Dims d;
     if (check_grid(g, &d) != VERIS_OK || n < 1) return 0;
-    if (elem_size == 8) return (size_t)(n + 1) * 5 * tape_field<double>(d);
-    if (elem_size == 4) return (size_t)(n + 1) * 5 * tape_field<float>(d);
+    if (elem_size == 8) return (size_t)(n + 1) * tape_slot_fields<double>() * tape_field<double>(d);
+    if (elem_size == 4) return (size_t)(n + 1) * tape_slot_fields<float>() * tape_field<float>(d);
     return 0;
 }
 

@@ -195,11 +195,22 @@ constexpr int N_WALK_VARIANTS = 4;
 // paired: the state buffers hold the walk's own layout ((u, v, sigma1,
 // sigma2) in 16 bytes per point over the four buffers, sigma12 alone; the
 // prep writes the first state so); the last subcycle writes planar `outs`
-// unless paired_outs
+// unless paired_outs.  `rich` (one paired subcycle with paired outs,
+// constant alpha): the subcycle's Delta, zeta and ocean-drag coefficient at
+// every point, pitch lp, into rich[0..2] (a float32 tape slot's last three
+// fields)
 int evp_walk_subcycles(bool adapt, bool paired, const Dims &d, const HaloFill &h, const FastConsts<float> &c,
                        const FastScalars<float> &k,
                        float *const state[2][5], float *const outs[5], int64_t ldo, int n, bool basal, bool turn,
-                       int rows, int variant, cudaStream_t st, bool paired_outs = false, int *status = nullptr);
+                       int rows, int variant, cudaStream_t st, bool paired_outs = false, int *status = nullptr,
+                       float *const *rich = nullptr);
+
+// Fields per slot of an EVP tape (each the size of one internal array):
+// float64 (u, v, Delta, zeta, cDrag), the stresses staying in the
+// workspace; float32 the register walk's state, (u, v, sigma1, sigma2) per
+// point over four fields and sigma12, then Delta, zeta and cDrag
+template <class T>
+constexpr int tape_slot_fields() { return sizeof(T) == 8 ? 5 : 8; }
 // the walk's layout (its first four fields at `quad`, sigma12 at `s12`, pitch
 // lp) -> five planar arrays of pitch ldo
 int evp_walk_unpack(const Dims &d, const float *quad, const float *s12, float *const outs[5], int64_t ldo,

@@ -33,8 +33,8 @@ evp_walk_kernel(Dims d, int64_t lp, HaloFill h, FastConsts<float> c, FastScalars
     const int strip = w % nstrips, rb = w / nstrips;
     // the single-domain walk takes the cell areas along j (the caller has
     // checked that the state's areas vary along j only: V_AREA2D clear)
-    walk_strip<BASAL, TURN, Variant<V>::UNROLL, Variant<V>::PRE, ADAPT, (L != 0), (L == 1), true>(
-        d, lp, h, c, k, io, rb * H, strip * TW, H, lane);
+    walk_strip<BASAL, TURN, Variant<V>::UNROLL, Variant<V>::PRE, ADAPT, (L != 0), (L == 1 || L == 3), true, false,
+               (L == 3)>(d, lp, h, c, k, io, rb * H, strip * TW, H, lane);
 }
 
 // ---------------------------------------------------------------- persistent
@@ -163,7 +163,8 @@ static int launch_val(bool basal, bool turn, const Dims &d, int64_t lp, const Ha
                 : launch<false, false, V, A, L>(d, lp, h, c, k, io, H, st);
 }
 
-// layout L: 0 planar state in and out, 1 paired in and out, 2 paired in, planar out
+// layout L: 0 planar state in and out, 1 paired in and out, 2 paired in, planar out,
+// 3 paired in and out with Delta, zeta and cDrag written (a float32 tape slot)
 template <int V, int L>
 static int launch_vl(bool adapt, bool basal, bool turn, const Dims &d, int64_t lp, const HaloFill &h,
                      const FastConsts<float> &c, const FastScalars<float> &k, const FastIO<float> &io, int H,
@@ -178,6 +179,11 @@ static int launch_v(int layout, bool adapt, bool basal, bool turn, const Dims &d
                     cudaStream_t st) {
     if (layout == 1) return launch_vl<V, 1>(adapt, basal, turn, d, lp, h, c, k, io, H, st);
     if (layout == 2) return launch_vl<V, 2>(adapt, basal, turn, d, lp, h, c, k, io, H, st);
+    if (layout == 3) {   // the tape's kernels: variant 0, constant alpha
+        if constexpr (V == 0)
+            if (!adapt) return launch_val<0, false, 3>(basal, turn, d, lp, h, c, k, io, H, st);
+        return VERIS_ERR_UNSUPPORTED;
+    }
     return launch_vl<V, 0>(adapt, basal, turn, d, lp, h, c, k, io, H, st);
 }
 
@@ -252,9 +258,10 @@ static std::atomic<int> g_persistent{0};
 int evp_walk_subcycles(bool adapt, bool paired, const Dims &d, const HaloFill &h, const FastConsts<float> &c,
                        const FastScalars<float> &k,
                        float *const state[2][5], float *const outs[5], int64_t ldo, int n, bool basal, bool turn,
-                       int rows, int variant, cudaStream_t st, bool paired_outs, int *status) {
+                       int rows, int variant, cudaStream_t st, bool paired_outs, int *status, float *const *rich) {
     const int64_t lp = internal_pitch(d.NY);
     if ((rows != 0 && (rows < 4 || rows > 4096)) || variant < 0 || variant >= walk::N_VARIANTS) return VERIS_ERR_ARG;
+    if (rich && !(n == 1 && paired && paired_outs && !adapt && variant == 0)) return VERIS_ERR_ARG;
     int it0 = 0;
     if (paired && n >= 3 && status && walk::g_persistent.load(std::memory_order_relaxed)) {
         // subcycles 0 .. n-2 in one launch; the last below writes the caller's layout
@@ -272,11 +279,17 @@ int evp_walk_subcycles(bool adapt, bool paired, const Dims &d, const HaloFill &h
         const bool last = it == n - 1;
         const int b = it % 2;
         float *const *dst = last ? outs : state[(it + 1) % 2];
-        const FastIO<float> io{state[b][0], state[b][1], state[b][2], state[b][3], state[b][4],
-                               dst[0], dst[1], dst[2], dst[3], dst[4], last ? ldo : lp};
+        FastIO<float> io{state[b][0], state[b][1], state[b][2], state[b][3], state[b][4],
+                         dst[0], dst[1], dst[2], dst[3], dst[4], last ? ldo : lp};
         // paired: the state buffers hold (u, v, sigma1, sigma2) per point over
         // their four buffers; the last subcycle writes the caller's planar arrays
-        const int layout = paired ? ((last && !paired_outs) ? 2 : 1) : 0;
+        int layout = paired ? ((last && !paired_outs) ? 2 : 1) : 0;
+        if (rich) {   // checked above: one paired subcycle, paired outs, constant alpha, variant 0
+            layout = 3;
+            io.tDel = rich[0];
+            io.tZeta = rich[1];
+            io.tCd = rich[2];
+        }
         int stt;
         switch (variant) {
         case 1: stt = walk::launch_v<1>(layout, adapt, basal, turn, d, lp, h, c, k, io, rows, st); break;

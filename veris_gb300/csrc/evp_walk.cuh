@@ -105,9 +105,11 @@ __device__ __forceinline__ void load_row(Row &r, const FastConsts<float> &c, con
 // (u, v, sigma1, sigma2) in 16 bytes per point and sigma12 alone; with POUT
 // a row's stresses wait one walk step in registers and are stored with its
 // velocities.  A1D: the cell areas (0.25/rA, rAz, 1/rAu, 1/rAv) vary along j
-// only and live in registers for the whole walk.
+// only and live in registers for the whole walk.  TAPE: Delta, zeta and the
+// ocean-drag coefficient of every own C point go to io.tDel, io.tZeta,
+// io.tCd (pitch io.ldo): a float32 tape's terms for the adjoint.
 template <bool BASAL, bool TURN, int UNROLL, bool PRE = false, bool ADAPT = false, bool PIN = false,
-          bool POUT = false, bool A1D = false, bool COH = false>
+          bool POUT = false, bool A1D = false, bool COH = false, bool TAPE = false>
 __device__ __forceinline__ void walk_strip(const Dims &d, int64_t lp, const HaloFill &h, const FastConsts<float> &c,
                                            const FastScalars<float> &k, const FastIO<float> &io, int i0, int j0,
                                            int H, int lane) {
@@ -234,6 +236,12 @@ __device__ __forceinline__ void walk_strip(const Dims &d, int64_t lp, const Halo
             const bool south = A.f & F_SOUTH;
             const float dc = south ? k.dS : k.dN, dc2 = south ? k.dS2 : k.dN2;
             cd_new = ((dc2 * tt > k.cmin2) ? dc * sqrt_approx(tt) : k.cmin) * mC;
+            if (TAPE && own_j && t >= 3 && t <= H + 2 && i0 + t - 3 < d.NX) {
+                const int64_t wo = (int64_t)(i0 + t - 3) * ldo + jl;
+                io.tDel[wo] = delta;
+                io.tZeta[wo] = zeta;
+                io.tCd[wo] = cd_new;
+            }
             if (BASAL) {
                 const float a = A.u * one_if<float>(A.f, F_INU), b = N.u * one_if<float>(fe, F_INU);
                 const float cc = A.v * one_if<float>(A.f, F_INV), e = vn * one_if<float>(fn, F_INV);
