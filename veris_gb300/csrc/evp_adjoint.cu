@@ -670,7 +670,7 @@ static int evp_adjoint(const VerisGrid *g, const VerisParams *p, const VerisFiel
     if (K <= 0 || K > n || tape) K = n;
     const bool taped = tape != nullptr;
     // float64: the gather passes; float32: the passes on large grids (memory-bound there), the
-    // tile kernel on small ones (its one launch per subcycle beats six latency-bound ones)
+    // tile kernel on small ones (its one launch per subcycle beats four to six latency-bound ones)
     const int f32_form = g_f32_form.load(std::memory_order_relaxed);
     const bool gather = sizeof(T) == 8 || f32_form == 2 ||
                         (f32_form == 0 && (int64_t)d.NX * d.NY >= F32_GATHER_CELLS);

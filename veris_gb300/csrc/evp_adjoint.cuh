@@ -22,8 +22,9 @@ int reduce_drag(const Dims &d, int64_t lp, const uint32_t *flags, const double *
 // One subcycle of the adjoint sweep in gather passes (evp_adjoint_gather.cu).
 // Its tape entries: the velocities before and after it (element stride sst:
 // 1 planar, 4 in the float32 register walk's (u, v, sigma1, sigma2) layout)
-// and the Delta, zeta and ocean-drag coefficient it computed (a float64 tape
-// holds them; for a float32 tape the adjoint recomputes them first: NULL).
+// and the Delta, zeta and ocean-drag coefficient it computed (a tape holds
+// them; for a float32 segment recomputed from a checkpoint the adjoint
+// recomputes them first: NULL).
 template <class T>
 struct TapeG {
     const T *u, *v;          // slot k (pitch lp)

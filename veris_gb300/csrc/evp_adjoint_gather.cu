@@ -27,9 +27,11 @@
 // so the adjoint takes no square root of the forward's; its reciprocals and
 // the basal drag's reciprocal square root use the series-refined hardware
 // approximations of f64math.cuh, masks are selects and zero tests run on the
-// integer pipe.  A float32 tape (the register walk's) keeps the stresses
-// instead: two first passes recompute e12, then Delta, zeta and the drag
-// coefficient, with IEEE-rounded float32 square roots and reciprocals.
+// integer pipe.  A float32 tape (the register walk's) holds the walk's own
+// Delta, zeta and drag coefficient beside its state; a float32 segment
+// recomputed from a checkpoint does not, and two first passes recompute e12,
+// then Delta, zeta and the drag coefficient, with IEEE-rounded float32 square
+// roots and reciprocals.
 //
 // Non-differentiable points take the subgradients of the shared-memory
 // form (evp_adjoint.cu): 0 at Delta = 0 and on the drag floor's constant
