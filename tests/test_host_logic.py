@@ -1,7 +1,7 @@
 """Host-side logic that needs no GPU: the binomial checkpoint schedule of the
-multi-step adjoint, the choice of the EVP checkpoint spacing from free
-device memory, and the host exchange's plan of which rows of Growth's
-outputs can go to the host before the halo fill."""
+multi-step adjoint, the choice of the EVP checkpoint spacing and of the EVP
+tape policy from free device memory, and the host exchange's plan of which
+rows of Growth's outputs can go to the host before the halo fill."""
 import functools
 from types import SimpleNamespace
 
@@ -104,3 +104,29 @@ def test_growth_row_plan(veros_fill):
         else:
             assert n not in plan, n                        # columns of every row: after the fill
     assert "TSurf" in plan and "hIceMean" in plan if veros_fill else "hIceMean" not in plan
+
+
+def test_tape_policy():
+    """All steps' tapes when they fit beside every snapshot; else, in float32,
+    one step's tape written during the reverse; else the recompute."""
+    from veris_gb300.trajectory import tape_mode
+    G = 1 << 30
+    tb, ws = 65 * G, 1 * G   # one 0.1-degree float32 step's tape, the taped adjoint's workspace
+    # 24 steps do not fit in 60 % of 250 GB; one step does
+    assert tape_mode("auto", True, True, 24, tb, ws, 250 * G, 0.6) == "step"
+    assert tape_mode("auto", False, True, 24, tb, ws, 250 * G, 0.6) is False   # float64: recompute
+    # two steps fit: every step taped during the forward
+    assert tape_mode("auto", True, True, 1, tb, ws, 250 * G, 0.6) is True
+    assert tape_mode("auto", False, True, 1, tb, ws, 250 * G, 0.6) is True
+    # without a snapshot of every step the forward cannot keep per-step tapes
+    assert tape_mode("auto", True, False, 1, tb, ws, 250 * G, 0.6) == "step"
+    # not even one step fits
+    assert tape_mode("auto", True, True, 24, tb, ws, 100 * G, 0.6) is False
+    # explicit choices
+    assert tape_mode("step", True, True, 24, tb, ws, 0, 0.6) == "step"
+    assert tape_mode(False, True, True, 24, tb, ws, 0, 0.6) is False
+    assert tape_mode(True, True, True, 24, tb, ws, 0, 0.6) is True
+    with pytest.raises(ValueError):
+        tape_mode("step", False, True, 24, tb, ws, 0, 0.6)
+    with pytest.raises(ValueError):
+        tape_mode(True, True, False, 24, tb, ws, 0, 0.6)

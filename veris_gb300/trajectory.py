@@ -69,6 +69,28 @@ def interior_mask(shape, olx=2, oly=2, device="cuda"):
     return m
 
 
+def tape_mode(tape, f32, every_step_snapshotted, n_steps, tape_bytes, taped_ws, free, fraction):
+    """The EVP tape policy of a trajectory: True (every step's tape written
+    during the forward), "step" (float32: one step's tape written during the
+    reverse) or False (the EVP adjoint recomputes its subcycles).  ``tape``
+    "auto" takes the first that fits in ``fraction`` of ``free`` bytes; an
+    explicit choice is checked."""
+    if tape == "auto":
+        if every_step_snapshotted and (n_steps + 1) * tape_bytes <= fraction * free:
+            return True
+        if f32 and tape_bytes + taped_ws <= fraction * free:
+            return "step"
+        return False
+    if tape == "step":
+        if not f32:
+            raise ValueError("tape='step' is a float32 form (the float64 adjoint's one-segment recompute "
+                             "already runs the forward's own kernel)")
+        return "step"
+    if tape and not every_step_snapshotted:
+        raise ValueError("taping needs every step snapshotted (snapshots=None)")
+    return bool(tape)
+
+
 class Trajectory:
     """n float64 steps from the state's current values and their adjoint."""
 
@@ -152,20 +174,9 @@ class Trajectory:
         tape_bytes = int(self.lib.veris_evp_tape_bytes(g, esize, self.eng.n_sub))
         taped_ws = int(self.lib.veris_evp_adjoint_taped_workspace_bytes_f32(g, self.eng.n_sub) if f32 else
                        self.lib.veris_evp_adjoint_taped_workspace_bytes(g, self.eng.n_sub))
-        if tape == "auto":
-            free = torch.cuda.mem_get_info(dev)[0]
-            if self.snaps == self.n - 1 and (self.n + 1) * tape_bytes <= tape_memory_fraction * free:
-                tape = True
-            elif f32 and tape_bytes + taped_ws <= tape_memory_fraction * free:
-                tape = "step"
-            else:
-                tape = False
-        elif tape == "step":
-            if not f32:
-                raise ValueError("tape='step' is a float32 form (the float64 adjoint's one-segment recompute "
-                                 "already runs the forward's own kernel)")
-        elif tape and self.snaps != self.n - 1:
-            raise ValueError("taping needs every step snapshotted (snapshots=None)")
+        free = torch.cuda.mem_get_info(dev)[0] if tape == "auto" else 0
+        tape = tape_mode(tape, f32, self.snaps == self.n - 1, self.n, tape_bytes, taped_ws, free,
+                         tape_memory_fraction)
         self.tape_mode = "step" if tape == "step" else ("all" if tape else "off")
         tdt = torch.float32 if f32 else torch.float64
         # one tape, rewritten by every step's reverse
