@@ -435,9 +435,13 @@ size_t veris_evp_adjoint_taped_workspace_bytes_f32(const VerisGrid *g, int32_t n
 /*
  * Form of the float32 EVP adjoint subcycle: 0 by grid size (the gather
  * passes from 2^19 padded cells up, where they are memory-bound; below, one
- * tile kernel per subcycle, which beats six latency-bound launches), 1 the
- * tile kernel, 2 the gather passes.  Process-wide, for every later call;
- * the two agree to float32 rounding.  VERIS_ERR_ARG for other values.
+ * tile kernel per subcycle, which beats four to six latency-bound launches),
+ * 1 the tile kernel, 2 the gather passes (without a turning angle the last
+ * pass of each subcycle runs fused with the first of the subcycle before
+ * it), 3 the gather passes each in its own launch (the same values as 2, bit
+ * for bit, but for the order of the per-warp drag sums' atomics).
+ * Process-wide, for every later call; the tile kernel and the passes agree
+ * to float32 rounding.  VERIS_ERR_ARG for other values.
  */
 int veris_evp_adjoint_f32_form(int32_t form);
 int veris_evp_adjoint_taped_f32(const VerisGrid *g, const VerisParams *p, const VerisFieldsF64 *vs,

@@ -112,7 +112,43 @@ def test_float32_evp_adjoint_is_the_transpose_to_float32_rounding(golden, form, 
     assert mag > 0
     assert abs(lhs - rhs) <= 1e-4 * mag, \
         f"evp f32 form {form} tape {tape}/{golden}: {lhs:.9e} vs {rhs:.9e} ({abs(lhs - rhs) / mag:.2e})"
-    assert lib.veris_evp_adjoint_f32_form(3) != 0
+    assert lib.veris_evp_adjoint_f32_form(4) != 0
+
+
+@pytest.mark.parametrize("golden,veros_fill", [("c1", True), ("c1", False), ("moving", True)])
+@pytest.mark.parametrize("tape", [False, True])
+def test_float32_linked_passes_equal_the_separate_ones(golden, veros_fill, tape):
+    """The float32 gather passes with P4 of each subcycle fused with P1 of
+    the one before it (form 2) against every pass in its own launch (form
+    3), with the x halo or both halos filled (the fused pass evaluates P4 at
+    a point's images itself): the same state and field adjoints bit for bit,
+    the drag scalars up to the order of their per-warp atomics."""
+    from veris_gb300 import _abi
+    from veris_gb300 import adjoint as A
+    from veris_gb300.state import VerisState
+    lib = _abi.load()
+    rng = np.random.default_rng(9)
+    st = jitter(golden_state("evp", golden), rng)
+    st.settings.veros_fill = veros_fill
+    _routine, _ins, outs, _f = CASES["evp"]
+    gst = VerisState.from_numpy(vars(st.variables), st.settings)
+    lam = {k: torch.as_tensor(rng.standard_normal(getattr(st.variables, k).shape), device="cuda") for k in outs}
+    res = {}
+    try:
+        for form in (2, 3):
+            assert lib.veris_evp_adjoint_f32_form(form) == 0
+            res[form] = A.evp_adjoint(gst, lam, n_subcycles=4, precision="f32", tape=tape)
+    finally:
+        lib.veris_evp_adjoint_f32_form(0)
+    torch.cuda.synchronize()
+    (s2, f2, d2), (s3, f3, d3) = res[2], res[3]
+    for k in s2:
+        assert torch.equal(s2[k], s3[k]), k
+    for k in f2:
+        assert torch.equal(f2[k], f3[k]), k
+    for k in d2:
+        a, b = float(d2[k]), float(d3[k])
+        assert abs(a - b) <= 1e-12 * max(abs(b), 1e-30), (k, a, b)
 
 
 def test_evp_adjoint_is_the_transpose_with_both_halos_refreshed():

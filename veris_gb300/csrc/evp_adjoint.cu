@@ -649,7 +649,8 @@ static int copy_state(T *const dst[5], T *const src[5], size_t bytes, cudaStream
     return VERIS_OK;
 }
 
-// the float32 adjoint's form: 0 by grid size, 1 the tile kernel, 2 the gather passes
+// the float32 adjoint's form: 0 by grid size, 1 the tile kernel, 2 the gather passes, 3 the
+// gather passes with P4 and P1 of consecutive subcycles in separate launches
 static std::atomic<int> g_f32_form{0};
 // padded cells from which the float32 adjoint takes the gather passes (measured: 360 x 180
 // faster with the tile kernel, 3600 x 1800 with the passes)
@@ -672,7 +673,7 @@ static int evp_adjoint(const VerisGrid *g, const VerisParams *p, const VerisFiel
     // float64: the gather passes; float32: the passes on large grids (memory-bound there), the
     // tile kernel on small ones (its one launch per subcycle beats four to six latency-bound ones)
     const int f32_form = g_f32_form.load(std::memory_order_relaxed);
-    const bool gather = sizeof(T) == 8 || f32_form == 2 ||
+    const bool gather = sizeof(T) == 8 || f32_form >= 2 ||
                         (f32_form == 0 && (int64_t)d.NX * d.NY >= F32_GATHER_CELLS);
     Plan<T> pl;
     VERIS_REQUIRE(ws && wsb >= plan<T>(d, n, K, nullptr, &pl, taped), VERIS_ERR_WORKSPACE);
@@ -760,36 +761,66 @@ static int evp_adjoint(const VerisGrid *g, const VerisParams *p, const VerisFiel
             if (gather) {
                 // gather passes: every adjoint array written whole, nothing to clear.  A float64
                 // slot holds (u, v, Delta, zeta, cDrag); a float32 tape the walk's (u, v, sigma1,
-                // sigma2) layout, a float32 segment five planar state arrays: the passes recompute
-                // Delta, zeta and cDrag
+                // sigma2) layout and its Delta, zeta, cDrag; a float32 segment five planar state
+                // arrays: the passes recompute Delta, zeta and cDrag
                 const bool quad = taped && sizeof(T) == 4;
-                TapeG<T> tt;
-                tt.u = slot(segb, pl.field, rs, 0, W);
-                tt.v = quad ? tt.u + 1 : slot(segb, pl.field, rs, 1, W);
-                tt.un = slot(segb, pl.field, rs + 1, 0, W);
-                tt.vn = quad ? tt.un + 1 : slot(segb, pl.field, rs + 1, 1, W);
-                tt.sst = quad ? 4 : 1;
-                // Delta, zeta, cDrag: a float64 slot's fields 2-4, a float32 tape's 5-7 (the walk's
-                // own values); a float32 segment has none and the passes recompute them
-                const int qd = sizeof(T) == 8 ? 2 : 5;
-                const bool rich = sizeof(T) == 8 || quad;
-                tt.del = rich ? slot(segb, pl.field, rs, qd, W) : nullptr;
-                tt.zeta = rich ? slot(segb, pl.field, rs, qd + 1, W) : nullptr;
-                tt.cd = rich ? slot(segb, pl.field, rs, qd + 2, W) : nullptr;
-                LamG<T> ll;
-                if (first) {
-                    ll.lu = lout[0]; ll.lv = lout[1]; ll.ls1 = lout[2]; ll.ls2 = lout[3]; ll.ls12 = lout[4];
-                    ll.ldl = d.ld;
-                } else {
-                    ll.lu = pl.lam[lb][0]; ll.lv = pl.lam[lb][1]; ll.ls1 = pl.lam[lb][2];
-                    ll.ls2 = pl.lam[lb][3]; ll.ls12 = pl.lam[lb][4];
-                    ll.ldl = lp;
+                auto tape_of = [&](int sub) {
+                    const int r = taped ? sub : sub - s0;   // slot of the subcycle's input state
+                    TapeG<T> tt;
+                    tt.u = slot(segb, pl.field, r, 0, W);
+                    tt.v = quad ? tt.u + 1 : slot(segb, pl.field, r, 1, W);
+                    tt.un = slot(segb, pl.field, r + 1, 0, W);
+                    tt.vn = quad ? tt.un + 1 : slot(segb, pl.field, r + 1, 1, W);
+                    tt.sst = quad ? 4 : 1;
+                    const int qd = sizeof(T) == 8 ? 2 : 5;
+                    const bool rich = sizeof(T) == 8 || quad;
+                    tt.del = rich ? slot(segb, pl.field, r, qd, W) : nullptr;
+                    tt.zeta = rich ? slot(segb, pl.field, r, qd + 1, W) : nullptr;
+                    tt.cd = rich ? slot(segb, pl.field, r, qd + 2, W) : nullptr;
+                    return tt;
+                };
+                // the adjoints of subcycle `sub`: in from its result's buffer (the caller's at the
+                // last subcycle), out to the other of the two
+                auto lam_of = [&](int sub, int b) {
+                    LamG<T> ll;
+                    if (sub == n - 1) {
+                        ll.lu = lout[0]; ll.lv = lout[1]; ll.ls1 = lout[2]; ll.ls2 = lout[3]; ll.ls12 = lout[4];
+                        ll.ldl = d.ld;
+                    } else {
+                        ll.lu = pl.lam[b][0]; ll.lv = pl.lam[b][1]; ll.ls1 = pl.lam[b][2];
+                        ll.ls2 = pl.lam[b][3]; ll.ls12 = pl.lam[b][4];
+                        ll.ldl = lp;
+                    }
+                    T *const *o5 = pl.lam[sub == n - 1 ? 0 : b ^ 1];
+                    ll.ou = o5[0]; ll.ov = o5[1]; ll.os1 = o5[2]; ll.os2 = o5[3]; ll.os12 = o5[4];
+                    return ll;
+                };
+                const TapeG<T> tt = tape_of(ss);
+                const LamG<T> ll = lam_of(ss, lb);
+                const int lb_next = first ? 0 : lb ^ 1;
+                bool done = false;
+                if constexpr (sizeof(T) == 4) {
+                    // float32 without turning angle: P4 of each subcycle fused with P1 of the one
+                    // before it in the segment
+                    if (!turn && f32_form != 3) {
+                        const bool head = ss == s1 - 1;
+                        if (ss > s0) {
+                            const TapeG<T> tp = tape_of(ss - 1);
+                            const LamG<T> lpv = lam_of(ss - 1, lb_next);
+                            stt = adjoint_gather_chain<T>(d, lp, h, pl.c, k, p->rhoSea, tt, ll, pl.a, pl.scr, basal,
+                                                          head, &tp, &lpv, st);
+                        } else {
+                            stt = adjoint_gather_chain<T>(d, lp, h, pl.c, k, p->rhoSea, tt, ll, pl.a, pl.scr, basal,
+                                                          head, nullptr, nullptr, st);
+                        }
+                        done = true;
+                    }
                 }
-                ll.ou = out[0]; ll.ov = out[1]; ll.os1 = out[2]; ll.os2 = out[3]; ll.os12 = out[4];
-                if ((stt = adjoint_gather_subcycle<T>(d, lp, h, pl.c, k, p->rhoSea, tt, ll, pl.a, pl.scr, basal, turn,
-                                                      st)) != VERIS_OK)
-                    return stt;
-                lb = first ? 0 : lb ^ 1;
+                if (!done)
+                    stt = adjoint_gather_subcycle<T>(d, lp, h, pl.c, k, p->rhoSea, tt, ll, pl.a, pl.scr, basal, turn,
+                                                     st);
+                if (stt != VERIS_OK) return stt;
+                lb = lb_next;
                 continue;
             }
             if constexpr (sizeof(T) == 4) {   // the float32 tile kernel (float64 always gathers)
@@ -935,7 +966,7 @@ int veris_evp_adjoint_f64(const VerisGrid *g, const VerisParams *p, const VerisF
 }
 
 int veris_evp_adjoint_f32_form(int32_t form) {
-    VERIS_REQUIRE(form >= 0 && form <= 2, VERIS_ERR_ARG);
+    VERIS_REQUIRE(form >= 0 && form <= 3, VERIS_ERR_ARG);
     adj::g_f32_form.store(form, std::memory_order_relaxed);
     return VERIS_OK;
 }

@@ -55,6 +55,18 @@ int adjoint_gather_subcycle(const Dims &d, int64_t lp, const HaloFill &h, const 
                             const FastScalars<T> &k, double rhoSea, const TapeG<T> &t, const LamG<T> &l,
                             const Adj<T> &a, T *const scratch[N_SCRATCH], bool basal, bool turn, cudaStream_t st);
 
+// The sweep as a chain of subcycles, P4 of each fused with P1 of the one
+// before it (no turning angle; instantiated for float32): `head` runs P1 of
+// subcycle t first (the chain's first subcycle); then P2 and P3 of t; then,
+// with t_prev and l_prev (subcycle t - 1: its tape entries, and the
+// adjoints whose inputs are l's outputs), the fused P4 of t and P1 of t - 1,
+// else P4 of t alone (the chain's last subcycle).
+template <class T>
+int adjoint_gather_chain(const Dims &d, int64_t lp, const HaloFill &h, const FastConsts<T> &c,
+                         const FastScalars<T> &k, double rhoSea, const TapeG<T> &t, const LamG<T> &l,
+                         const Adj<T> &a, T *const scratch[N_SCRATCH], bool basal, bool head,
+                         const TapeG<T> *t_prev, const LamG<T> *l_prev, cudaStream_t st);
+
 }  // namespace adj
 
 }  // namespace veris

@@ -323,19 +323,18 @@ __device__ __forceinline__ void own_adjoints(const Dims &d, const HaloFill &h, c
 //   den = mU (beta+1)/dt + kU [+ AW (cb + cb_w)/2],  kU = cos/2 AW (cd + cd_w),
 //   num = mU beta/dt u + cU + kU uOc + (Fv + Fv_w)/2 [+ turning] + rrAu (dyV (s11 - s11_w) + dxV (s12'_n - s12'))
 // (veris/evp_solver.py:113-187); V(i, j) the same with the j neighbours.
-template <class T, bool BASAL, bool TURN>
-__global__ void __launch_bounds__(BX * BY) uv_reverse_kernel(Dims d, int64_t lp, HaloFill h, FastConsts<T> c,
-                                                              TapeG<T> t, LamG<T> l, Adj<T> a, KT<T> k, Scr<T> s) {
-    const int j = blockIdx.x * BX + threadIdx.x, i = blockIdx.y * BY + threadIdx.y;
-    const bool act = i < d.NX && j < d.NY;
-    const unsigned m = __ballot_sync(ALL, act);
-    if (!act) return;
+// P1 at U(i, j), V(i, j) given the adjoints LU, LV of its new velocities;
+// luo, lvo: ocean-velocity adjoint shares of the subcycle after it (its P4
+// run in the same kernel), added to a.uOc, a.vOc before this subcycle's
+// (the order of the separate passes); MERGE: there are such shares
+template <class T, bool BASAL, bool TURN, bool MERGE>
+__device__ __forceinline__ void p1_point(const Dims &d, int64_t lp, const FastConsts<T> &c, const TapeG<T> &t,
+                                         const LamG<T> &l, const Adj<T> &a, const KT<T> &k, const Scr<T> &s,
+                                         unsigned m, int i, int j, T LU, T LV, T luo, T lvo) {
     const Fold<T> F{c, k};
     const int iw = wxp(d, i - 1), js = wyp(d, j - 1);
     const int64_t o = (int64_t)i * lp + j, ow = (int64_t)iw * lp + j, os = (int64_t)i * lp + js;
     const uint32_t f0 = c.flags[o];
-    T LU, LV;
-    own_adjoints(d, h, l, i, j, LU, LV);
     const T cd0 = t.cd[o], cdw = t.cd[ow], cds = t.cd[os];
     T cb0 = T(0), cbw = T(0), cbs = T(0);
     if (BASAL) {
@@ -346,6 +345,7 @@ __global__ void __launch_bounds__(BX * BY) uv_reverse_kernel(Dims d, int64_t lp,
     T sg = T(0);
     if (TURN) sg = (f0 & F_SPOS) ? T(1) : ((f0 & F_SNEG) ? T(-1) : T(0));
     if (!__any_sync(m, f0 & F_MU)) {   // a warp of dry U points: no momentum adjoint, nothing to add
+        if (MERGE) a.uOc[o] += luo;
         l.ou[o] = T(0);
         s.gU[o] = T(0);
         s.rU[o] = T(0);
@@ -371,7 +371,7 @@ __global__ void __launch_bounds__(BX * BY) uv_reverse_kernel(Dims d, int64_t lp,
             lAW = fma(T(0.5) * (cb0 + cbw), lden, lAW);
             s.bU[o] = T(0.5) * c.AW[o] * lden;
         }
-        a.uOc[o] = fma(kU, g, a.uOc[o]);
+        a.uOc[o] = fma(kU, g, MERGE ? a.uOc[o] + luo : a.uOc[o]);
         s.gU[o] = g;
         s.rU[o] = c.rrAu[o] * g;
         if (TURN) {
@@ -393,6 +393,7 @@ __global__ void __launch_bounds__(BX * BY) uv_reverse_kernel(Dims d, int64_t lp,
         a.AW[o] = lAW;
     }
     if (!__any_sync(m, f0 & F_MV)) {
+        if (MERGE) a.vOc[o] += lvo;
         l.ov[o] = T(0);
         s.gV[o] = T(0);
         s.rV[o] = T(0);
@@ -418,7 +419,7 @@ __global__ void __launch_bounds__(BX * BY) uv_reverse_kernel(Dims d, int64_t lp,
             lAS = fma(T(0.5) * (cb0 + cbs), lden, lAS);
             s.bV[o] = T(0.5) * c.AS[o] * lden;
         }
-        a.vOc[o] = fma(kV, g, a.vOc[o]);
+        a.vOc[o] = fma(kV, g, MERGE ? a.vOc[o] + lvo : a.vOc[o]);
         s.gV[o] = g;
         s.rV[o] = c.rrAv[o] * g;
         if (TURN) {
@@ -439,6 +440,18 @@ __global__ void __launch_bounds__(BX * BY) uv_reverse_kernel(Dims d, int64_t lp,
         }
         a.AS[o] = lAS;
     }
+}
+
+template <class T, bool BASAL, bool TURN>
+__global__ void __launch_bounds__(BX * BY) uv_reverse_kernel(Dims d, int64_t lp, HaloFill h, FastConsts<T> c,
+                                                              TapeG<T> t, LamG<T> l, Adj<T> a, KT<T> k, Scr<T> s) {
+    const int j = blockIdx.x * BX + threadIdx.x, i = blockIdx.y * BY + threadIdx.y;
+    const bool act = i < d.NX && j < d.NY;
+    const unsigned m = __ballot_sync(ALL, act);
+    if (!act) return;
+    T LU, LV;
+    own_adjoints(d, h, l, i, j, LU, LV);
+    p1_point<T, BASAL, TURN, false>(d, lp, c, t, l, a, k, s, m, i, j, LU, LV, T(0), T(0));
 }
 
 // ------------------------------------------------------------------ P2
@@ -610,13 +623,15 @@ __device__ __forceinline__ T e12_coef(bool mz, int h, int sign) {
 // U(i, j), V(i, j): the velocity and ocean-velocity adjoints gathered from
 // the C points (strain rates, drag, basal drag, Coriolis), the Z points
 // (e12) and the turning-angle terms of the neighbouring U, V points
-template <class T, bool BASAL, bool TURN>
-__global__ void __launch_bounds__(BX * BY) uv_gather_kernel(Dims d, int64_t lp, FastConsts<T> c, TapeG<T> t,
-                                                             LamG<T> l, Adj<T> a, KT<T> k, Scr<T> s) {
-    const int j = blockIdx.x * BX + threadIdx.x, i = blockIdx.y * BY + threadIdx.y;
-    const bool act = i < d.NX && j < d.NY;
-    const unsigned m = __ballot_sync(ALL, act);
-    if (!act) return;
+// P4 at U(i, j), V(i, j): the velocity adjoints gathered from the C and Z
+// points (lu, lv: to be added to the momentum share P1 left in l.ou, l.ov)
+// and the ocean-velocity shares (luo, lvo); `m` the lanes that call it.
+// VOTE false: no warp vote (for lanes that call it alone; the no-slip terms'
+// general form then runs everywhere, with the same values)
+template <class T, bool BASAL, bool TURN, bool VOTE = true>
+__device__ __forceinline__ void p4_point(const Dims &d, int64_t lp, const FastConsts<T> &c, const TapeG<T> &t,
+                                         const KT<T> &k, const Scr<T> &s, unsigned m, int i, int j, T &lu_out,
+                                         T &lv_out, T &luo_out, T &lvo_out) {
     const Fold<T> F{c, k};
     const int iw = wxp(d, i - 1), ie = wxp(d, i + 1), js = wyp(d, j - 1), jn = wyp(d, j + 1);
     const int64_t o = (int64_t)i * lp + j, ow = (int64_t)iw * lp + j, oe = (int64_t)ie * lp + j,
@@ -637,7 +652,7 @@ __global__ void __launch_bounds__(BX * BY) uv_gather_kernel(Dims d, int64_t lp, 
     const T ru0 = z0 * F.rdyUh(j), run = zn * F.rdyUh(jn);
     const T rv0 = z0 * F.rdxVh(i), rve = ze * F.rdxVh(ie);
     T lu, lv;
-    if (__any_sync(m, (hU0 | hUn | hV0 | hVe) != 0)) {   // no-slip boundary terms in this warp
+    if (!VOTE || __any_sync(m, (hU0 | hUn | hV0 | hVe) != 0)) {   // no-slip boundary terms in this warp
         lu = fma(ru0, e12_coef<T>(mz0, hU0, 1), run * e12_coef<T>(mzn, hUn, -1));
         lv = fma(rv0, e12_coef<T>(mz0, hV0, 1), rve * e12_coef<T>(mze, hVe, -1));
     } else {
@@ -668,46 +683,160 @@ __global__ void __launch_bounds__(BX * BY) uv_gather_kernel(Dims d, int64_t lp, 
         luo += qu;
         lvo += qv;
     }
+    lu_out = lu;
+    lv_out = lv;
+    luo_out = luo;
+    lvo_out = lvo;
+}
+
+template <class T, bool BASAL, bool TURN>
+__global__ void __launch_bounds__(BX * BY) uv_gather_kernel(Dims d, int64_t lp, FastConsts<T> c, TapeG<T> t,
+                                                             LamG<T> l, Adj<T> a, KT<T> k, Scr<T> s) {
+    const int j = blockIdx.x * BX + threadIdx.x, i = blockIdx.y * BY + threadIdx.y;
+    const bool act = i < d.NX && j < d.NY;
+    const unsigned m = __ballot_sync(ALL, act);
+    if (!act) return;
+    T lu, lv, luo, lvo;
+    p4_point<T, BASAL, TURN>(d, lp, c, t, k, s, m, i, j, lu, lv, luo, lvo);
+    const int64_t o = (int64_t)i * lp + j;
     l.ou[o] += lu;
     l.ov[o] += lv;
     a.uOc[o] += luo;
     a.vOc[o] += lvo;
 }
 
+// P4 of subcycle k and P1 of subcycle k - 1 in one pass (no turning angle).
+// The velocity adjoints P4 gathers at a point, added to its momentum share
+// (which P1 of subcycle k left in l4.ou, l4.ov) and to those of the point's
+// images in a filled halo (their P4 terms evaluated here as well), are what
+// P1 of subcycle k - 1 reads there: they stay in registers, and the
+// ocean-velocity adjoints take one read-modify-write for both subcycles, in
+// the separate passes' order of additions.  t4, l4: subcycle k; t1, l1:
+// subcycle k - 1.  Six 256-thread CTAs per SM (40 registers, 8 bytes
+// spilled): the passes are latency-bound, and on 3600 x 1800 a reverse
+// step took 389.5 ms so, 401.2 ms with five CTAs per SM (48 registers, no
+// spill), 428.6 ms with four, 400.0 ms with the passes separate.
+template <class T, bool BASAL>
+__global__ void __launch_bounds__(BX * BY, 6) uv_link_kernel(Dims d, int64_t lp, HaloFill h, FastConsts<T> c,
+                                                           TapeG<T> t4, TapeG<T> t1, LamG<T> l4, LamG<T> l1,
+                                                           Adj<T> a, KT<T> k, Scr<T> s) {
+    const int j = blockIdx.x * BX + threadIdx.x, i = blockIdx.y * BY + threadIdx.y;
+    const bool act = i < d.NX && j < d.NY;
+    const unsigned m = __ballot_sync(ALL, act);
+    if (!act) return;
+    T lu, lv, luo, lvo;
+    p4_point<T, BASAL, false>(d, lp, c, t4, k, s, m, i, j, lu, lv, luo, lvo);
+    // own_adjoints of the separate passes, on subcycle k's completed adjoints
+    T LU = T(0), LV = T(0);
+    const bool hx = h.x_fill && in_xhalo(d, h.olx, i);
+    const bool hy = h.y_fill && in_yhalo(d, h.oly, j);
+    if (!(hx || hy)) {
+        const int64_t o = (int64_t)i * lp + j;
+        LU = l4.ou[o] + lu;
+        LV = l4.ov[o] + lv;
+        int ix[2] = {i, -1}, jy[2] = {j, -1};
+        if (h.x_fill) {
+            if (i + d.nx < d.NX && in_xhalo(d, h.olx, i + d.nx)) ix[1] = i + d.nx;
+            else if (i - d.nx >= 0 && in_xhalo(d, h.olx, i - d.nx)) ix[1] = i - d.nx;
+        }
+        if (h.y_fill) {
+            if (j + d.ny < d.NY && in_yhalo(d, h.oly, j + d.ny)) jy[1] = j + d.ny;
+            else if (j - d.ny >= 0 && in_yhalo(d, h.oly, j - d.ny)) jy[1] = j - d.ny;
+        }
+        if (ix[1] >= 0 || jy[1] >= 0) {   // a point whose images lie in a filled halo (the edges)
+#pragma unroll 1
+            for (int q3 = 1; q3 < 4; ++q3) {   // images (i, j'), (i', j), (i', j') in the separate passes' order
+                const int x = q3 >> 1, y = q3 & 1;
+                if (ix[x] < 0 || jy[y] < 0) continue;
+                T qu, qv, qo, qp;
+                p4_point<T, BASAL, false, false>(d, lp, c, t4, k, s, 0u, ix[x], jy[y], qu, qv, qo, qp);
+                const int64_t q = (int64_t)ix[x] * lp + jy[y];
+                LU += l4.ou[q] + qu;
+                LV += l4.ov[q] + qv;
+            }
+        }
+    }
+    p1_point<T, BASAL, false, true>(d, lp, c, t1, l1, a, k, s, m, i, j, LU, LV, luo, lvo);
+}
+
 }  // namespace
 
-template <class T, bool B, bool R>
-static int run_passes(const Dims &d, int64_t lp, const HaloFill &h, const FastConsts<T> &c, const KT<T> &k,
-                      TapeG<T> t, const LamG<T> &l, const Adj<T> &a, const Scr<T> &s, cudaStream_t st) {
-    const dim3 blk(BX, BY), grd((d.NY + BX - 1) / BX, (d.NX + BY - 1) / BY);
-    const bool recompute = t.del == nullptr;   // a tape without the forward's terms (float32)
-    if (recompute) {
-        e12_kernel<T><<<grd, blk, 0, st>>>(d, lp, c, t, k, s);
-        viscosity_kernel<T><<<grd, blk, 0, st>>>(d, lp, c, t, k, s);
+// The passes of one subcycle in phases: head (the recomputed terms of a
+// tape without them, the basal coefficient, P1), body (P2, P3), tail (P4),
+// or, chaining the sweep, the link (the next subcycle's recomputed terms and
+// basal coefficient, then P4 fused with its P1).
+template <class T>
+static TapeG<T> with_terms(TapeG<T> t, const Scr<T> &s) {
+    if (t.del == nullptr) {   // a tape without the forward's terms (float32 segment)
         t.del = s.del;
         t.zeta = s.zeta;
         t.cd = s.cd;
     }
-    if (B) basal_kernel<T><<<grd, blk, 0, st>>>(d, lp, c, t, k, s);
-    uv_reverse_kernel<T, B, R><<<grd, blk, 0, st>>>(d, lp, h, c, t, l, a, k, s);
-    z_reverse_kernel<T><<<grd, blk, 0, st>>>(d, lp, c, t, l, k, s, recompute);
-    c_reverse_kernel<T, B, R><<<grd, blk, 0, st>>>(d, lp, c, t, l, a, k, s);
-    uv_gather_kernel<T, B, R><<<grd, blk, 0, st>>>(d, lp, c, t, l, a, k, s);
+    return t;
+}
+
+template <class T, bool B>
+static void pre_p1(const Dims &d, int64_t lp, const FastConsts<T> &c, const KT<T> &k, const TapeG<T> &t,
+                   const Scr<T> &s, dim3 grd, dim3 blk, cudaStream_t st) {
+    if (t.del == nullptr) {
+        e12_kernel<T><<<grd, blk, 0, st>>>(d, lp, c, t, k, s);
+        viscosity_kernel<T><<<grd, blk, 0, st>>>(d, lp, c, t, k, s);
+    }
+    if (B) basal_kernel<T><<<grd, blk, 0, st>>>(d, lp, c, with_terms(t, s), k, s);
+}
+
+template <class T, bool B, bool R>
+static int run_phases(const Dims &d, int64_t lp, const HaloFill &h, const FastConsts<T> &c, const KT<T> &k,
+                      const TapeG<T> &t, const LamG<T> &l, const Adj<T> &a, const Scr<T> &s, bool head,
+                      const TapeG<T> *tp, const LamG<T> *lpv, cudaStream_t st) {
+    const dim3 blk(BX, BY), grd((d.NY + BX - 1) / BX, (d.NX + BY - 1) / BY);
+    const TapeG<T> tt = with_terms(t, s);
+    if (head) {
+        pre_p1<T, B>(d, lp, c, k, t, s, grd, blk, st);
+        uv_reverse_kernel<T, B, R><<<grd, blk, 0, st>>>(d, lp, h, c, tt, l, a, k, s);
+    }
+    z_reverse_kernel<T><<<grd, blk, 0, st>>>(d, lp, c, tt, l, k, s, t.del == nullptr);
+    c_reverse_kernel<T, B, R><<<grd, blk, 0, st>>>(d, lp, c, tt, l, a, k, s);
+    if (tp) {
+        if constexpr (!R && sizeof(T) == 4) {
+            pre_p1<T, B>(d, lp, c, k, *tp, s, grd, blk, st);
+            uv_link_kernel<T, B><<<grd, blk, 0, st>>>(d, lp, h, c, tt, with_terms(*tp, s), l, *lpv, a, k, s);
+        }
+    } else {
+        uv_gather_kernel<T, B, R><<<grd, blk, 0, st>>>(d, lp, c, tt, l, a, k, s);
+    }
     return launch_status();
+}
+
+template <class T>
+static int phases(const Dims &d, int64_t lp, const HaloFill &h, const FastConsts<T> &c, const FastScalars<T> &k,
+                  double rhoSea, const TapeG<T> &t, const LamG<T> &l, const Adj<T> &a, T *const scratch[N_SCRATCH],
+                  bool basal, bool turn, bool head, const TapeG<T> *tp, const LamG<T> *lpv, cudaStream_t st) {
+    if (tp && turn) return VERIS_ERR_ARG;   // the link keeps no turning-angle shares
+    Scr<T> s;
+    std::memcpy(&s, scratch, sizeof s);
+    const KT<T> kk = kt<T>(k, rhoSea);
+    if (basal)
+        return turn ? run_phases<T, true, true>(d, lp, h, c, kk, t, l, a, s, head, tp, lpv, st)
+                    : run_phases<T, true, false>(d, lp, h, c, kk, t, l, a, s, head, tp, lpv, st);
+    return turn ? run_phases<T, false, true>(d, lp, h, c, kk, t, l, a, s, head, tp, lpv, st)
+                : run_phases<T, false, false>(d, lp, h, c, kk, t, l, a, s, head, tp, lpv, st);
 }
 
 template <class T>
 int adjoint_gather_subcycle(const Dims &d, int64_t lp, const HaloFill &h, const FastConsts<T> &c,
                             const FastScalars<T> &k, double rhoSea, const TapeG<T> &t, const LamG<T> &l,
                             const Adj<T> &a, T *const scratch[N_SCRATCH], bool basal, bool turn, cudaStream_t st) {
-    Scr<T> s;
-    std::memcpy(&s, scratch, sizeof s);
-    const KT<T> kk = kt<T>(k, rhoSea);
-    if (basal)
-        return turn ? run_passes<T, true, true>(d, lp, h, c, kk, t, l, a, s, st)
-                    : run_passes<T, true, false>(d, lp, h, c, kk, t, l, a, s, st);
-    return turn ? run_passes<T, false, true>(d, lp, h, c, kk, t, l, a, s, st)
-                : run_passes<T, false, false>(d, lp, h, c, kk, t, l, a, s, st);
+    return phases<T>(d, lp, h, c, k, rhoSea, t, l, a, scratch, basal, turn, true, nullptr, nullptr, st);
+}
+
+template <class T>
+int adjoint_gather_chain(const Dims &d, int64_t lp, const HaloFill &h, const FastConsts<T> &c,
+                         const FastScalars<T> &k, double rhoSea, const TapeG<T> &t, const LamG<T> &l,
+                         const Adj<T> &a, T *const scratch[N_SCRATCH], bool basal, bool head,
+                         const TapeG<T> *t_prev, const LamG<T> *l_prev, cudaStream_t st) {
+    if ((t_prev == nullptr) != (l_prev == nullptr)) return VERIS_ERR_ARG;
+    return phases<T>(d, lp, h, c, k, rhoSea, t, l, a, scratch, basal, false, head, t_prev, l_prev, st);
 }
 
 // the per-cell water-drag sums of the whole sweep, by hemisphere: block sums in float64 (fixed
@@ -760,6 +889,10 @@ template int adjoint_gather_subcycle<float>(const Dims &, int64_t, const HaloFil
                                             const FastScalars<float> &, double, const TapeG<float> &,
                                             const LamG<float> &, const Adj<float> &, float *const[N_SCRATCH], bool,
                                             bool, cudaStream_t);
+template int adjoint_gather_chain<float>(const Dims &, int64_t, const HaloFill &, const FastConsts<float> &,
+                                         const FastScalars<float> &, double, const TapeG<float> &,
+                                         const LamG<float> &, const Adj<float> &, float *const[N_SCRATCH], bool,
+                                         bool, const TapeG<float> *, const LamG<float> *, cudaStream_t);
 
 }  // namespace adj
 
