@@ -434,8 +434,9 @@ int veris_evp_adjoint_f32(const VerisGrid *g, const VerisParams *p, const VerisF
 size_t veris_evp_adjoint_taped_workspace_bytes_f32(const VerisGrid *g, int32_t n_subcycles);
 /*
  * Form of the float32 EVP adjoint subcycle: 0 by grid size (the gather
- * passes from 2^19 padded cells up, where they are memory-bound; below, one
- * tile kernel per subcycle, which beats four to six latency-bound launches),
+ * passes from 2^16 padded cells up when reading a tape, from 2^19 when
+ * recomputing a segment, where they are memory-bound; below, one tile
+ * kernel per subcycle, which beats three to five latency-bound launches),
  * 1 the tile kernel, 2 the gather passes (without a turning angle the last
  * pass of each subcycle runs fused with the first of the subcycle before
  * it), 3 the gather passes each in its own launch (the same values as 2, bit

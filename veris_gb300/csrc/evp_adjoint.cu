@@ -652,9 +652,13 @@ static int copy_state(T *const dst[5], T *const src[5], size_t bytes, cudaStream
 // the float32 adjoint's form: 0 by grid size, 1 the tile kernel, 2 the gather passes, 3 the
 // gather passes with P4 and P1 of consecutive subcycles in separate launches
 static std::atomic<int> g_f32_form{0};
-// padded cells from which the float32 adjoint takes the gather passes (measured: 360 x 180
-// faster with the tile kernel, 3600 x 1800 with the passes)
+// padded cells from which the float32 adjoint takes the gather passes: a recomputed segment
+// (two more passes per subcycle) from 2^19 (measured: 360 x 180 faster with the tile kernel,
+// 3600 x 1800 with the passes), a tape with the walk's terms from 2^16 (360 x 180, 66,976
+// padded cells: 1-degree trajectory 3.53x its forward with the passes, 3.70x with the tile
+// kernel)
 constexpr int64_t F32_GATHER_CELLS = 1 << 19;
+constexpr int64_t F32_GATHER_CELLS_TAPED = 1 << 16;
 
 // tape != nullptr: the forward's subcycle states (slot k = after k
 // subcycles, 5 arrays per slot, plan field bytes each) replace the
@@ -674,7 +678,8 @@ static int evp_adjoint(const VerisGrid *g, const VerisParams *p, const VerisFiel
     // tile kernel on small ones (its one launch per subcycle beats four to six latency-bound ones)
     const int f32_form = g_f32_form.load(std::memory_order_relaxed);
     const bool gather = sizeof(T) == 8 || f32_form >= 2 ||
-                        (f32_form == 0 && (int64_t)d.NX * d.NY >= F32_GATHER_CELLS);
+                        (f32_form == 0 &&
+                         (int64_t)d.NX * d.NY >= (taped ? F32_GATHER_CELLS_TAPED : F32_GATHER_CELLS));
     Plan<T> pl;
     VERIS_REQUIRE(ws && wsb >= plan<T>(d, n, K, nullptr, &pl, taped), VERIS_ERR_WORKSPACE);
     plan<T>(d, n, K, static_cast<char *>(ws), &pl, taped);
