@@ -488,8 +488,9 @@ __global__ void __launch_bounds__(BX * BY) z_reverse_kernel(Dims d, int64_t lp, 
 // drag (veris/dynamics_routines.py:21-52), basal drag (:55-96) and the
 // Coriolis terms (veris/evp_solver.py:124-131)
 template <class T, bool BASAL, bool TURN>
-__global__ void __launch_bounds__(BX * BY) c_reverse_kernel(Dims d, int64_t lp, FastConsts<T> c, TapeG<T> t,
-                                                             LamG<T> l, Adj<T> a, KT<T> k, Scr<T> s) {
+__device__ __forceinline__ void c_reverse_body(const Dims &d, int64_t lp, const FastConsts<T> &c, const TapeG<T> &t,
+                                               const LamG<T> &l, const Adj<T> &a, const KT<T> &k,
+                                               const Scr<T> &s) {
     const int j = blockIdx.x * BX + threadIdx.x, i = blockIdx.y * BY + threadIdx.y;
     const bool act = i < d.NX && j < d.NY;
     const unsigned m = __ballot_sync(ALL, act);
@@ -599,6 +600,23 @@ __global__ void __launch_bounds__(BX * BY) c_reverse_kernel(Dims d, int64_t lp, 
             if (dragS != 0.f) atomicAdd(a.dragS, (double)dragS * k.wS);
         }
     }
+}
+
+template <class T, bool BASAL, bool TURN>
+__global__ void __launch_bounds__(BX * BY) c_reverse_kernel(Dims d, int64_t lp, FastConsts<T> c, TapeG<T> t,
+                                                             LamG<T> l, Adj<T> a, KT<T> k, Scr<T> s) {
+    c_reverse_body<T, BASAL, TURN>(d, lp, c, t, l, a, k, s);
+}
+
+// On a float32 grid of more CTAs than the GPU holds at once, eight CTAs per
+// SM (32 registers, 20-24 bytes spilled): the latency-bound pass gains more
+// from the resident warps than it loses to the spills (a 0.1-degree reverse
+// step 383.7 -> 375.1 ms); on a grid the GPU holds at once the spills would
+// only cost.
+template <class T, bool BASAL, bool TURN>
+__global__ void __launch_bounds__(BX * BY, 8) c_reverse_occ_kernel(Dims d, int64_t lp, FastConsts<T> c, TapeG<T> t,
+                                                                   LamG<T> l, Adj<T> a, KT<T> k, Scr<T> s) {
+    c_reverse_body<T, BASAL, TURN>(d, lp, c, t, l, a, k, s);
 }
 
 // e12's full adjoint at Z(i, j): its share through sigma12 plus
@@ -712,14 +730,11 @@ __global__ void __launch_bounds__(BX * BY) uv_gather_kernel(Dims d, int64_t lp, 
 // P1 of subcycle k - 1 reads there: they stay in registers, and the
 // ocean-velocity adjoints take one read-modify-write for both subcycles, in
 // the separate passes' order of additions.  t4, l4: subcycle k; t1, l1:
-// subcycle k - 1.  Six 256-thread CTAs per SM (40 registers, 8 bytes
-// spilled): the passes are latency-bound, and on 3600 x 1800 a reverse
-// step took 389.5 ms so, 401.2 ms with five CTAs per SM (48 registers, no
-// spill), 428.6 ms with four, 400.0 ms with the passes separate.
+// subcycle k - 1.
 template <class T, bool BASAL>
-__global__ void __launch_bounds__(BX * BY, 6) uv_link_kernel(Dims d, int64_t lp, HaloFill h, FastConsts<T> c,
-                                                           TapeG<T> t4, TapeG<T> t1, LamG<T> l4, LamG<T> l1,
-                                                           Adj<T> a, KT<T> k, Scr<T> s) {
+__device__ __forceinline__ void uv_link_body(const Dims &d, int64_t lp, const HaloFill &h, const FastConsts<T> &c,
+                                             const TapeG<T> &t4, const TapeG<T> &t1, const LamG<T> &l4,
+                                             const LamG<T> &l1, const Adj<T> &a, const KT<T> &k, const Scr<T> &s) {
     const int j = blockIdx.x * BX + threadIdx.x, i = blockIdx.y * BY + threadIdx.y;
     const bool act = i < d.NX && j < d.NY;
     const unsigned m = __ballot_sync(ALL, act);
@@ -759,7 +774,32 @@ __global__ void __launch_bounds__(BX * BY, 6) uv_link_kernel(Dims d, int64_t lp,
     p1_point<T, BASAL, false, true>(d, lp, c, t1, l1, a, k, s, m, i, j, LU, LV, luo, lvo);
 }
 
+template <class T, bool BASAL>
+__global__ void __launch_bounds__(BX * BY) uv_link_kernel(Dims d, int64_t lp, HaloFill h, FastConsts<T> c,
+                                                           TapeG<T> t4, TapeG<T> t1, LamG<T> l4, LamG<T> l1,
+                                                           Adj<T> a, KT<T> k, Scr<T> s) {
+    uv_link_body<T, BASAL>(d, lp, h, c, t4, t1, l4, l1, a, k, s);
+}
+
+// On a grid of more CTAs than the GPU holds at once, eight CTAs per SM (32
+// registers, spilling).  On 3600 x 1800 a reverse step took 400.0 ms with
+// the passes separate, 428.6 / 401.2 / 389.5 ms with the fused one at four
+// / five / six CTAs per SM, and with P3 at eight CTAs 375.1 ms at six,
+// 364.7 ms at eight.
+template <class T, bool BASAL>
+__global__ void __launch_bounds__(BX * BY, 8) uv_link_occ_kernel(Dims d, int64_t lp, HaloFill h, FastConsts<T> c,
+                                                                 TapeG<T> t4, TapeG<T> t1, LamG<T> l4, LamG<T> l1,
+                                                                 Adj<T> a, KT<T> k, Scr<T> s) {
+    uv_link_body<T, BASAL>(d, lp, h, c, t4, t1, l4, l1, a, k, s);
+}
+
 }  // namespace
+
+// padded cells from which the float32 passes P3 and P4+P1 run at eight CTAs
+// per SM (the *_occ_kernel forms; 2^19: 3600 x 1800 faster so; 360 x 180,
+// whose passes fit the GPU at once, slower: 1-degree trajectory 3.75x
+// against 3.53-3.60x)
+constexpr int64_t OCCUPY_CELLS = 1 << 19;
 
 // The passes of one subcycle in phases: head (the recomputed terms of a
 // tape without them, the basal coefficient, P1), body (P2, P3), tail (P4),
@@ -796,11 +836,20 @@ static int run_phases(const Dims &d, int64_t lp, const HaloFill &h, const FastCo
         uv_reverse_kernel<T, B, R><<<grd, blk, 0, st>>>(d, lp, h, c, tt, l, a, k, s);
     }
     z_reverse_kernel<T><<<grd, blk, 0, st>>>(d, lp, c, tt, l, k, s, t.del == nullptr);
-    c_reverse_kernel<T, B, R><<<grd, blk, 0, st>>>(d, lp, c, tt, l, a, k, s);
+    // float32 on a grid of more CTAs than the GPU holds: P3 and the fused pass at eight CTAs per SM
+    const bool occupy = sizeof(T) == 4 && (int64_t)d.NX * d.NY >= OCCUPY_CELLS;
+    if constexpr (sizeof(T) == 4) {
+        if (occupy) c_reverse_occ_kernel<T, B, R><<<grd, blk, 0, st>>>(d, lp, c, tt, l, a, k, s);
+        else c_reverse_kernel<T, B, R><<<grd, blk, 0, st>>>(d, lp, c, tt, l, a, k, s);
+    } else {
+        c_reverse_kernel<T, B, R><<<grd, blk, 0, st>>>(d, lp, c, tt, l, a, k, s);
+    }
     if (tp) {
         if constexpr (!R && sizeof(T) == 4) {
             pre_p1<T, B>(d, lp, c, k, *tp, s, grd, blk, st);
-            uv_link_kernel<T, B><<<grd, blk, 0, st>>>(d, lp, h, c, tt, with_terms(*tp, s), l, *lpv, a, k, s);
+            const TapeG<T> t1 = with_terms(*tp, s);
+            if (occupy) uv_link_occ_kernel<T, B><<<grd, blk, 0, st>>>(d, lp, h, c, tt, t1, l, *lpv, a, k, s);
+            else uv_link_kernel<T, B><<<grd, blk, 0, st>>>(d, lp, h, c, tt, t1, l, *lpv, a, k, s);
         }
     } else {
         uv_gather_kernel<T, B, R><<<grd, blk, 0, st>>>(d, lp, c, tt, l, a, k, s);
