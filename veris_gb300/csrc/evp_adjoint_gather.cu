@@ -20,6 +20,13 @@
 //       Coriolis, ocean and basal drag adjoints;
 //   P4  U and V points: the gathered velocity and ocean-velocity adjoints.
 //
+// In float32 without a turning angle, P4 of each subcycle and P1 of the
+// subcycle before it run as one pass (uv_link_kernel): what P4 gathers at a
+// point is what that P1 reads there.  On grids of more CTAs than the GPU
+// holds at once, the float32 P3 and the fused pass are bounded to 32
+// registers (eight CTAs per SM): latency-bound, they gain more from the
+// resident warps than they lose to spills.
+//
 // Every point is computed once, nothing is recomputed on rings and nothing
 // is accumulated with atomics (each input adjoint is written by the pass
 // that owns its position).  In float64 the forward's Delta, zeta and drag
